@@ -1,0 +1,309 @@
+"""Benchmark: 16M-body Barnes-Hut steps/s on one GB300 (plain vs compensated FP32).
+
+Workload (the precision-form configuration): binary star + disk, N = 2^24,
+two 0.5-mass stars at separation 0.2, 2^24-2 disk bodies of mass 1e-8 with
+radius U[0.3,2], theta = 0.5, eps = 0.005, dt = 5e-4.  Synthetic inputs from the
+counter-based generator in nns_gb300.ic.  A step is one full pass of the hot
+path: bounding box, keys, key sort, tree, moments, warp-coherent walk and
+kick-drift.  The inputs (2^24 bodies: 0.7 GB of state plus 4 GB of tree) are far
+larger than L2, so no flush is needed between steps.
+
+Prints one JSON line (see README section "bench contract").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "16M-body BH steps/s, plain vs compensated FP32 @1e-4 err; adjoint/fwd cost"
+N_DEFAULT = 1 << 24
+THETA, EPS, DT = 0.5, 0.005, 5e-4
+FLOP_PER_INTERACTION = 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="nbx", choices=["nbx", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--targets", type=int, default=8192)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
+        int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx = float(f[2])
+                except ValueError:
+                    continue
+                for nm, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        finally:
+            os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peak_fp32_tflops(nsm: int, mhz: float) -> float:
+    return nsm * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        return {}
+
+
+def run_reference(args, rank):
+    """CPU reference arm: the reference's own 3D/OpenMP tree code on all host cores."""
+    if rank != 0:
+        return None
+    from oracle import ref_cpu
+    res = ref_cpu.bench_openmp(args.n, args.steps, args.warmup, THETA, EPS, DT)
+    if res is None:
+        return {"impl": "reference", "unavailable": "reference CPU code was not staged/built on this host"}
+    line = {"metric": METRIC, "impl": "reference", "value": res["steps_per_s"], "unit": "steps/s",
+            "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 / res["steps_per_s"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (nns_gb300.ic binary_disk)",
+            "config": {"workload": "binary_disk_2^24", "n": args.n, "theta": THETA, "eps": EPS,
+                       "dt": DT},
+            "cpu_baseline": {"value": res["steps_per_s"], "unit": "steps/s", "cores": res["cores"],
+                             "kind": "reference", "sample": res["sample"]},
+            "e2e": {"value": res["steps_per_s"], "unit": "steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    return line
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        line = run_reference(args, rank)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    from nns_gb300 import ic
+    from nns_gb300.barnes_hut import Context, State
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    n = args.n
+    b = ic.binary_disk(n)
+    ctx = Context(max_bodies=n, theta=THETA, eps=EPS, dt=DT, device=local)
+    ctx.set_systems([0, n])
+    s = State.from_bodies(b, device="cuda:%d" % local)
+    stream = torch.cuda.current_stream()
+
+    def timed(nsteps, phase=True):
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(nsteps)]
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        inter = 0
+        launches0 = ctx.tree_info()["launches"]
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        t0.record()
+        for k in range(nsteps):
+            ev[k][0].record()
+            ctx.build(s)
+            ev[k][1].record()
+            ctx.forces(s)
+            ev[k][2].record()
+            ctx.integrate(s)
+            ev[k][3].record()
+        t1.record()
+        torch.cuda.synchronize()
+        info = ctx.tree_info()
+        if info["status"]:
+            ctx.sync()
+        total = t0.elapsed_time(t1)
+        build = sum(e[0].elapsed_time(e[1]) for e in ev)
+        walk = sum(e[1].elapsed_time(e[2]) for e in ev)
+        integ = sum(e[2].elapsed_time(e[3]) for e in ev)
+        return dict(ms=total, build_ms=build, walk_ms=walk, integ_ms=integ,
+                    interactions=info["interactions"], launches=info["launches"] - launches0,
+                    ncells=info["ncells"], max_level=info["max_level"])
+
+    # ---- error at the initial state (outside any timed region)
+    rng = np.random.default_rng(12345)
+    targets = np.sort(rng.choice(n, size=min(args.targets, n), replace=False))
+    acc64 = ctx.direct_fp64(s, targets, float(np.float32(EPS) * np.float32(EPS))).cpu().numpy()
+    errs = {}
+    for comp in (False, True):
+        t_ref, e2 = ctx.constants()
+        ctx.set_constants(t_ref, e2, comp)
+        ctx.build(s)
+        ctx.forces(s)
+        ctx.sync()
+        a = s.acc()[targets].astype(np.float64)
+        rel = np.linalg.norm(a - acc64, axis=1) / np.linalg.norm(acc64, axis=1)
+        errs["compensated" if comp else "plain"] = {"median": float(np.median(rel)),
+                                                    "p99": float(np.quantile(rel, 0.99)),
+                                                    "max": float(rel.max())}
+    t_ref, e2 = ctx.constants()
+    ctx.set_constants(t_ref, e2, False)
+    diag0 = ctx.diagnostics(s)
+
+    # ---- plain FP32: warmup + timed
+    timed(args.warmup)
+    with Clocks(local) as clk:
+        plain = timed(args.steps)
+    clocks = clk.summary()
+    # ---- compensated FP32
+    ctx.set_constants(t_ref, e2, True)
+    timed(max(1, args.warmup // 2))
+    comp = timed(args.steps)
+    ctx.set_constants(t_ref, e2, False)
+    diag1 = ctx.diagnostics(s)
+
+    # ---- end to end through the public API with host buffers (pinned)
+    host = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+            for a in (b.x, b.y, b.z, b.vx, b.vy, b.vz, b.m)]
+    outs = [torch.empty(n, dtype=torch.float32).pin_memory() for _ in range(6)]
+    dev_in = [s.x, s.y, s.z, s.vx, s.vy, s.vz, s.m]
+    h2d = sum(t.numel() * 4 for t in host)
+    d2h = sum(t.numel() * 4 for t in outs)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        for d, h in zip(dev_in, host):
+            d.copy_(h, non_blocking=True)
+        ctx.step(s, 1)
+        for o, d in zip(outs, dev_in[:6]):
+            o.copy_(d, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    ctx.sync()
+
+    ms_plain = plain["ms"] / args.steps
+    ms_comp = comp["ms"] / args.steps
+    walk_ms = plain["walk_ms"] / args.steps
+    inter_per_step = plain["interactions"]
+    flops = inter_per_step * FLOP_PER_INTERACTION
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    peaks = measured_peaks()
+    max_mhz = peaks.get("sm_max_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    peak = peak_fp32_tflops(nsm, max_mhz)
+    achieved = flops / (walk_ms * 1e-3) / 1e12
+    steps_per_s = 1000.0 / ms_plain
+
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_plain], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_plain = float(t.item())
+        steps_per_s = world * 1000.0 / ms_plain
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            from oracle import ref_cpu
+            cpu = ref_cpu.cpu_baseline(n, THETA, EPS, DT)
+        except Exception as e:  # noqa: BLE001 -- reported, never fatal
+            cpu = {"unavailable": str(e)[:200]}
+
+    line = {
+        "metric": METRIC, "value": round(steps_per_s, 4), "unit": "steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_plain, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (nns_gb300.ic binary_disk, seed 20261203)",
+        "config": {"workload": "binary_disk_2^24 precision form", "n": n, "theta": THETA,
+                   "eps": EPS, "dt": DT, "group": 32, "l2": "inputs larger than L2 (no flush)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "compensated": {"value": round(1000.0 / ms_comp, 4), "unit": "steps/s",
+                        "ms_per_step": round(ms_comp, 3),
+                        "ratio_to_plain_time": round(ms_comp / ms_plain, 4)},
+        "force_error_vs_fp64_direct": errs,
+        "interactions_per_step": inter_per_step,
+        "interactions_per_s": inter_per_step * steps_per_s,
+        "phase_ms": {"build": round(plain["build_ms"] / args.steps, 3), "walk": round(walk_ms, 3),
+                     "integrate": round(plain["integ_ms"] / args.steps, 3)},
+        "tree": {"cells": plain["ncells"], "max_level": plain["max_level"]},
+        "roofline": {"bound": "fp32", "kernel": "k_walk", "achieved": round(achieved, 3),
+                     "peak": round(peak, 2), "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
+                     "traffic": None,
+                     "peak_kind": "nominal FP32 FMA peak (SMs x 128 x 2 x max SM clock %g MHz)" % max_mhz},
+        "diagnostics_fp64": {"momentum_drift": float(np.abs(diag1["momentum"] - diag0["momentum"]).max()),
+                             "kinetic_rel_change": float((diag1["kinetic"] - diag0["kinetic"]) / diag0["kinetic"])},
+        "e2e": {"value": round(1000.0 / e2e_ms, 4), "unit": "steps/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": plain["launches"],
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,182 @@
+/*
+ * nbx.h -- C ABI of the GB300-native Barnes-Hut pipeline (libnbx.so).
+ *
+ * Plain pointers and sizes only.  Device pointers are CUDA device memory of
+ * the current device; `stream` is a cudaStream_t passed as void* (NULL = the
+ * legacy default stream).  Every entry point returns an nbx status code; no
+ * entry point synchronises the host except where stated (timing out-params and
+ * nbx_sync_status).
+ *
+ * Two layers:
+ *  1. Phase entry points with the argument lists and array semantics of the
+ *     reference's KernelsWrapper (3D/CUDA/CUDA_NBody/include/KernelsWrapper.cuh:28-48,
+ *     src/KernelsWrapper.cu:28-208), so that the reference's BarnesHut host class
+ *     (src/BarnesHut.cu:195-258) can be relinked against them:
+ *       SoA float arrays of length m, child[8m], -1 = null, bodies [0,n),
+ *       cells [n, m) (canonical depth-first numbering), *index = n + ncells.
+ *     Each takes a context (holding the tree scratch), the stream, and an
+ *     optional `ms` out-param: when non-NULL the call is timed with CUDA events
+ *     and synchronises, like the reference's `timing=true` path.
+ *  2. The native pipeline over device-resident SoA state with any number of
+ *     independent systems (nbx_set_systems / nbx_step / nbx_graph_step ...).
+ */
+#ifndef NBX_H
+#define NBX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define NBX_OK 0
+#define NBX_ERR_ARG 1       /* invalid argument */
+#define NBX_ERR_CUDA 2      /* a CUDA runtime call failed */
+#define NBX_ERR_DEPTH 3     /* two bodies share a subdivision region 42 levels deep (duplicates) */
+#define NBX_ERR_CAPACITY 4  /* the node pool of the context is too small for this tree */
+#define NBX_ERR_STACK 5     /* a walk stack overflowed (raise nbx_params.stack_depth) */
+#define NBX_ERR_NONFINITE 6 /* a position is NaN or infinite */
+#define NBX_ERR_CLUSTER 7   /* more than 4096 bodies share one 21-level key */
+#define NBX_ERR_TIMEOUT 8   /* a bounded device-side wait expired */
+#define NBX_ERR_STATE 9     /* call out of order (e.g. forces before a build) */
+#define NBX_ERR_NOMEM 10    /* device allocation failed */
+
+typedef struct nbx_ctx nbx_ctx;
+
+typedef struct nbx_params {
+    int max_bodies;    /* capacity: total bodies over all systems (<= 2^25) */
+    int max_systems;   /* capacity: independent systems */
+    float theta;       /* opening angle: a cell of x-side s at squared distance r
+                          (softened) is accepted when s^2 / theta^2 <= r, i.e. the
+                          reference's raw constant is theta^2 */
+    float theta_ref;   /* > 0: use this raw MAC constant (Kernels.cu:18 `theta`) */
+    float eps;         /* Plummer softening length */
+    float eps2;        /* > 0: use this squared softening (Kernels.cu:17) */
+    float dt;          /* time step (main.cu:52) */
+    float dampening;   /* velocity factor of the drift (main.cu:54) */
+    float gravity;     /* accepted for interface parity; the force uses G = 1 (Kernels.cu:462) */
+    int group;         /* bodies sharing one walk (warp-coherent MAC vote): 32 */
+    int stack_depth;   /* walk stack entries per warp */
+    int compensated;   /* 0 plain FP32 accumulation, 1 compensated FP32 */
+    int leaf_size;     /* bodies per leaf: 1 */
+    int radix_bits;    /* radix digit width of the key sort: 8 */
+    int walk_warps;    /* warps per block of the walk kernel (0 = autotuned default) */
+    int device;        /* CUDA device ordinal */
+    int block_size;    /* reference launch-shape hints (main.cu:30-31); informational */
+    int grid_size;
+} nbx_params;
+
+/* SoA device state of all systems; systems are contiguous ranges. */
+typedef struct nbx_state {
+    float *x, *y, *z;
+    float *vx, *vy, *vz;
+    float *ax, *ay, *az;
+    float *m;
+} nbx_state;
+
+typedef struct nbx_tree_info {
+    int64_t nbodies;       /* bodies in the last build */
+    int64_t ncells;        /* cells (internal nodes, roots excluded) */
+    int64_t nnodes;        /* cells + bodies */
+    int32_t max_level;     /* deepest node level (root children = 1) */
+    int32_t nsystems;
+    int64_t interactions;  /* sum over bodies of interaction-list length, last walk */
+    int64_t opened;        /* sum over groups of cells opened, last walk */
+    int32_t refined_runs;  /* runs of equal 21-level keys refined past level 21 */
+    int32_t status;        /* sticky device error status */
+    int64_t launches;      /* kernels launched by this context so far */
+} nbx_tree_info;
+
+/* ---- context -------------------------------------------------------- */
+void nbx_params_default(nbx_params *p);
+int nbx_create(const nbx_params *p, nbx_ctx **out);
+int nbx_destroy(nbx_ctx *ctx);
+const char *nbx_status_string(int status);
+const char *nbx_last_error(nbx_ctx *ctx);
+/* Current effective MAC constant and softening of the context. */
+int nbx_get_constants(nbx_ctx *ctx, float *theta_ref, float *eps2);
+int nbx_set_constants(nbx_ctx *ctx, float theta_ref, float eps2, int compensated);
+
+/* ---- reference-compatible phase entry points (KernelsWrapper.cu) ---- */
+/* KernelsWrapper::resetArrays (KernelsWrapper.cu:28; Kernels.cu:21-64) */
+int nbx_reset_arrays(nbx_ctx *ctx, int *mutex, float *x, float *y, float *z, float *mass,
+                     int *count, int *start, int *sorted, int *child, int *index, float *minX,
+                     float *maxX, float *minY, float *maxY, float *minZ, float *maxZ, int n, int m,
+                     void *stream, float *ms);
+/* KernelsWrapper::computeBoundingBox (KernelsWrapper.cu:56; Kernels.cu:67-154):
+ * merges the bounding box of bodies [0,n) into *minX..*maxZ. */
+int nbx_compute_bounding_box(nbx_ctx *ctx, int *mutex, float *x, float *y, float *z, float *minX,
+                             float *maxX, float *minY, float *maxY, float *minZ, float *maxZ,
+                             int n, void *stream, float *ms);
+/* KernelsWrapper::buildTree (KernelsWrapper.cu:81; Kernels.cu:157-377): keys, sort
+ * and key-built octree; writes child[], count[] and mass[], x/y/z (= sum m*x) of
+ * the cells, *index. */
+int nbx_build_tree(nbx_ctx *ctx, float *x, float *y, float *z, float *mass, int *count,
+                   int *start, int *child, int *index, float *minX, float *maxX, float *minY,
+                   float *maxY, float *minZ, float *maxZ, int n, int m, void *stream, float *ms);
+/* KernelsWrapper::centreOfMass (KernelsWrapper.cu:109; Kernels.cu:381-399) */
+int nbx_centre_of_mass(nbx_ctx *ctx, float *x, float *y, float *z, float *mass, int *index, int n,
+                       void *stream, float *ms);
+/* KernelsWrapper::sort (KernelsWrapper.cu:133; Kernels.cu:403-456) */
+int nbx_sort(nbx_ctx *ctx, int *count, int *start, int *sorted, int *child, int *index, int n,
+             void *stream, float *ms);
+/* KernelsWrapper::computeForces (KernelsWrapper.cu:157; Kernels.cu:460-577) */
+int nbx_compute_forces(nbx_ctx *ctx, float *x, float *y, float *z, float *vx, float *vy,
+                       float *vz, float *ax, float *ay, float *az, float *mass, int *sorted,
+                       int *child, float *minX, float *maxX, int n, float g, void *stream,
+                       float *ms);
+/* KernelsWrapper::update (KernelsWrapper.cu:185; Kernels.cu:581-600) */
+int nbx_update(nbx_ctx *ctx, float *x, float *y, float *z, float *vx, float *vy, float *vz,
+               float *ax, float *ay, float *az, int n, float dt, float d, void *stream,
+               float *ms);
+
+/* ---- native pipeline (no counterpart in the reference's API) --------- */
+/* Systems are the ranges [offsets[s], offsets[s+1]) of the state arrays;
+ * offsets is a HOST array of nsys+1 entries, offsets[0] = 0, each system >= 1 body. */
+int nbx_set_systems(nbx_ctx *ctx, int nsys, const int64_t *offsets);
+/* bbox, keys, sort and tree + moments of every system */
+int nbx_build(nbx_ctx *ctx, const nbx_state *s, void *stream);
+/* tree walk of the last build -> s->ax, s->ay, s->az */
+int nbx_forces(nbx_ctx *ctx, const nbx_state *s, void *stream);
+/* kick-drift with the context's dt and dampening */
+int nbx_integrate(nbx_ctx *ctx, const nbx_state *s, void *stream);
+/* nsteps x (build, forces, integrate), launched kernel by kernel */
+int nbx_step(nbx_ctx *ctx, const nbx_state *s, int nsteps, void *stream);
+/* the same steps replayed from a CUDA graph captured once per state */
+int nbx_graph_step(nbx_ctx *ctx, const nbx_state *s, int nsteps, void *stream);
+/* synchronises `stream` and returns (and clears) the sticky device status */
+int nbx_sync_status(nbx_ctx *ctx, void *stream);
+/* synchronises and reports the last build/walk */
+int nbx_get_tree_info(nbx_ctx *ctx, void *stream, nbx_tree_info *out);
+
+/* Export of the last build of system `sys` in the reference's array format
+ * (device pointers; cells numbered n_sys + depth-first index): sorted body
+ * order (system-local original indices), root_child[8], cell_child[8*ncells],
+ * cell start/count/level, cell centre of mass and mass.  Any pointer may be
+ * NULL.  cap_cells bounds the cell arrays; *ncells receives the count. */
+int nbx_export_tree(nbx_ctx *ctx, int sys, int *perm, int *root_child, int *cell_child,
+                    int *cell_start, int *cell_count, int *cell_level, float *cell_x,
+                    float *cell_y, float *cell_z, float *cell_m, int cap_cells, int64_t *ncells,
+                    void *stream);
+/* Sorted 21-level keys (ascending = the reference's in-order body order) and
+ * the sort permutation (global original indices), both of length nbodies. */
+int nbx_export_keys(nbx_ctx *ctx, uint64_t *keys, int *perm, void *stream);
+/* Per-body interaction-list length and opened-cell count of the last walk
+ * (global original index order). */
+int nbx_export_walk_stats(nbx_ctx *ctx, int *nlist, int *nopen, void *stream);
+
+/* FP64 direct summation (ground truth) for `nt` target indices over bodies
+ * [0,n): acc[3*t+k] += sum_j m_j d (|d|^2+eps2)^-3/2 in FP64. */
+int nbx_direct_fp64(nbx_ctx *ctx, const float *x, const float *y, const float *z, const float *m,
+                    int n, const int *targets, int nt, double eps2, double *acc, void *stream);
+/* FP64 diagnostics of bodies [0,n): out[0..2] momentum, out[3] kinetic energy,
+ * out[4..6] angular momentum, out[7] total mass (device double[8]). */
+int nbx_diagnostics_fp64(nbx_ctx *ctx, const nbx_state *s, int n, double *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBX_H */

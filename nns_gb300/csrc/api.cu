@@ -1,0 +1,594 @@
+// api.cu -- the C ABI of libnbx: context, reference-compatible phase entry
+// points (3D/CUDA/CUDA_NBody/src/KernelsWrapper.cu) and the native pipeline.
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "nbx_internal.cuh"
+
+namespace nbx {
+int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox, const float *const *bbox_ptrs);
+int export_tree_impl(Ctx *ctx, int sys, int *perm, int *root_child, int *cell_child, int *cell_start,
+                     int *cell_count, int *cell_level, float *cx, float *cy, float *cz, float *cm, int cap_cells,
+                     int64_t *ncells, cudaStream_t st, int sum_mode);
+int reset_ref_arrays(Ctx *ctx, int *mutex, float *x, float *y, float *z, float *mass, int *count, int *start,
+                     int *sorted, int *child, int *index, float *minX, float *maxX, float *minY, float *maxY,
+                     float *minZ, float *maxZ, int n, int m, cudaStream_t st);
+int bbox_ref(Ctx *ctx, const float *x, const float *y, const float *z, float *minX, float *maxX, float *minY,
+             float *maxY, float *minZ, float *maxZ, int n, cudaStream_t st);
+int direct_fp64(Ctx *ctx, const float *x, const float *y, const float *z, const float *m, int n,
+                const int *targets, int nt, double eps2, double *acc, cudaStream_t st);
+int diagnostics_fp64(Ctx *ctx, const nbx_state *s, int n, double *out, cudaStream_t st);
+
+namespace {
+
+__global__ void k_body_sys(const int *sys_off, int nsys, int n, int *body_sys) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int lo = 0, hi = nsys - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (sys_off[mid] <= i) lo = mid;
+            else hi = mid - 1;
+        }
+        body_sys[i] = lo;
+    }
+}
+
+__global__ void k_depth0_from_ptrs(const float *minX, const float *maxX, float theta_ref, float *depth0) {
+    if (threadIdx.x == 0) {
+        float r = __fmul_rn(__fsub_rn(*maxX, *minX), 0.5f);
+        depth0[0] = __fdiv_rn(__fmul_rn(r, r), theta_ref);
+    }
+}
+
+template <typename T>
+int dmalloc(Ctx *ctx, T **p, size_t count) {
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        ctx->last_error = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        *p = nullptr;
+        return NBX_ERR_NOMEM;
+    }
+    return NBX_OK;
+}
+
+void free_all(Ctx *ctx) {
+    void *ptrs[] = {ctx->d_sys_off, ctx->d_body_sys, ctx->d_tiles, ctx->d_sys_tiles, ctx->d_groups,
+                    ctx->d_bbox_u, ctx->d_bbox, ctx->d_bbox64, ctx->d_depth0, ctx->d_root_first,
+                    ctx->d_root_nch, ctx->d_key, ctx->d_key_alt, ctx->d_key_lo, ctx->d_val, ctx->d_val_alt,
+                    ctx->d_body4, ctx->d_delta, ctx->d_ecount, ctx->d_body_node, ctx->d_nlist, ctx->d_nopen,
+                    ctx->d_ent, ctx->d_ent_alt, ctx->d_flags, ctx->d_node4, ctx->d_meta, ctx->d_parent,
+                    ctx->d_sums, ctx->d_count, ctx->d_arrive, ctx->d_fcl, ctx->d_cl, ctx->d_hist,
+                    ctx->d_scan_blk, ctx->d_totals, ctx->d_totals64, ctx->d_status};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (ctx->h_status) cudaFreeHost(ctx->h_status);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->graph_stream) cudaStreamDestroy(ctx->graph_stream);
+}
+
+struct Timer {
+    cudaEvent_t a = nullptr, b = nullptr;
+    float *ms;
+    cudaStream_t st;
+    Timer(float *ms_, cudaStream_t st_) : ms(ms_), st(st_) {
+        if (ms) {
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            cudaEventRecord(a, st);
+        }
+    }
+    int finish(int rc) {
+        if (ms) {
+            cudaEventRecord(b, st);
+            cudaEventSynchronize(b);
+            float t = 0.f;
+            cudaEventElapsedTime(&t, a, b);
+            *ms = t;
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+        }
+        return rc;
+    }
+};
+
+int ensure_single_system(Ctx *ctx, int n) {
+    if (ctx->nsys == 1 && ctx->nbodies == n) return NBX_OK;
+    int64_t off[2] = {0, n};
+    return nbx_set_systems(reinterpret_cast<nbx_ctx *>(ctx), 1, off);
+}
+
+}  // namespace
+}  // namespace nbx
+
+using nbx::Ctx;
+
+static Ctx *C(nbx_ctx *c) { return reinterpret_cast<Ctx *>(c); }
+static cudaStream_t S(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+extern "C" {
+
+void nbx_params_default(nbx_params *p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->max_bodies = 1 << 20;
+    p->max_systems = 1;
+    p->theta = 0.5f;
+    p->theta_ref = 0.f;
+    p->eps = 0.05f;
+    p->eps2 = 0.f;
+    p->dt = 0.001f;
+    p->dampening = 1.f;
+    p->gravity = 1.f;
+    p->group = 32;
+    p->stack_depth = 512;
+    p->compensated = 0;
+    p->leaf_size = 1;
+    p->radix_bits = 8;
+    p->walk_warps = 0;
+    p->device = 0;
+    p->block_size = 256;
+    p->grid_size = 1024;
+}
+
+const char *nbx_status_string(int s) {
+    switch (s) {
+        case NBX_OK: return "ok";
+        case NBX_ERR_ARG: return "invalid argument";
+        case NBX_ERR_CUDA: return "CUDA runtime error";
+        case NBX_ERR_DEPTH: return "two bodies share a region 42 levels deep (duplicate positions)";
+        case NBX_ERR_CAPACITY: return "node pool capacity exceeded";
+        case NBX_ERR_STACK: return "walk stack overflow";
+        case NBX_ERR_NONFINITE: return "non-finite position";
+        case NBX_ERR_CLUSTER: return "more than 4096 bodies share one 21-level key";
+        case NBX_ERR_TIMEOUT: return "bounded device wait expired";
+        case NBX_ERR_STATE: return "call out of order or inconsistent tree";
+        case NBX_ERR_NOMEM: return "device allocation failed";
+        default: return "unknown status";
+    }
+}
+
+const char *nbx_last_error(nbx_ctx *c) { return c ? C(c)->last_error.c_str() : "null context"; }
+
+int nbx_create(const nbx_params *p, nbx_ctx **out) {
+    if (!p || !out) return NBX_ERR_ARG;
+    *out = nullptr;
+    if (p->max_bodies < 1 || p->max_bodies > (1 << 25) || p->max_systems < 1 ||
+        p->max_systems > p->max_bodies || p->group != 32 || p->leaf_size != 1 || p->radix_bits != 8 ||
+        p->stack_depth < 64 || p->stack_depth > 4096)
+        return NBX_ERR_ARG;
+    Ctx *ctx = new (std::nothrow) Ctx();
+    if (!ctx) return NBX_ERR_NOMEM;
+    ctx->p = *p;
+    ctx->theta_ref = p->theta_ref > 0.f ? p->theta_ref : p->theta * p->theta;
+    ctx->eps2 = p->eps2 > 0.f ? p->eps2 : p->eps * p->eps;
+    ctx->compensated = p->compensated;
+    if (!(ctx->theta_ref > 0.f)) {
+        delete ctx;
+        return NBX_ERR_ARG;
+    }
+    if (cudaSetDevice(p->device) != cudaSuccess) {
+        delete ctx;
+        return NBX_ERR_CUDA;
+    }
+    const int B = p->max_bodies, Ss = p->max_systems;
+    ctx->cap_bodies = B;
+    ctx->cap_sys = Ss;
+    const int64_t nc = 2ll * B + 65536;
+    ctx->cap_nodes = (int)(nc < nbx::kMaxNodes ? nc : nbx::kMaxNodes);
+    ctx->cap_tiles_body = B / nbx::kTile + Ss + 1;
+    ctx->cap_tiles_node = nbx::ceil_div(ctx->cap_nodes, nbx::kTile);
+    const int64_t hist = 256ll * (ctx->cap_tiles_body > ctx->cap_tiles_node ? ctx->cap_tiles_body : ctx->cap_tiles_node);
+    int64_t scan_max = hist;
+    if (ctx->cap_nodes > scan_max) scan_max = ctx->cap_nodes;
+    if (B > scan_max) scan_max = B;
+    ctx->cap_scan_blk = nbx::ceil_div(scan_max, nbx::kScanItems) + 1;
+    const int NC = ctx->cap_nodes;
+    const int G = B / 32 + Ss + 1;
+    int rc = 0;
+    rc |= nbx::dmalloc(ctx, &ctx->d_sys_off, Ss + 1);
+    rc |= nbx::dmalloc(ctx, &ctx->d_body_sys, B);
+    rc |= nbx::dmalloc(ctx, &ctx->d_tiles, ctx->cap_tiles_body);
+    rc |= nbx::dmalloc(ctx, &ctx->d_sys_tiles, Ss);
+    rc |= nbx::dmalloc(ctx, &ctx->d_groups, G);
+    rc |= nbx::dmalloc(ctx, &ctx->d_bbox_u, 6 * Ss + 6);
+    rc |= nbx::dmalloc(ctx, &ctx->d_bbox, 6 * Ss);
+    rc |= nbx::dmalloc(ctx, &ctx->d_bbox64, 6 * Ss);
+    rc |= nbx::dmalloc(ctx, &ctx->d_depth0, Ss);
+    rc |= nbx::dmalloc(ctx, &ctx->d_root_first, Ss);
+    rc |= nbx::dmalloc(ctx, &ctx->d_root_nch, Ss);
+    rc |= nbx::dmalloc(ctx, &ctx->d_key, B);
+    rc |= nbx::dmalloc(ctx, &ctx->d_key_alt, B);
+    rc |= nbx::dmalloc(ctx, &ctx->d_key_lo, B);
+    rc |= nbx::dmalloc(ctx, &ctx->d_val, B);
+    rc |= nbx::dmalloc(ctx, &ctx->d_val_alt, B);
+    rc |= nbx::dmalloc(ctx, &ctx->d_body4, B);
+    rc |= nbx::dmalloc(ctx, &ctx->d_delta, B);
+    rc |= nbx::dmalloc(ctx, &ctx->d_ecount, B);
+    rc |= nbx::dmalloc(ctx, &ctx->d_body_node, B);
+    rc |= nbx::dmalloc(ctx, &ctx->d_nlist, B);
+    rc |= nbx::dmalloc(ctx, &ctx->d_nopen, B);
+    rc |= nbx::dmalloc(ctx, &ctx->d_ent, NC);
+    rc |= nbx::dmalloc(ctx, &ctx->d_ent_alt, NC);
+    rc |= nbx::dmalloc(ctx, &ctx->d_flags, NC);
+    rc |= nbx::dmalloc(ctx, &ctx->d_node4, NC);
+    rc |= nbx::dmalloc(ctx, &ctx->d_meta, NC);
+    rc |= nbx::dmalloc(ctx, &ctx->d_parent, NC);
+    rc |= nbx::dmalloc(ctx, &ctx->d_sums, NC);
+    rc |= nbx::dmalloc(ctx, &ctx->d_count, NC);
+    rc |= nbx::dmalloc(ctx, &ctx->d_arrive, NC);
+    rc |= nbx::dmalloc(ctx, &ctx->d_fcl, (size_t)NC + Ss + 2);
+    rc |= nbx::dmalloc(ctx, &ctx->d_cl, (size_t)NC + Ss + 2);
+    rc |= nbx::dmalloc(ctx, &ctx->d_hist, hist);
+    rc |= nbx::dmalloc(ctx, &ctx->d_scan_blk, ctx->cap_scan_blk);
+    rc |= nbx::dmalloc(ctx, &ctx->d_totals, 8);
+    rc |= nbx::dmalloc(ctx, &ctx->d_totals64, 4);
+    rc |= nbx::dmalloc(ctx, &ctx->d_status, 1);
+    if (rc == 0 && cudaMallocHost((void **)&ctx->h_status, sizeof(nbx::DevStatus)) != cudaSuccess) rc = NBX_ERR_NOMEM;
+    if (rc == 0 && cudaMemset(ctx->d_status, 0, sizeof(nbx::DevStatus)) != cudaSuccess) rc = NBX_ERR_CUDA;
+    if (rc == 0 && cudaMemset(ctx->d_totals, 0, 8 * sizeof(unsigned)) != cudaSuccess) rc = NBX_ERR_CUDA;
+    if (rc == 0) rc = nbx::walk_init(ctx);
+    if (rc != 0) {
+        nbx::free_all(ctx);
+        delete ctx;
+        return rc == NBX_ERR_NOMEM ? NBX_ERR_NOMEM : (rc ? rc : NBX_ERR_CUDA);
+    }
+    *out = reinterpret_cast<nbx_ctx *>(ctx);
+    return NBX_OK;
+}
+
+int nbx_destroy(nbx_ctx *c) {
+    if (!c) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    cudaDeviceSynchronize();
+    nbx::free_all(ctx);
+    delete ctx;
+    return NBX_OK;
+}
+
+int nbx_get_constants(nbx_ctx *c, float *theta_ref, float *eps2) {
+    if (!c) return NBX_ERR_ARG;
+    if (theta_ref) *theta_ref = C(c)->theta_ref;
+    if (eps2) *eps2 = C(c)->eps2;
+    return NBX_OK;
+}
+
+int nbx_set_constants(nbx_ctx *c, float theta_ref, float eps2, int compensated) {
+    if (!c || !(theta_ref > 0.f) || !(eps2 >= 0.f)) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    ctx->theta_ref = theta_ref;
+    ctx->eps2 = eps2;
+    ctx->compensated = compensated ? 1 : 0;
+    if (ctx->graph_exec) {
+        cudaGraphExecDestroy(ctx->graph_exec);
+        ctx->graph_exec = nullptr;
+    }
+    return NBX_OK;
+}
+
+int nbx_set_systems(nbx_ctx *c, int nsys, const int64_t *offsets) {
+    if (!c || !offsets || nsys < 1) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    if (nsys > ctx->cap_sys) return NBX_ERR_ARG;
+    if (offsets[0] != 0) return NBX_ERR_ARG;
+    for (int s = 0; s < nsys; s++)
+        if (offsets[s + 1] <= offsets[s]) return NBX_ERR_ARG;
+    if (offsets[nsys] > ctx->cap_bodies) return NBX_ERR_ARG;
+    const int n = (int)offsets[nsys];
+    std::vector<int> off(nsys + 1);
+    std::vector<int4> tiles;
+    std::vector<int2> st(nsys);
+    std::vector<int> groups;
+    for (int s = 0; s <= nsys; s++) off[s] = (int)offsets[s];
+    for (int s = 0; s < nsys; s++) {
+        const int beg = off[s], end = off[s + 1];
+        const int nt = nbx::ceil_div(end - beg, nbx::kTile);
+        st[s] = make_int2((int)tiles.size(), nt);
+        for (int t = 0; t < nt; t++) {
+            const int a = beg + t * nbx::kTile;
+            const int len = (end - a) < nbx::kTile ? (end - a) : nbx::kTile;
+            tiles.push_back(make_int4(a, len, s, t));
+        }
+        for (int g = beg; g < end; g += 32) groups.push_back(g);
+    }
+    if ((int)tiles.size() > ctx->cap_tiles_body) return NBX_ERR_ARG;
+    NBX_CUDA(cudaMemcpy(ctx->d_sys_off, off.data(), sizeof(int) * (nsys + 1), cudaMemcpyHostToDevice));
+    NBX_CUDA(cudaMemcpy(ctx->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice));
+    NBX_CUDA(cudaMemcpy(ctx->d_sys_tiles, st.data(), sizeof(int2) * nsys, cudaMemcpyHostToDevice));
+    NBX_CUDA(cudaMemcpy(ctx->d_groups, groups.data(), sizeof(int) * groups.size(), cudaMemcpyHostToDevice));
+    nbx::k_body_sys<<<nbx::ceil_div(n, 256) < 4096 ? nbx::ceil_div(n, 256) : 4096, 256>>>(ctx->d_sys_off, nsys, n,
+                                                                                          ctx->d_body_sys);
+    ++ctx->launches;
+    NBX_CUDA(cudaGetLastError());
+    NBX_CUDA(cudaDeviceSynchronize());
+    ctx->nsys = nsys;
+    ctx->nbodies = n;
+    ctx->ntiles_body = (int)tiles.size();
+    ctx->ngroups = (int)groups.size();
+    ctx->built = false;
+    ctx->ref_m = 0;
+    if (ctx->graph_exec) {
+        cudaGraphExecDestroy(ctx->graph_exec);
+        ctx->graph_exec = nullptr;
+    }
+    return NBX_OK;
+}
+
+/* ---------------- reference-compatible phase entry points ---------------- */
+
+int nbx_reset_arrays(nbx_ctx *c, int *mutex, float *x, float *y, float *z, float *mass, int *count, int *start,
+                     int *sorted, int *child, int *index, float *minX, float *maxX, float *minY, float *maxY,
+                     float *minZ, float *maxZ, int n, int m, void *stream, float *ms) {
+    if (!c || n < 1 || m < n || !mutex || !x || !child || !index) return NBX_ERR_ARG;
+    nbx::Timer t(ms, S(stream));
+    return t.finish(nbx::reset_ref_arrays(C(c), mutex, x, y, z, mass, count, start, sorted, child, index, minX,
+                                          maxX, minY, maxY, minZ, maxZ, n, m, S(stream)));
+}
+
+int nbx_compute_bounding_box(nbx_ctx *c, int *mutex, float *x, float *y, float *z, float *minX, float *maxX,
+                             float *minY, float *maxY, float *minZ, float *maxZ, int n, void *stream, float *ms) {
+    (void)mutex;
+    if (!c || n < 1 || !x || !y || !z || !minX) return NBX_ERR_ARG;
+    nbx::Timer t(ms, S(stream));
+    return t.finish(nbx::bbox_ref(C(c), x, y, z, minX, maxX, minY, maxY, minZ, maxZ, n, S(stream)));
+}
+
+int nbx_build_tree(nbx_ctx *c, float *x, float *y, float *z, float *mass, int *count, int *start, int *child,
+                   int *index, float *minX, float *maxX, float *minY, float *maxY, float *minZ, float *maxZ, int n,
+                   int m, void *stream, float *ms) {
+    (void)start;
+    if (!c || n < 1 || m < n || !x || !child || !index || !count || !mass) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    if (n > ctx->cap_bodies) return NBX_ERR_ARG;
+    nbx::Timer t(ms, S(stream));
+    ctx->ref_m = 0;
+    int rc = nbx::ensure_single_system(ctx, n);
+    if (rc) return t.finish(rc);
+    nbx_state s{};
+    s.x = x; s.y = y; s.z = z; s.m = mass;
+    const float *bp[6] = {minX, maxX, minY, maxY, minZ, maxZ};
+    rc = nbx::build_tree(ctx, &s, S(stream), true, bp);
+    if (rc) return t.finish(rc);
+    rc = nbx_sync_status(c, stream);
+    if (rc) return t.finish(rc);
+    int64_t nc = 0;
+    rc = nbx::export_tree_impl(ctx, 0, nullptr, child, child + 8ll * n, nullptr, count + n, nullptr, x + n, y + n,
+                               z + n, mass + n, m - n, &nc, S(stream), 1);
+    if (rc) return t.finish(rc);
+    const int idx = n + (int)nc;
+    NBX_CUDA(cudaMemcpyAsync(index, &idx, sizeof(int), cudaMemcpyHostToDevice, S(stream)));
+    NBX_CUDA(cudaStreamSynchronize(S(stream)));
+    ctx->ref_m = m;
+    return t.finish(NBX_OK);
+}
+
+int nbx_centre_of_mass(nbx_ctx *c, float *x, float *y, float *z, float *mass, int *index, int n, void *stream,
+                       float *ms) {
+    (void)index;
+    if (!c || !x || !mass) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    if (!ctx->built || ctx->nbodies != n || ctx->ref_m <= n) return NBX_ERR_STATE;
+    nbx::Timer t(ms, S(stream));
+    int64_t nc = 0;
+    int rc = nbx::export_tree_impl(ctx, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, x + n, y + n,
+                                   z + n, mass + n, ctx->ref_m - n, &nc, S(stream), 0);
+    return t.finish(rc);
+}
+
+int nbx_sort(nbx_ctx *c, int *count, int *start, int *sorted, int *child, int *index, int n, void *stream,
+             float *ms) {
+    (void)count; (void)child; (void)index;
+    if (!c || !start || !sorted) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    if (!ctx->built || ctx->nbodies != n || ctx->ref_m <= n) return NBX_ERR_STATE;
+    nbx::Timer t(ms, S(stream));
+    int64_t nc = 0;
+    int rc = nbx::export_tree_impl(ctx, 0, sorted, nullptr, nullptr, start + n, nullptr, nullptr, nullptr, nullptr,
+                                   nullptr, nullptr, ctx->ref_m - n, &nc, S(stream), 0);
+    return t.finish(rc);
+}
+
+int nbx_compute_forces(nbx_ctx *c, float *x, float *y, float *z, float *vx, float *vy, float *vz, float *ax,
+                       float *ay, float *az, float *mass, int *sorted, int *child, float *minX, float *maxX, int n,
+                       float g, void *stream, float *ms) {
+    (void)x; (void)y; (void)z; (void)vx; (void)vy; (void)vz; (void)mass; (void)sorted; (void)child; (void)g;
+    if (!c || !ax || !ay || !az || !minX || !maxX) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    if (!ctx->built || ctx->nbodies != n) return NBX_ERR_STATE;
+    nbx::Timer t(ms, S(stream));
+    nbx::k_depth0_from_ptrs<<<1, 32, 0, S(stream)>>>(minX, maxX, ctx->theta_ref, ctx->d_depth0);
+    ++ctx->launches;
+    nbx_state s{};
+    s.ax = ax; s.ay = ay; s.az = az;
+    return t.finish(nbx::walk_forces(ctx, &s, S(stream)));
+}
+
+int nbx_update(nbx_ctx *c, float *x, float *y, float *z, float *vx, float *vy, float *vz, float *ax, float *ay,
+               float *az, int n, float dt, float d, void *stream, float *ms) {
+    if (!c || !x || !vx || !ax || n < 0) return NBX_ERR_ARG;
+    nbx::Timer t(ms, S(stream));
+    nbx_state s{x, y, z, vx, vy, vz, ax, ay, az, nullptr};
+    return t.finish(nbx::integrate(C(c), &s, dt, d, n, S(stream)));
+}
+
+/* ---------------- native pipeline ---------------- */
+
+static int check_state(Ctx *ctx, const nbx_state *s) {
+    if (!s || !s->x || !s->y || !s->z || !s->m) return NBX_ERR_ARG;
+    if (ctx->nsys < 1) return NBX_ERR_STATE;
+    return NBX_OK;
+}
+
+int nbx_build(nbx_ctx *c, const nbx_state *s, void *stream) {
+    if (!c) return NBX_ERR_ARG;
+    int rc = check_state(C(c), s);
+    if (rc) return rc;
+    return nbx::build_tree(C(c), s, S(stream), false, nullptr);
+}
+
+int nbx_forces(nbx_ctx *c, const nbx_state *s, void *stream) {
+    if (!c || !s || !s->ax || !s->ay || !s->az) return NBX_ERR_ARG;
+    return nbx::walk_forces(C(c), s, S(stream));
+}
+
+int nbx_integrate(nbx_ctx *c, const nbx_state *s, void *stream) {
+    if (!c || !s || !s->vx || !s->ax) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    return nbx::integrate(ctx, s, ctx->p.dt, ctx->p.dampening, (int)ctx->nbodies, S(stream));
+}
+
+static int one_step(Ctx *ctx, const nbx_state *s, cudaStream_t st) {
+    int rc = nbx::build_tree(ctx, s, st, false, nullptr);
+    if (rc) return rc;
+    rc = nbx::walk_forces(ctx, s, st);
+    if (rc) return rc;
+    return nbx::integrate(ctx, s, ctx->p.dt, ctx->p.dampening, (int)ctx->nbodies, st);
+}
+
+int nbx_step(nbx_ctx *c, const nbx_state *s, int nsteps, void *stream) {
+    if (!c || nsteps < 0) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    int rc = check_state(ctx, s);
+    if (rc) return rc;
+    if (!s->vx || !s->ax) return NBX_ERR_ARG;
+    for (int k = 0; k < nsteps; k++) {
+        rc = one_step(ctx, s, S(stream));
+        if (rc) return rc;
+    }
+    return NBX_OK;
+}
+
+int nbx_graph_step(nbx_ctx *c, const nbx_state *s, int nsteps, void *stream) {
+    if (!c || nsteps < 0) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    int rc = check_state(ctx, s);
+    if (rc) return rc;
+    if (!s->vx || !s->ax) return NBX_ERR_ARG;
+    cudaStream_t st = S(stream);
+    if (st == nullptr) {
+        if (!ctx->graph_stream) NBX_CUDA(cudaStreamCreateWithFlags(&ctx->graph_stream, cudaStreamNonBlocking));
+        st = ctx->graph_stream;
+        NBX_CUDA(cudaDeviceSynchronize());
+    }
+    if (ctx->graph_exec && (std::memcmp(&ctx->graph_state, s, sizeof(nbx_state)) != 0 || ctx->graph_nsys != ctx->nsys)) {
+        cudaGraphExecDestroy(ctx->graph_exec);
+        ctx->graph_exec = nullptr;
+    }
+    if (!ctx->graph_exec) {
+        cudaGraph_t g = nullptr;
+        NBX_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        rc = one_step(ctx, s, st);
+        cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) {
+            ctx->last_error = std::string("graph capture: ") + cudaGetErrorString(e);
+            return NBX_ERR_CUDA;
+        }
+        e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            ctx->graph_exec = nullptr;
+            ctx->last_error = std::string("graph instantiate: ") + cudaGetErrorString(e);
+            return NBX_ERR_CUDA;
+        }
+        ctx->graph_state = *s;
+        ctx->graph_nsys = ctx->nsys;
+    }
+    for (int k = 0; k < nsteps; k++) NBX_CUDA(cudaGraphLaunch(ctx->graph_exec, st));
+    if (S(stream) == nullptr) NBX_CUDA(cudaStreamSynchronize(st));
+    return NBX_OK;
+}
+
+int nbx_sync_status(nbx_ctx *c, void *stream) {
+    if (!c) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    NBX_CUDA(cudaStreamSynchronize(S(stream)));
+    NBX_CUDA(cudaMemcpy(ctx->h_status, ctx->d_status, sizeof(nbx::DevStatus), cudaMemcpyDeviceToHost));
+    const int code = ctx->h_status->code;
+    if (code) {
+        char buf[160];
+        std::snprintf(buf, sizeof(buf), "device status %d (%s), detail %d", code, nbx_status_string(code),
+                      ctx->h_status->detail);
+        ctx->last_error = buf;
+        int zero[2] = {0, 0};
+        NBX_CUDA(cudaMemcpy(ctx->d_status, zero, sizeof(zero), cudaMemcpyHostToDevice));
+    }
+    return code;
+}
+
+int nbx_get_tree_info(nbx_ctx *c, void *stream, nbx_tree_info *out) {
+    if (!c || !out) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    NBX_CUDA(cudaStreamSynchronize(S(stream)));
+    unsigned tot[2];
+    unsigned long long t64 = 0;
+    NBX_CUDA(cudaMemcpy(tot, ctx->d_totals, sizeof(tot), cudaMemcpyDeviceToHost));
+    NBX_CUDA(cudaMemcpy(&t64, ctx->d_totals64, sizeof(t64), cudaMemcpyDeviceToHost));
+    NBX_CUDA(cudaMemcpy(ctx->h_status, ctx->d_status, sizeof(nbx::DevStatus), cudaMemcpyDeviceToHost));
+    out->nbodies = ctx->nbodies;
+    out->ncells = (int64_t)(t64 >> 32);
+    out->nnodes = tot[1];
+    out->max_level = ctx->h_status->max_level;
+    out->nsystems = ctx->nsys;
+    out->interactions = (int64_t)ctx->h_status->interactions;
+    out->opened = (int64_t)ctx->h_status->opened;
+    out->refined_runs = ctx->h_status->refined_runs;
+    out->status = ctx->h_status->code;
+    out->launches = ctx->launches;
+    return NBX_OK;
+}
+
+int nbx_export_tree(nbx_ctx *c, int sys, int *perm, int *root_child, int *cell_child, int *cell_start,
+                    int *cell_count, int *cell_level, float *cell_x, float *cell_y, float *cell_z, float *cell_m,
+                    int cap_cells, int64_t *ncells, void *stream) {
+    if (!c) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    int rc = nbx_sync_status(c, stream);
+    if (rc) return rc;
+    rc = nbx::export_tree_impl(ctx, sys, perm, root_child, cell_child, cell_start, cell_count, cell_level, cell_x,
+                               cell_y, cell_z, cell_m, cap_cells, ncells, S(stream), 0);
+    if (rc) return rc;
+    NBX_CUDA(cudaStreamSynchronize(S(stream)));
+    return NBX_OK;
+}
+
+int nbx_export_keys(nbx_ctx *c, uint64_t *keys, int *perm, void *stream) {
+    if (!c) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    if (!ctx->built) return NBX_ERR_STATE;
+    if (keys)
+        NBX_CUDA(cudaMemcpyAsync(keys, ctx->d_key, sizeof(uint64_t) * ctx->nbodies, cudaMemcpyDeviceToDevice, S(stream)));
+    if (perm)
+        NBX_CUDA(cudaMemcpyAsync(perm, ctx->d_val, sizeof(int) * ctx->nbodies, cudaMemcpyDeviceToDevice, S(stream)));
+    NBX_CUDA(cudaStreamSynchronize(S(stream)));
+    return NBX_OK;
+}
+
+int nbx_export_walk_stats(nbx_ctx *c, int *nlist, int *nopen, void *stream) {
+    if (!c) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    if (nlist)
+        NBX_CUDA(cudaMemcpyAsync(nlist, ctx->d_nlist, sizeof(int) * ctx->nbodies, cudaMemcpyDeviceToDevice, S(stream)));
+    if (nopen)
+        NBX_CUDA(cudaMemcpyAsync(nopen, ctx->d_nopen, sizeof(int) * ctx->nbodies, cudaMemcpyDeviceToDevice, S(stream)));
+    NBX_CUDA(cudaStreamSynchronize(S(stream)));
+    return NBX_OK;
+}
+
+int nbx_direct_fp64(nbx_ctx *c, const float *x, const float *y, const float *z, const float *m, int n,
+                    const int *targets, int nt, double eps2, double *acc, void *stream) {
+    if (!c || !x || !y || !z || !m || !targets || !acc || n < 0 || nt < 0) return NBX_ERR_ARG;
+    return nbx::direct_fp64(C(c), x, y, z, m, n, targets, nt, eps2, acc, S(stream));
+}
+
+int nbx_diagnostics_fp64(nbx_ctx *c, const nbx_state *s, int n, double *out, void *stream) {
+    if (!c || !s || !out || n < 0) return NBX_ERR_ARG;
+    return nbx::diagnostics_fp64(C(c), s, n, out, S(stream));
+}
+
+}  // extern "C"

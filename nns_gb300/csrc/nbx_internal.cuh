@@ -1,0 +1,172 @@
+// nbx_internal.cuh -- context layout and shared device helpers of libnbx.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/nbx.h"
+
+namespace nbx {
+
+constexpr int kTile = 2048;       // keys per radix tile (one warp: 32 lanes x 64)
+constexpr int kRadixBins = 256;   // 8-bit digits
+constexpr int kMaxLevel = 43;     // 42 key levels + the body level
+constexpr int kBodyFlag = int(0x80000000u);
+constexpr int kLevelShift = 26;   // walk stack entry = node | level << 26
+constexpr int kMaxNodes = 1 << 26;
+constexpr int kScanItems = 4096;  // elements per scan block (1024 threads x 4)
+constexpr int kMaxRun = 4096;     // longest run of equal 21-level keys refined
+
+// Device-side sticky status word layout.
+struct DevStatus {
+    int code;          // first error code (NBX_*), 0 = ok
+    int detail;        // e.g. the offending index
+    int refined_runs;
+    int max_level;
+    unsigned long long interactions;
+    unsigned long long opened;
+};
+
+struct Ctx {
+    nbx_params p;
+    float theta_ref, eps2;
+    int compensated;
+    std::string last_error;
+
+    // capacity
+    int cap_bodies, cap_sys, cap_nodes, cap_tiles_body, cap_tiles_node;
+    int nsm = 152;         // multiprocessors of the device
+    long long launches = 0;  // kernels launched by this context
+
+    // systems
+    int nsys = 0;
+    int64_t nbodies = 0;
+    int ntiles_body = 0;   // radix tiles over all systems
+    int ngroups = 0;       // walk groups over all systems
+    int *d_sys_off = nullptr;       // [S+1]
+    int *d_body_sys = nullptr;      // [B] system of original index
+    int4 *d_tiles = nullptr;        // [tiles] start, len, sys, local tile index
+    int2 *d_sys_tiles = nullptr;    // [S] tile base, ntiles
+    int *d_groups = nullptr;        // [G] first sorted position of each walk group
+
+    // per-system tree parameters
+    unsigned *d_bbox_u = nullptr;   // [6S] ordered-int encodings during the reduction
+    float *d_bbox = nullptr;        // [6S]
+    double *d_bbox64 = nullptr;     // [6S]
+    float *d_depth0 = nullptr;      // [S]
+    int *d_root_first = nullptr;    // [S]
+    int *d_root_nch = nullptr;      // [S]
+
+    // per body
+    unsigned long long *d_key = nullptr, *d_key_alt = nullptr;  // [B]
+    unsigned long long *d_key_lo = nullptr;                     // [B] levels 22..42 (refined runs)
+    int *d_val = nullptr, *d_val_alt = nullptr;                 // [B] permutation
+    float4 *d_body4 = nullptr;   // [B] sorted bodies (x,y,z,m)
+    unsigned char *d_delta = nullptr;  // [B]
+    unsigned *d_ecount = nullptr;      // [B] entries per position -> exclusive offsets
+    int *d_body_node = nullptr;        // [B] node of sorted position
+    int *d_nlist = nullptr;            // [B] per original index (walk statistics)
+    int *d_nopen = nullptr;
+
+    // per node (entry / BFS order)
+    unsigned *d_ent = nullptr, *d_ent_alt = nullptr;  // [NC] packed level<<26 | position
+    unsigned long long *d_flags = nullptr;            // [NC] cell<<32 | first-child
+    float4 *d_node4 = nullptr;                        // [NC]
+    int *d_meta = nullptr;                            // [NC]
+    int *d_parent = nullptr;                          // [NC]
+    double4 *d_sums = nullptr;                        // [NC] m, m*x, m*y, m*z (FP64)
+    int *d_count = nullptr;                           // [NC]
+    int *d_arrive = nullptr;                          // [NC]
+    int *d_fcl = nullptr;                             // [NC+S+1] first-child list
+    int *d_cl = nullptr;                              // [NC+S] cell list (BFS index)
+
+    // radix + scan scratch
+    unsigned *d_hist = nullptr;        // [256 * max(tiles)]
+    unsigned long long *d_scan_blk = nullptr;  // block sums
+    unsigned *d_totals = nullptr;      // [8] device-side totals: 0 entries, 1 cells+first..., etc
+    unsigned long long *d_totals64 = nullptr;
+    int cap_scan_blk = 0;
+
+    DevStatus *d_status = nullptr;
+    DevStatus *h_status = nullptr;     // pinned mirror
+
+    // reference-array bridge (single system)
+    bool built = false;
+    int ref_m = 0;         // m of the last successful nbx_build_tree (0 = none)
+
+    // graph
+    cudaGraphExec_t graph_exec = nullptr;
+    nbx_state graph_state{};
+    int graph_nsys = -1;
+    cudaStream_t graph_stream = nullptr;
+};
+
+// ---- host helpers ----
+#define NBX_CUDA(call)                                                      \
+    do {                                                                    \
+        cudaError_t e_ = (call);                                            \
+        if (e_ != cudaSuccess) {                                            \
+            ctx->last_error = std::string(#call) + ": " + cudaGetErrorString(e_); \
+            return NBX_ERR_CUDA;                                            \
+        }                                                                   \
+    } while (0)
+
+inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+// ---- device helpers ----
+__device__ __forceinline__ void set_status(DevStatus *st, int code, int detail) {
+    if (atomicCAS(&st->code, 0, code) == 0) st->detail = detail;
+}
+
+__device__ __forceinline__ unsigned f2ord(float f) {
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// One subdivision step along one axis (Kernels.cu:200-206): returns 1 for the
+// lower half.  (double)v < 0.5*(double)(mn+mx)  <=>  v+v < fl(mn+mx), exactly;
+// the new bound fl(mn+mx)*0.5 rounds as the reference's double->float store.
+__device__ __forceinline__ int split_axis(float v, float &mn, float &mx) {
+    float s = __fadd_rn(mn, mx);
+    float h = __fmul_rn(s, 0.5f);
+    if (__fadd_rn(v, v) < s) { mx = h; return 1; }
+    mn = h;
+    return 0;
+}
+
+// Number of leading equal 3-bit digits of two 63-bit keys (bit 63 unused).
+__device__ __forceinline__ int common_digits(unsigned long long a, unsigned long long b) {
+    unsigned long long x = a ^ b;
+    if (x == 0ull) return 21;
+    return (__clzll(x) - 1) / 3;
+}
+
+__device__ __forceinline__ int digit_of(unsigned long long hi, unsigned long long lo, int level) {
+    return level <= 21 ? (int)((hi >> (3 * (21 - level))) & 7ull)
+                       : (int)((lo >> (3 * (42 - level))) & 7ull);
+}
+
+// ---- kernels / launchers shared across translation units ----
+// scan.cu
+int scan_exclusive_u32(Ctx *ctx, const unsigned *in, unsigned *out, int n_cap,
+                       const unsigned *n_dev, unsigned *total_out, cudaStream_t st);
+int scan_exclusive_u64(Ctx *ctx, const unsigned long long *in, unsigned long long *out, int n_cap,
+                       const unsigned *n_dev, unsigned long long *total_out, cudaStream_t st);
+// radix.cu
+int radix_sort_bodies(Ctx *ctx, cudaStream_t st);
+int radix_sort_entries(Ctx *ctx, cudaStream_t st);
+// tree.cu
+int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox,
+               const float *const *bbox_ptrs);
+// walk.cu
+int walk_init(Ctx *ctx);
+int walk_forces(Ctx *ctx, const nbx_state *s, cudaStream_t st);
+// integrate.cu
+int integrate(Ctx *ctx, const nbx_state *s, float dt, float d, int n, cudaStream_t st);
+
+}  // namespace nbx

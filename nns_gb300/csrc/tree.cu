@@ -1,0 +1,594 @@
+// tree.cu -- bounding box, keys, key sort, key-built octree and FP64 moments.
+//
+// Replaces the reference's insertion build (3D/CUDA/CUDA_NBody/src/Kernels.cu:157-377),
+// its bounding box (:67-154), centre of mass (:381-399) and sort (:403-456) with a
+// sort-based construction that produces the same tree:
+//
+//  keys     each body replays the reference's float subdivision (:200-258) for 21
+//           levels; the child codes c = [x<mid] + 2[y<mid] + 4[z<mid] packed most
+//           significant first give a 63-bit key whose ascending order is the
+//           reference's in-order body order.  Bodies sharing all 21 levels are
+//           refined to 42 levels (k_refine).
+//  delta    delta(i) = number of leading levels sorted neighbours i, i+1 share.
+//           A cell (a region holding >= 2 bodies) at level L starts at sorted
+//           position a iff delta(a-1) < L <= delta(a); the body at position i sits
+//           at level max(delta(i-1), delta(i)) + 1.  Position i therefore owns the
+//           node levels lo..hi = delta(i-1)+1 .. max(delta(i-1),delta(i))+1.
+//  nodes    entries (level, position) generated in position order are the
+//           depth-first pre-order; a stable sort by level gives breadth-first
+//           order, in which the children of every cell are contiguous.
+//  links    a node is the first child of its parent iff the parent starts at the
+//           same position.  The k-th first child in BFS order belongs to the k-th
+//           cell in BFS order (roots first), so two prefix counts give every cell's
+//           child block and every node's parent -- no search, no locks.
+//  moments  bottom-up FP64 sums in child order; the last child to arrive at a
+//           parent (one atomic per node) sums it, so results are deterministic.
+#include "nbx_internal.cuh"
+
+namespace nbx {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ int grid_stride_start() { return blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ int grid_stride() { return gridDim.x * blockDim.x; }
+
+__global__ void k_step_reset(unsigned *bbox_u, int nsys, DevStatus *st) {
+    int i = grid_stride_start();
+    if (i < 6 * nsys) bbox_u[i] = f2ord(0.0f);  // Kernels.cu:56-62: the box contains the origin
+    if (i == 0) {
+        st->refined_runs = 0;
+        st->max_level = 0;
+        st->interactions = 0ull;
+        st->opened = 0ull;
+    }
+}
+
+// Per-tile min/max of the bodies of one system, merged with ordered-int atomics.
+__global__ void __launch_bounds__(kBlock) k_bbox(const float *__restrict__ x, const float *__restrict__ y,
+                                                  const float *__restrict__ z, const int4 *__restrict__ tiles,
+                                                  int ntiles, unsigned *bbox_u) {
+    const int t = blockIdx.x;
+    if (t >= ntiles) return;
+    const int4 tl = tiles[t];
+    float v[6] = {INFINITY, -INFINITY, INFINITY, -INFINITY, INFINITY, -INFINITY};
+    for (int i = threadIdx.x; i < tl.y; i += kBlock) {
+        float a = x[tl.x + i], b = y[tl.x + i], c = z[tl.x + i];
+        v[0] = fminf(v[0], a); v[1] = fmaxf(v[1], a);
+        v[2] = fminf(v[2], b); v[3] = fmaxf(v[3], b);
+        v[4] = fminf(v[4], c); v[5] = fmaxf(v[5], c);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 6; k += 2) {
+            v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+            v[k + 1] = fmaxf(v[k + 1], __shfl_xor_sync(0xffffffffu, v[k + 1], o));
+        }
+    }
+    __shared__ float part[kBlock / 32][6];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+        for (int k = 0; k < 6; k++) part[w][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
+        float r = part[0][k];
+        for (int q = 1; q < kBlock / 32; q++) r = (k & 1) ? fmaxf(r, part[q][k]) : fminf(r, part[q][k]);
+        if (!isnan(r) && !isinf(r)) {
+            unsigned *dst = &bbox_u[6 * tl.z + k];
+            if (k & 1) atomicMax(dst, f2ord(r));
+            else atomicMin(dst, f2ord(r));
+        }
+    }
+}
+
+__device__ __forceinline__ float depth0_of(float mnx, float mxx, float theta_ref) {
+    float r = __fmul_rn(__fsub_rn(mxx, mnx), 0.5f);  // Kernels.cu:477
+    return __fdiv_rn(__fmul_rn(r, r), theta_ref);    // Kernels.cu:513
+}
+
+__global__ void k_bbox_finalize(const unsigned *bbox_u, int nsys, float theta_ref, float *bbox,
+                                double *bbox64, float *depth0) {
+    int s = grid_stride_start();
+    if (s >= nsys) return;
+    float b[6];
+    for (int k = 0; k < 6; k++) {
+        b[k] = __fadd_rn(ord2f(bbox_u[6 * s + k]), 0.0f);  // -0 -> +0
+        bbox[6 * s + k] = b[k];
+        bbox64[6 * s + k] = (double)b[k];
+    }
+    depth0[s] = depth0_of(b[0], b[1], theta_ref);
+}
+
+// Single-system box supplied by the caller (reference-compatible entry points).
+__global__ void k_bbox_from_ptrs(const float *mnx, const float *mxx, const float *mny,
+                                 const float *mxy, const float *mnz, const float *mxz,
+                                 float theta_ref, float *bbox, double *bbox64, float *depth0,
+                                 DevStatus *st) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    float b[6] = {*mnx, *mxx, *mny, *mxy, *mnz, *mxz};
+    for (int k = 0; k < 6; k++) { bbox[k] = b[k]; bbox64[k] = (double)b[k]; }
+    depth0[0] = depth0_of(b[0], b[1], theta_ref);
+    st->refined_runs = 0;
+    st->max_level = 0;
+}
+
+__device__ __forceinline__ unsigned long long make_key(float px, float py, float pz, const float *bb) {
+    float mnx = bb[0], mxx = bb[1], mny = bb[2], mxy = bb[3], mnz = bb[4], mxz = bb[5];
+    unsigned long long key = 0ull;
+#pragma unroll 3
+    for (int l = 1; l <= 21; l++) {
+        int c = split_axis(px, mnx, mxx) + 2 * split_axis(py, mny, mxy) + 4 * split_axis(pz, mnz, mxz);
+        key = (key << 3) | (unsigned long long)c;
+    }
+    return key;
+}
+
+__global__ void __launch_bounds__(kBlock) k_keys(const float *__restrict__ x, const float *__restrict__ y,
+                                                  const float *__restrict__ z, const int *__restrict__ body_sys,
+                                                  const float *__restrict__ bbox, int n,
+                                                  unsigned long long *__restrict__ key, int *__restrict__ val,
+                                                  DevStatus *st) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        const float px = x[i], py = y[i], pz = z[i];
+        if (!isfinite(px) || !isfinite(py) || !isfinite(pz)) set_status(st, NBX_ERR_NONFINITE, i);
+        const int s = body_sys[i];
+        float bb[6];
+#pragma unroll
+        for (int k = 0; k < 6; k++) bb[k] = bbox[6 * s + k];
+        key[i] = make_key(px, py, pz, bb);
+        val[i] = i;
+    }
+}
+
+// Runs of equal 21-level keys: compute levels 22..42 and order the run by them.
+__global__ void k_refine(const float *__restrict__ x, const float *__restrict__ y,
+                         const float *__restrict__ z, const int *__restrict__ body_sys,
+                         const int *__restrict__ sys_off, const float *__restrict__ bbox, int n,
+                         const unsigned long long *__restrict__ key,
+                         unsigned long long *__restrict__ key_lo, int *__restrict__ val,
+                         DevStatus *st) {
+    for (int p = grid_stride_start(); p < n; p += grid_stride()) {
+        const int s = body_sys[p];
+        const int beg = sys_off[s], end = sys_off[s + 1];
+        const unsigned long long k = key[p];
+        if (p + 1 >= end || key[p + 1] != k) continue;
+        if (p > beg && key[p - 1] == k) continue;
+        int e = p + 1;
+        while (e + 1 < end && key[e + 1] == k) e++;
+        if (e - p + 1 > kMaxRun) {
+            set_status(st, NBX_ERR_CLUSTER, p);
+            continue;
+        }
+        atomicAdd(&st->refined_runs, 1);
+        float bb[6];
+        for (int q = 0; q < 6; q++) bb[q] = bbox[6 * s + q];
+        for (int q = p; q <= e; q++) {
+            const int b = val[q];
+            float mnx = bb[0], mxx = bb[1], mny = bb[2], mxy = bb[3], mnz = bb[4], mxz = bb[5];
+            unsigned long long lo = 0ull;
+            const float px = x[b], py = y[b], pz = z[b];
+            for (int l = 1; l <= 42; l++) {
+                int c = split_axis(px, mnx, mxx) + 2 * split_axis(py, mny, mxy) + 4 * split_axis(pz, mnz, mxz);
+                if (l > 21) lo = (lo << 3) | (unsigned long long)c;
+            }
+            key_lo[q] = lo;
+        }
+        // stable insertion sort of the run by key_lo (runs are short)
+        for (int q = p + 1; q <= e; q++) {
+            unsigned long long kl = key_lo[q];
+            int v = val[q];
+            int r = q - 1;
+            while (r >= p && key_lo[r] > kl) {
+                key_lo[r + 1] = key_lo[r];
+                val[r + 1] = val[r];
+                r--;
+            }
+            key_lo[r + 1] = kl;
+            val[r + 1] = v;
+        }
+        for (int q = p; q < e; q++)
+            if (key_lo[q] == key_lo[q + 1]) set_status(st, NBX_ERR_DEPTH, val[q]);
+    }
+}
+
+__device__ __forceinline__ int delta_of(const unsigned long long *key, const unsigned long long *key_lo,
+                                        int a) {
+    const unsigned long long ka = key[a], kb = key[a + 1];
+    if (ka != kb) return common_digits(ka, kb);
+    int d = 21 + common_digits(key_lo[a], key_lo[a + 1]);
+    return d > 41 ? 41 : d;  // equal 42-level keys were reported as NBX_ERR_DEPTH
+}
+
+// Sorted bodies as float4 plus delta and the number of node entries per position.
+__global__ void __launch_bounds__(kBlock) k_delta(const float *__restrict__ x, const float *__restrict__ y,
+                                                   const float *__restrict__ z, const float *__restrict__ m,
+                                                   const int *__restrict__ body_sys, const int *__restrict__ sys_off,
+                                                   int n, const unsigned long long *__restrict__ key,
+                                                   const unsigned long long *__restrict__ key_lo,
+                                                   const int *__restrict__ val, float4 *__restrict__ body4,
+                                                   unsigned char *__restrict__ delta,
+                                                   unsigned *__restrict__ ecount, DevStatus *st) {
+    int lvl_max = 0;
+    for (int p = grid_stride_start(); p < n; p += grid_stride()) {
+        const int s = body_sys[p];
+        const int beg = sys_off[s], end = sys_off[s + 1];
+        const int di = p + 1 < end ? delta_of(key, key_lo, p) : 0;
+        const int dp = p > beg ? delta_of(key, key_lo, p - 1) : 0;
+        delta[p] = (unsigned char)di;
+        ecount[p] = (unsigned)((di > dp ? di - dp : 0) + 1);
+        const int b = val[p];
+        body4[p] = make_float4(x[b], y[b], z[b], m[b]);
+        lvl_max = max(lvl_max, max(di, dp) + 1);
+    }
+    lvl_max = __reduce_max_sync(0xffffffffu, lvl_max);
+    if ((threadIdx.x & 31) == 0 && lvl_max > 0) atomicMax(&st->max_level, lvl_max);
+}
+
+__device__ __forceinline__ void levels_of(const unsigned char *delta, int p, int beg, int &lo, int &hi,
+                                          int &dp) {
+    dp = p > beg ? (int)delta[p - 1] : 0;
+    const int di = delta[p];
+    lo = dp + 1;
+    hi = max(dp, di) + 1;
+}
+
+// Node entries (level << 26 | position) in position order = depth-first pre-order.
+__global__ void __launch_bounds__(kBlock) k_entries(const int *__restrict__ body_sys,
+                                                     const int *__restrict__ sys_off, int n,
+                                                     const unsigned char *__restrict__ delta,
+                                                     const unsigned *__restrict__ eoff, unsigned *totals,
+                                                     int cap_nodes, unsigned *__restrict__ ent,
+                                                     DevStatus *st) {
+    if (grid_stride_start() == 0) {
+        unsigned T = totals[0];
+        if (T > (unsigned)cap_nodes) {
+            set_status(st, NBX_ERR_CAPACITY, (int)min(T, 0x7fffffffu));
+            T = 0u;  // nothing downstream reads a partial entry list
+        }
+        totals[1] = T;  // node count used downstream
+    }
+    for (int p = grid_stride_start(); p < n; p += grid_stride()) {
+        const int beg = sys_off[body_sys[p]];
+        int lo, hi, dp;
+        levels_of(delta, p, beg, lo, hi, dp);
+        const unsigned e = eoff[p];
+        if (e + (unsigned)(hi - lo + 1) > (unsigned)cap_nodes) continue;
+        for (int l = lo; l <= hi; l++) ent[e + (l - lo)] = ((unsigned)l << kLevelShift) | (unsigned)p;
+    }
+}
+
+__device__ __forceinline__ void node_kind(unsigned u, const int *body_sys, const int *sys_off,
+                                          const unsigned char *delta, int &p, int &l, bool &is_cell,
+                                          bool &first) {
+    l = (int)(u >> kLevelShift);
+    p = (int)(u & ((1u << kLevelShift) - 1u));
+    const int beg = sys_off[body_sys[p]];
+    int lo, hi, dp;
+    levels_of(delta, p, beg, lo, hi, dp);
+    is_cell = l < hi;
+    first = (l == 1) ? (p == beg) : (dp < l - 1);
+}
+
+__global__ void __launch_bounds__(kBlock) k_node_flags(const unsigned *__restrict__ ent_bfs,
+                                                        const unsigned *__restrict__ totals,
+                                                        const int *__restrict__ body_sys,
+                                                        const int *__restrict__ sys_off,
+                                                        const unsigned char *__restrict__ delta,
+                                                        unsigned long long *__restrict__ flags) {
+    const int T = (int)totals[1];
+    for (int b = grid_stride_start(); b < T; b += grid_stride()) {
+        int p, l;
+        bool c, f;
+        node_kind(ent_bfs[b], body_sys, sys_off, delta, p, l, c, f);
+        flags[b] = ((unsigned long long)c << 32) | (unsigned long long)f;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_nodes_a(const unsigned *__restrict__ ent_bfs,
+                                                     const unsigned *__restrict__ totals,
+                                                     const unsigned long long *__restrict__ totals64,
+                                                     const int *__restrict__ body_sys,
+                                                     const int *__restrict__ sys_off,
+                                                     const unsigned char *__restrict__ delta,
+                                                     const unsigned long long *__restrict__ flags_ex,
+                                                     const float4 *__restrict__ body4, int nsys,
+                                                     int *__restrict__ fcl, int *__restrict__ cl,
+                                                     float4 *__restrict__ node4, int *__restrict__ meta,
+                                                     int *__restrict__ body_node, int *__restrict__ count,
+                                                     int *__restrict__ arrive, DevStatus *st) {
+    const int T = (int)totals[1];
+    if (grid_stride_start() == 0) {
+        const unsigned long long tot = totals64[0];
+        const int ncell = (int)(tot >> 32), nfirst = (int)(tot & 0xffffffffull);
+        if (nfirst != nsys + ncell && st->code == 0) set_status(st, NBX_ERR_STATE, nfirst);
+        fcl[nsys + ncell] = T;
+    }
+    for (int b = grid_stride_start(); b < T; b += grid_stride()) {
+        int p, l;
+        bool c, f;
+        node_kind(ent_bfs[b], body_sys, sys_off, delta, p, l, c, f);
+        const unsigned long long ex = flags_ex[b];
+        if (f) fcl[(int)(ex & 0xffffffffull)] = b;
+        arrive[b] = 0;
+        if (c) {
+            cl[nsys + (int)(ex >> 32)] = b;
+        } else {
+            node4[b] = body4[p];
+            meta[b] = kBodyFlag | p;
+            body_node[p] = b;
+            count[b] = 1;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_nodes_b(const unsigned *__restrict__ ent_bfs,
+                                                     const unsigned *__restrict__ totals,
+                                                     const int *__restrict__ body_sys,
+                                                     const int *__restrict__ sys_off,
+                                                     const unsigned char *__restrict__ delta,
+                                                     const unsigned long long *__restrict__ flags_ex,
+                                                     int nsys, const int *__restrict__ fcl,
+                                                     const int *__restrict__ cl, int *__restrict__ meta,
+                                                     int *__restrict__ parent, int *__restrict__ root_first,
+                                                     int *__restrict__ root_nch, DevStatus *st) {
+    const int T = (int)totals[1];
+    for (int s = grid_stride_start(); s < nsys; s += grid_stride()) {
+        root_first[s] = fcl[s];
+        root_nch[s] = fcl[s + 1] - fcl[s];
+    }
+    for (int b = grid_stride_start(); b < T; b += grid_stride()) {
+        int p, l;
+        bool c, f;
+        node_kind(ent_bfs[b], body_sys, sys_off, delta, p, l, c, f);
+        const unsigned long long ex = flags_ex[b];
+        const int fcx = (int)(ex & 0xffffffffull);
+        if (c) {
+            const int k = nsys + (int)(ex >> 32);
+            const int first = fcl[k];
+            const int nch = fcl[k + 1] - first;
+            if (nch < 1 || nch > 8) {
+                set_status(st, NBX_ERR_STATE, b);
+                meta[b] = first;  // keeps the walk in bounds
+            } else {
+                meta[b] = first | ((nch - 1) << 28);
+            }
+        }
+        const int j = fcx + (f ? 1 : 0) - 1;
+        parent[b] = j < nsys ? (-1 - j) : cl[j];
+    }
+}
+
+// Bottom-up FP64 moments: the last child to arrive sums its parent in child order.
+__global__ void __launch_bounds__(kBlock) k_moments(int n, const int *__restrict__ body_node,
+                                                     const int *__restrict__ parent,
+                                                     const int *__restrict__ meta, float4 *node4,
+                                                     double4 *sums, int *count, int *arrive,
+                                                     const DevStatus *st) {
+    if (st->code != 0) return;  // an inconsistent tree is never summed
+    for (int p = grid_stride_start(); p < n; p += grid_stride()) {
+        int cur = body_node[p];
+        for (int guard = 0; guard < 64; guard++) {
+            const int par = parent[cur];
+            if (par < 0) break;
+            const int pm = meta[par];
+            const int first = pm & 0x0fffffff;
+            const int nch = ((pm >> 28) & 7) + 1;
+            __threadfence();
+            if (atomicAdd(&arrive[par], 1) != nch - 1) break;
+            __threadfence();
+            double sm = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
+            int cnt = 0;
+            for (int c = first; c < first + nch; c++) {
+                if (meta[c] < 0) {
+                    const float4 q = node4[c];
+                    const double mb = (double)q.w;
+                    sm += mb;
+                    sx += mb * (double)q.x;
+                    sy += mb * (double)q.y;
+                    sz += mb * (double)q.z;
+                    cnt += 1;
+                } else {
+                    const double2 a = __ldcg(reinterpret_cast<const double2 *>(&sums[c]));
+                    const double2 b = __ldcg(reinterpret_cast<const double2 *>(&sums[c]) + 1);
+                    sm += a.x;
+                    sx += a.y;
+                    sy += b.x;
+                    sz += b.y;
+                    cnt += __ldcg(&count[c]);
+                }
+            }
+            sums[par] = make_double4(sm, sx, sy, sz);
+            count[par] = cnt;
+            node4[par] = make_float4((float)(sx / sm), (float)(sy / sm), (float)(sz / sm), (float)sm);
+            cur = par;
+        }
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox,
+               const float *const *bbox_ptrs) {
+    const int n = (int)ctx->nbodies;
+    const int S = ctx->nsys;
+    if (n <= 0 || S <= 0) return NBX_ERR_STATE;
+    const int gb = ceil_div(n, kBlock) < ctx->nsm * 8 ? ceil_div(n, kBlock) : ctx->nsm * 8;
+    k_step_reset<<<ceil_div(6 * S + 1, kBlock), kBlock, 0, st>>>(ctx->d_bbox_u, S, ctx->d_status);
+    ++ctx->launches;
+    if (!external_bbox) {
+        k_bbox<<<ctx->ntiles_body, kBlock, 0, st>>>(s->x, s->y, s->z, ctx->d_tiles, ctx->ntiles_body,
+                                                    ctx->d_bbox_u);
+        ++ctx->launches;
+        k_bbox_finalize<<<ceil_div(S, kBlock), kBlock, 0, st>>>(ctx->d_bbox_u, S, ctx->theta_ref,
+                                                                ctx->d_bbox, ctx->d_bbox64, ctx->d_depth0);
+        ++ctx->launches;
+    } else {
+        k_bbox_from_ptrs<<<1, 32, 0, st>>>(bbox_ptrs[0], bbox_ptrs[1], bbox_ptrs[2], bbox_ptrs[3],
+                                           bbox_ptrs[4], bbox_ptrs[5], ctx->theta_ref, ctx->d_bbox,
+                                           ctx->d_bbox64, ctx->d_depth0, ctx->d_status);
+        ++ctx->launches;
+    }
+    k_keys<<<gb, kBlock, 0, st>>>(s->x, s->y, s->z, ctx->d_body_sys, ctx->d_bbox, n, ctx->d_key,
+                                  ctx->d_val, ctx->d_status);
+    ++ctx->launches;
+    int rc = radix_sort_bodies(ctx, st);
+    if (rc) return rc;
+    k_refine<<<gb, kBlock, 0, st>>>(s->x, s->y, s->z, ctx->d_body_sys, ctx->d_sys_off, ctx->d_bbox, n,
+                                    ctx->d_key, ctx->d_key_lo, ctx->d_val, ctx->d_status);
+    ++ctx->launches;
+    k_delta<<<gb, kBlock, 0, st>>>(s->x, s->y, s->z, s->m, ctx->d_body_sys, ctx->d_sys_off, n, ctx->d_key,
+                                   ctx->d_key_lo, ctx->d_val, ctx->d_body4, ctx->d_delta, ctx->d_ecount,
+                                   ctx->d_status);
+    ++ctx->launches;
+    rc = scan_exclusive_u32(ctx, ctx->d_ecount, ctx->d_ecount, n, nullptr, &ctx->d_totals[0], st);
+    if (rc) return rc;
+    k_entries<<<gb, kBlock, 0, st>>>(ctx->d_body_sys, ctx->d_sys_off, n, ctx->d_delta, ctx->d_ecount,
+                                     ctx->d_totals, ctx->cap_nodes, ctx->d_ent, ctx->d_status);
+    ++ctx->launches;
+    rc = radix_sort_entries(ctx, st);  // d_ent -> d_ent_alt (BFS order)
+    if (rc) return rc;
+    const int gn = ceil_div(ctx->cap_nodes, kBlock) < ctx->nsm * 8 ? ceil_div(ctx->cap_nodes, kBlock) : ctx->nsm * 8;
+    k_node_flags<<<gn, kBlock, 0, st>>>(ctx->d_ent_alt, ctx->d_totals, ctx->d_body_sys, ctx->d_sys_off,
+                                        ctx->d_delta, ctx->d_flags);
+    ++ctx->launches;
+    rc = scan_exclusive_u64(ctx, ctx->d_flags, ctx->d_flags, ctx->cap_nodes, &ctx->d_totals[1],
+                            &ctx->d_totals64[0], st);
+    if (rc) return rc;
+    k_nodes_a<<<gn, kBlock, 0, st>>>(ctx->d_ent_alt, ctx->d_totals, ctx->d_totals64, ctx->d_body_sys,
+                                     ctx->d_sys_off, ctx->d_delta, ctx->d_flags, ctx->d_body4, S, ctx->d_fcl,
+                                     ctx->d_cl, ctx->d_node4, ctx->d_meta, ctx->d_body_node, ctx->d_count,
+                                     ctx->d_arrive, ctx->d_status);
+    ++ctx->launches;
+    k_nodes_b<<<gn, kBlock, 0, st>>>(ctx->d_ent_alt, ctx->d_totals, ctx->d_body_sys, ctx->d_sys_off,
+                                     ctx->d_delta, ctx->d_flags, S, ctx->d_fcl, ctx->d_cl, ctx->d_meta,
+                                     ctx->d_parent, ctx->d_root_first, ctx->d_root_nch, ctx->d_status);
+    ++ctx->launches;
+    k_moments<<<gb, kBlock, 0, st>>>(n, ctx->d_body_node, ctx->d_parent, ctx->d_meta, ctx->d_node4,
+                                     ctx->d_sums, ctx->d_count, ctx->d_arrive, ctx->d_status);
+    ++ctx->launches;
+    NBX_CUDA(cudaGetLastError());
+    ctx->built = true;
+    return NBX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Export of one system's tree in the reference's array format.
+namespace {
+
+__global__ void __launch_bounds__(kBlock) k_export(const unsigned *__restrict__ ent_bfs,
+                                                    const unsigned *__restrict__ totals,
+                                                    const int *__restrict__ body_sys,
+                                                    const int *__restrict__ sys_off,
+                                                    const unsigned char *__restrict__ delta,
+                                                    const unsigned *__restrict__ eoff,
+                                                    const unsigned long long *__restrict__ key,
+                                                    const unsigned long long *__restrict__ key_lo,
+                                                    const int *__restrict__ val, const int *__restrict__ parent,
+                                                    const float4 *__restrict__ node4,
+                                                    const double4 *__restrict__ sums,
+                                                    const int *__restrict__ count, int sys, int cells_before,
+                                                    int cap_cells, int *root_child, int *cell_child,
+                                                    int *cell_start, int *cell_count, int *cell_level,
+                                                    float *cx, float *cy, float *cz, float *cm, int sum_mode) {
+    const int T = (int)totals[1];
+    const int beg = sys_off[sys];
+    const int nsys_bodies = sys_off[sys + 1] - beg;
+    for (int b = grid_stride_start(); b < T; b += grid_stride()) {
+        const unsigned u = ent_bfs[b];
+        const int l = (int)(u >> kLevelShift);
+        const int p = (int)(u & ((1u << kLevelShift) - 1u));
+        if (body_sys[p] != sys) continue;
+        int lo, hi, dp;
+        levels_of(delta, p, beg, lo, hi, dp);
+        const bool is_cell = l < hi;
+        const int pre = (int)(eoff[p] - (unsigned)p) - cells_before + (l - lo);
+        int value;
+        if (is_cell) {
+            value = nsys_bodies + pre;
+            if (pre < cap_cells) {
+                if (cell_start) cell_start[pre] = p - beg;
+                if (cell_count) cell_count[pre] = count[b];
+                if (cell_level) cell_level[pre] = l;
+                if (sum_mode) {
+                    const double4 q = sums[b];
+                    if (cx) cx[pre] = (float)q.y;
+                    if (cy) cy[pre] = (float)q.z;
+                    if (cz) cz[pre] = (float)q.w;
+                    if (cm) cm[pre] = (float)q.x;
+                } else {
+                    const float4 q = node4[b];
+                    if (cx) cx[pre] = q.x;
+                    if (cy) cy[pre] = q.y;
+                    if (cz) cz[pre] = q.z;
+                    if (cm) cm[pre] = q.w;
+                }
+            }
+        } else {
+            value = val[p] - beg;
+        }
+        const int slot = digit_of(key[p], key_lo[p], l);
+        const int par = parent[b];
+        if (par < 0) {
+            if (root_child) root_child[slot] = value;
+        } else if (cell_child) {
+            const unsigned pu = ent_bfs[par];
+            const int pl = (int)(pu >> kLevelShift);
+            const int pp = (int)(pu & ((1u << kLevelShift) - 1u));
+            int plo, phi, pdp;
+            levels_of(delta, pp, beg, plo, phi, pdp);
+            const int ppre = (int)(eoff[pp] - (unsigned)pp) - cells_before + (pl - plo);
+            if (ppre < cap_cells) cell_child[8 * ppre + slot] = value;
+        }
+    }
+}
+
+__global__ void k_perm_export(const int *val, int beg, int n, int *perm) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) perm[i] = val[beg + i] - beg;
+}
+
+}  // namespace
+
+int export_tree_impl(Ctx *ctx, int sys, int *perm, int *root_child, int *cell_child, int *cell_start,
+                     int *cell_count, int *cell_level, float *cx, float *cy, float *cz, float *cm,
+                     int cap_cells, int64_t *ncells, cudaStream_t st, int sum_mode) {
+    if (!ctx->built) return NBX_ERR_STATE;
+    if (sys < 0 || sys >= ctx->nsys) return NBX_ERR_ARG;
+    int off[2];
+    NBX_CUDA(cudaMemcpyAsync(off, ctx->d_sys_off + sys, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    unsigned e_beg = 0, e_end = 0, T = 0;
+    NBX_CUDA(cudaMemcpyAsync(&e_beg, ctx->d_ecount + off[0], sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    NBX_CUDA(cudaMemcpyAsync(&T, ctx->d_totals + 0, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    if (off[1] < ctx->nbodies)
+        NBX_CUDA(cudaMemcpyAsync(&e_end, ctx->d_ecount + off[1], sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    NBX_CUDA(cudaStreamSynchronize(st));
+    if (off[1] >= ctx->nbodies) e_end = T;
+    const int cells_before = (int)e_beg - off[0];
+    const int nc = (int)e_end - off[1] - cells_before;
+    if (ncells) *ncells = nc;
+    if (nc > cap_cells) {
+        ctx->last_error = "export: cell capacity too small";
+        return NBX_ERR_CAPACITY;
+    }
+    const int nb = off[1] - off[0];
+    if (perm) {
+        k_perm_export<<<ceil_div(nb, kBlock), kBlock, 0, st>>>(ctx->d_val, off[0], nb, perm);
+        ++ctx->launches;
+    }
+    if (root_child) NBX_CUDA(cudaMemsetAsync(root_child, 0xff, 8 * sizeof(int), st));
+    if (cell_child && nc > 0) NBX_CUDA(cudaMemsetAsync(cell_child, 0xff, 8 * sizeof(int) * (size_t)nc, st));
+    const int gn = ceil_div(ctx->cap_nodes, kBlock) < ctx->nsm * 8 ? ceil_div(ctx->cap_nodes, kBlock) : ctx->nsm * 8;
+    k_export<<<gn, kBlock, 0, st>>>(ctx->d_ent_alt, ctx->d_totals, ctx->d_body_sys, ctx->d_sys_off,
+                                    ctx->d_delta, ctx->d_ecount, ctx->d_key, ctx->d_key_lo, ctx->d_val,
+                                    ctx->d_parent, ctx->d_node4, ctx->d_sums, ctx->d_count, sys, cells_before,
+                                    cap_cells, root_child, cell_child, cell_start, cell_count, cell_level, cx,
+                                    cy, cz, cm, sum_mode);
+    ++ctx->launches;
+    NBX_CUDA(cudaGetLastError());
+    return NBX_OK;
+}
+
+}  // namespace nbx

@@ -1,0 +1,215 @@
+// walk.cu -- warp-coherent Barnes-Hut force walk (3D/CUDA/CUDA_NBody/src/Kernels.cu:460-577).
+//
+// One warp walks the tree for one aligned group of 32 consecutive sorted bodies
+// of a system.  Semantics of the reference: the root's children are always
+// opened (:505-517), a child body always interacts (:543), a child cell
+// interacts only if every body of the group accepts it, dp <= r (:543), with
+// dp = depth0 * 0.25^(L-1) for a level-L cell and r = |d|^2 + eps^2, else it is
+// pushed (:555-559).  a += m * d * rsqrt(r)^3 (:546-551), G = 1.
+// Differences by design: a root child that is a body interacts directly, the
+// stack holds int node ids and is bounded with an error flag, and r is
+// fma(dz,dz,fma(dy,dy,fma(dx,dx,eps2))) (the oracle uses the same rounding).
+//
+// Node layout: breadth-first node array, children of a cell contiguous;
+// node4 = (x, y, z, m) of the body / centre of mass, meta < 0 marks a body.
+// The 8 children of a popped cell are fetched by 8 lanes in one coalesced
+// access and broadcast with shuffles.
+#include "nbx_internal.cuh"
+
+namespace nbx {
+
+namespace {
+
+constexpr int kWalkWarps = 8;
+
+struct Acc {
+    float x = 0.f, y = 0.f, z = 0.f;
+};
+
+template <bool Comp>
+struct Accum;
+
+template <>
+struct Accum<false> {
+    float x = 0.f, y = 0.f, z = 0.f;
+    __device__ __forceinline__ void add(float f, float dx, float dy, float dz) {
+        x = fmaf(f, dx, x);
+        y = fmaf(f, dy, y);
+        z = fmaf(f, dz, z);
+    }
+    __device__ __forceinline__ void get(float &ox, float &oy, float &oz) const { ox = x; oy = y; oz = z; }
+};
+
+// Kahan-compensated accumulation per component.
+template <>
+struct Accum<true> {
+    float x = 0.f, y = 0.f, z = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    __device__ __forceinline__ static void kadd(float &s, float &c, float v) {
+        const float yv = __fsub_rn(v, c);
+        const float t = __fadd_rn(s, yv);
+        c = __fsub_rn(__fsub_rn(t, s), yv);
+        s = t;
+    }
+    __device__ __forceinline__ void add(float f, float dx, float dy, float dz) {
+        kadd(x, cx, __fmul_rn(f, dx));
+        kadd(y, cy, __fmul_rn(f, dy));
+        kadd(z, cz, __fmul_rn(f, dz));
+    }
+    __device__ __forceinline__ void get(float &ox, float &oy, float &oz) const { ox = x; oy = y; oz = z; }
+};
+
+template <bool Comp>
+__global__ void __launch_bounds__(kWalkWarps * 32)
+    k_walk(const float4 *__restrict__ node4, const int *__restrict__ meta, const float4 *__restrict__ body4,
+           const int *__restrict__ val, const int *__restrict__ groups, int ngroups,
+           const int *__restrict__ body_sys, const int *__restrict__ sys_off, const float *__restrict__ depth0,
+           const int *__restrict__ root_first, const int *__restrict__ root_nch, float eps2, int stack_cap,
+           float *__restrict__ ax, float *__restrict__ ay, float *__restrict__ az, int *__restrict__ nlist,
+           int *__restrict__ nopen, DevStatus *st) {
+    extern __shared__ int smem_stack[];
+    if (st->code != 0) return;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int *stack = smem_stack + w * stack_cap;
+    unsigned long long tot_len = 0ull, tot_open = 0ull;
+    for (int g = blockIdx.x * kWalkWarps + w; g < ngroups; g += gridDim.x * kWalkWarps) {
+        const int p0 = groups[g];
+        const int s = body_sys[p0];
+        const int end = min(sys_off[s + 1], p0 + 32);
+        const int p = p0 + lane;
+        const bool valid = p < end;
+        const float4 me = body4[valid ? p : p0];
+        const float d0 = depth0[s];
+        Accum<Comp> acc;
+        int top = 0, len = 0, opened = 0;
+        bool overflow = false;
+
+        // root children (level 1): bodies interact, cells are opened unconditionally
+        {
+            const int first = root_first[s], nch = min(root_nch[s], 8);
+            float4 c4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            int cm = 0;
+            if (lane < nch) {
+                c4 = node4[first + lane];
+                cm = meta[first + lane];
+            }
+            for (int j = 0; j < nch; j++) {
+                const int cmj = __shfl_sync(0xffffffffu, cm, j);
+                const float cx = __shfl_sync(0xffffffffu, c4.x, j);
+                const float cy = __shfl_sync(0xffffffffu, c4.y, j);
+                const float cz = __shfl_sync(0xffffffffu, c4.z, j);
+                const float cw = __shfl_sync(0xffffffffu, c4.w, j);
+                if (cmj < 0) {
+                    const float dx = cx - me.x, dy = cy - me.y, dz = cz - me.z;
+                    const float r = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+                    const float ri = rsqrtf(r);
+                    acc.add(cw * ri * ri * ri, dx, dy, dz);
+                    len++;
+                } else {
+                    if (lane == 0) stack[top] = (first + j) | (1 << kLevelShift);
+                    top++;
+                    opened++;
+                }
+            }
+            __syncwarp();
+        }
+
+        while (top > 0) {
+            const int e = stack[top - 1];
+            __syncwarp();
+            top--;
+            const int b = e & ((1 << kLevelShift) - 1);
+            const int lvl = e >> kLevelShift;
+            const int mb = meta[b];
+            const int first = mb & 0x0fffffff;
+            const int nch = ((mb >> 28) & 7) + 1;
+            const float dp = ldexpf(d0, -2 * lvl);
+            float4 c4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            int cm = 0;
+            if (lane < nch) {
+                c4 = node4[first + lane];
+                cm = meta[first + lane];
+            }
+            for (int j = 0; j < nch; j++) {
+                const int cmj = __shfl_sync(0xffffffffu, cm, j);
+                const float cx = __shfl_sync(0xffffffffu, c4.x, j);
+                const float cy = __shfl_sync(0xffffffffu, c4.y, j);
+                const float cz = __shfl_sync(0xffffffffu, c4.z, j);
+                const float cw = __shfl_sync(0xffffffffu, c4.w, j);
+                const float dx = cx - me.x, dy = cy - me.y, dz = cz - me.z;
+                const float r = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+                const bool accept = (cmj < 0) || __all_sync(0xffffffffu, !valid || dp <= r);
+                if (accept) {
+                    const float ri = rsqrtf(r);
+                    acc.add(cw * ri * ri * ri, dx, dy, dz);
+                    len++;
+                } else {
+                    if (top >= stack_cap) {
+                        overflow = true;
+                        break;
+                    }
+                    if (lane == 0) stack[top] = (first + j) | ((lvl + 1) << kLevelShift);
+                    top++;
+                    opened++;
+                }
+            }
+            __syncwarp();
+            if (overflow) break;
+        }
+        if (overflow) {
+            if (lane == 0) set_status(st, NBX_ERR_STACK, g);
+            continue;
+        }
+        if (valid) {
+            const int ob = val[p];
+            float fx, fy, fz;
+            acc.get(fx, fy, fz);
+            ax[ob] = fx;
+            ay[ob] = fy;
+            az[ob] = fz;
+            if (nlist) nlist[ob] = len;
+            if (nopen) nopen[ob] = opened;
+        }
+        tot_len += (unsigned long long)len * (unsigned long long)(end - p0);
+        tot_open += (unsigned long long)opened;
+    }
+    if (lane == 0 && (tot_len | tot_open)) {
+        atomicAdd(&st->interactions, tot_len);
+        atomicAdd(&st->opened, tot_open);
+    }
+}
+
+}  // namespace
+
+int walk_init(Ctx *ctx) {
+    const int smem = kWalkWarps * ctx->p.stack_depth * (int)sizeof(int);
+    NBX_CUDA(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->p.device));
+    NBX_CUDA(cudaFuncSetAttribute(k_walk<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    NBX_CUDA(cudaFuncSetAttribute(k_walk<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    return NBX_OK;
+}
+
+int walk_forces(Ctx *ctx, const nbx_state *s, cudaStream_t st) {
+    if (!ctx->built) return NBX_ERR_STATE;
+    const int cap = ctx->p.stack_depth;
+    const size_t smem = (size_t)kWalkWarps * cap * sizeof(int);
+    const int blocks_needed = ceil_div(ctx->ngroups, kWalkWarps);
+    const int grid = blocks_needed < ctx->nsm * 8 ? blocks_needed : ctx->nsm * 8;
+    if (grid <= 0) return NBX_OK;
+    if (ctx->compensated) {
+        k_walk<true><<<grid, kWalkWarps * 32, smem, st>>>(
+            ctx->d_node4, ctx->d_meta, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
+            ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay,
+            s->az, ctx->d_nlist, ctx->d_nopen, ctx->d_status);
+        ++ctx->launches;
+    } else {
+        k_walk<false><<<grid, kWalkWarps * 32, smem, st>>>(
+            ctx->d_node4, ctx->d_meta, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
+            ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay,
+            s->az, ctx->d_nlist, ctx->d_nopen, ctx->d_status);
+        ++ctx->launches;
+    }
+    NBX_CUDA(cudaGetLastError());
+    return NBX_OK;
+}
+
+}  // namespace nbx

@@ -1,0 +1,237 @@
+"""ctypes front end of the parity oracle (test infrastructure only).
+
+Wraps ``refemu.c`` (the CPU restatement of 3D/CUDA/CUDA_NBody/src/Kernels.cu)
+and, where it was built, the reference's own kernels run on the CPU
+(``_ref/libref_kernels.so``).  Only tests, the smoke check and the CPU-baseline
+leg of ``bench.py`` use this module, as a checker.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_ref = None
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(_build.build_oracle())
+        L = _lib
+        L.orc_bbox.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p]
+        L.orc_keys.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, _u64p, C.c_void_p]
+        L.orc_build.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int,
+                                _i32p, C.POINTER(C.c_int), _i32p, _i32p, _i32p, _i32p, _i32p,
+                                _f32p, _f32p, _f32p, _f32p, C.c_void_p, C.c_void_p]
+        L.orc_depth0.argtypes = [_f32p, C.c_float]
+        L.orc_depth0.restype = C.c_float
+        L.orc_forces.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, _i32p, C.c_int, _i32p,
+                                 _i32p, _f32p, _f32p, _f32p, _f32p, C.c_float, C.c_float, C.c_int,
+                                 C.c_void_p, C.c_int, _f32p, _f32p, _f32p, _f64p, _f64p, _f64p,
+                                 _i32p, _i32p]
+        L.orc_forces.restype = C.c_longlong
+        L.orc_update.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p,
+                                 _f32p, C.c_float, C.c_float]
+        L.orc_direct_fp64.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_double, C.c_int,
+                                      _i32p, _f64p, _f64p, _f64p]
+    return _lib
+
+
+def ref_lib():
+    """The reference kernels compiled for the CPU, or None where unavailable."""
+    global _ref
+    if _ref is None:
+        path = os.path.join(os.path.dirname(__file__), "_ref", "libref_kernels.so")
+        if not os.path.exists(path):
+            path = _build.build_ref_kernels()
+        if not path or not os.path.exists(path):
+            return None
+        _ref = C.CDLL(path)
+        _ref.ref_run_step.restype = C.c_int
+    return _ref
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def bbox(x, y, z):
+    out = np.zeros(6, np.float32)
+    lib().orc_bbox(len(x), _f32(x), _f32(y), _f32(z), out)
+    return out
+
+
+def keys(x, y, z, bb, levels=21):
+    n = len(x)
+    hi = np.zeros(n, np.uint64)
+    lo = np.zeros(n, np.uint64)
+    rc = lib().orc_keys(n, _f32(x), _f32(y), _f32(z), _f32(bb), levels, hi,
+                        lo.ctypes.data_as(C.c_void_p))
+    if rc:
+        raise ValueError("orc_keys rc=%d" % rc)
+    return hi, lo
+
+
+@dataclass
+class Tree:
+    n: int
+    bbox: np.ndarray
+    perm: np.ndarray
+    ncells: int
+    root_child: np.ndarray
+    cell_child: np.ndarray
+    cell_start: np.ndarray
+    cell_count: np.ndarray
+    cell_level: np.ndarray
+    cell_x: np.ndarray
+    cell_y: np.ndarray
+    cell_z: np.ndarray
+    cell_m: np.ndarray
+    cell_m64: np.ndarray | None = None
+    cell_com64: np.ndarray | None = None
+
+
+class OracleError(RuntimeError):
+    def __init__(self, rc, what):
+        super().__init__("%s failed with status %d" % (what, rc))
+        self.rc = rc
+
+
+def build(x, y, z, m, bb=None, max_depth=42):
+    n = len(x)
+    x, y, z, m = _f32(x), _f32(y), _f32(z), _f32(m)
+    if bb is None:
+        bb = bbox(x, y, z)
+    bb = _f32(bb)
+    cap = 2 * n + 4096
+    perm = np.zeros(n, np.int32)
+    nc = C.c_int(0)
+    rootc = np.zeros(8, np.int32)
+    cc = np.zeros(8 * cap, np.int32)
+    cs = np.zeros(cap, np.int32)
+    cn = np.zeros(cap, np.int32)
+    cl = np.zeros(cap, np.int32)
+    cx = np.zeros(cap, np.float32)
+    cy = np.zeros(cap, np.float32)
+    cz = np.zeros(cap, np.float32)
+    cm = np.zeros(cap, np.float32)
+    m64 = np.zeros(cap, np.float64)
+    com64 = np.zeros(3 * cap, np.float64)
+    rc = lib().orc_build(n, x, y, z, m, bb, max_depth, cap, perm, C.byref(nc), rootc, cc, cs, cn,
+                         cl, cx, cy, cz, cm, m64.ctypes.data_as(C.c_void_p),
+                         com64.ctypes.data_as(C.c_void_p))
+    if rc:
+        raise OracleError(rc, "orc_build")
+    k = nc.value
+    return Tree(n, bb, perm, k, rootc, cc[: 8 * k].reshape(k, 8).copy(), cs[:k].copy(),
+                cn[:k].copy(), cl[:k].copy(), cx[:k].copy(), cy[:k].copy(), cz[:k].copy(),
+                cm[:k].copy(), m64[:k].copy(), com64[: 3 * k].reshape(k, 3).copy())
+
+
+def depth0(bb, theta_ref):
+    return float(lib().orc_depth0(_f32(bb), C.c_float(theta_ref)))
+
+
+@dataclass
+class Forces:
+    a: np.ndarray        # (n,3) float32, plain FP32 walk (rows of unevaluated bodies are 0)
+    a64: np.ndarray      # (n,3) float64, FP64 evaluation of the same interaction lists
+    nlist: np.ndarray    # (n,) interaction-list length of the body's group
+    nopen: np.ndarray    # (n,) cells opened by the body's group
+    total: int           # sum over evaluated bodies of the list length
+
+
+def forces(x, y, z, m, tree: Tree, theta_ref, eps2, group=32, groups=None, depth0_value=None):
+    n = len(x)
+    x, y, z, m = _f32(x), _f32(y), _f32(z), _f32(m)
+    d0 = depth0(tree.bbox, theta_ref) if depth0_value is None else depth0_value
+    ax = np.zeros(n, np.float32); ay = np.zeros(n, np.float32); az = np.zeros(n, np.float32)
+    gx = np.zeros(n, np.float64); gy = np.zeros(n, np.float64); gz = np.zeros(n, np.float64)
+    nl = np.zeros(n, np.int32); no = np.zeros(n, np.int32)
+    cc = np.ascontiguousarray(tree.cell_child.reshape(-1), np.int32)
+    if cc.size == 0:
+        cc = np.full(8, -1, np.int32)
+    gptr, ng = None, 0
+    if groups is not None:
+        garr = np.ascontiguousarray(groups, np.int32)
+        gptr, ng = garr.ctypes.data_as(C.c_void_p), len(garr)
+    cxa = tree.cell_x if tree.ncells else np.zeros(1, np.float32)
+    cya = tree.cell_y if tree.ncells else np.zeros(1, np.float32)
+    cza = tree.cell_z if tree.ncells else np.zeros(1, np.float32)
+    cma = tree.cell_m if tree.ncells else np.zeros(1, np.float32)
+    tot = lib().orc_forces(n, x, y, z, m, np.ascontiguousarray(tree.perm, np.int32), tree.ncells,
+                           np.ascontiguousarray(tree.root_child, np.int32), cc,
+                           _f32(cxa), _f32(cya), _f32(cza), _f32(cma), C.c_float(d0),
+                           C.c_float(eps2), group, gptr, ng, ax, ay, az, gx, gy, gz, nl, no)
+    if tot < 0:
+        raise ValueError("orc_forces failed")
+    return Forces(np.stack([ax, ay, az], 1), np.stack([gx, gy, gz], 1), nl, no, int(tot))
+
+
+def update(x, y, z, vx, vy, vz, a, dt, d=1.0):
+    x, y, z, vx, vy, vz = (np.array(v, np.float32) for v in (x, y, z, vx, vy, vz))
+    a = np.asarray(a, np.float32)
+    lib().orc_update(len(x), x, y, z, vx, vy, vz, _f32(a[:, 0]), _f32(a[:, 1]), _f32(a[:, 2]),
+                     C.c_float(dt), C.c_float(d))
+    return x, y, z, vx, vy, vz
+
+
+def direct_fp64(x, y, z, m, eps2, targets):
+    t = np.ascontiguousarray(targets, np.int32)
+    ax = np.zeros(len(t)); ay = np.zeros(len(t)); az = np.zeros(len(t))
+    lib().orc_direct_fp64(len(x), _f32(x), _f32(y), _f32(z), _f32(m), C.c_double(eps2), len(t),
+                          t, ax, ay, az)
+    return np.stack([ax, ay, az], 1)
+
+
+def ref_step(x, y, z, vx, vy, vz, m, dt, force_bounds=None, stack_size=4096):
+    """One step of the reference's own kernels on the CPU (None if unavailable).
+
+    Returns a dict with the canonicalised tree, the forces (before the update)
+    and the updated state.  ``force_bounds`` replaces (minX, maxX) given to the
+    force kernel only, which scales its opening radius (Kernels.cu:477)."""
+    R = ref_lib()
+    if R is None:
+        return None
+    n = len(x)
+    x, y, z, vx, vy, vz = (np.array(v, np.float32) for v in (x, y, z, vx, vy, vz))
+    m = _f32(m)
+    cap = 2 * n + 12000
+    out = dict(bbox=np.zeros(6, np.float32), perm=np.zeros(n, np.int32),
+               root_child=np.zeros(8, np.int32), cell_child=np.zeros(8 * cap, np.int32),
+               cell_start=np.zeros(cap, np.int32), cell_count=np.zeros(cap, np.int32),
+               cell_level=np.zeros(cap, np.int32), cell_x=np.zeros(cap, np.float32),
+               cell_y=np.zeros(cap, np.float32), cell_z=np.zeros(cap, np.float32),
+               cell_m=np.zeros(cap, np.float32), ax=np.zeros(n, np.float32),
+               ay=np.zeros(n, np.float32), az=np.zeros(n, np.float32))
+    nc = C.c_int(0)
+    fmn, fmx = (float("nan"), float("nan")) if force_bounds is None else force_bounds
+    P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    rc = R.ref_run_step(C.c_int(n), P(x), P(y), P(z), P(vx), P(vy), P(vz), P(m), C.c_float(dt),
+                        C.c_float(fmn), C.c_float(fmx), C.c_int(stack_size), P(out["bbox"]),
+                        P(out["perm"]), C.byref(nc), C.c_int(cap), P(out["root_child"]),
+                        P(out["cell_child"]), P(out["cell_start"]), P(out["cell_count"]),
+                        P(out["cell_level"]), P(out["cell_x"]), P(out["cell_y"]),
+                        P(out["cell_z"]), P(out["cell_m"]), P(out["ax"]), P(out["ay"]),
+                        P(out["az"]))
+    if rc:
+        raise RuntimeError("ref_run_step rc=%d" % rc)
+    k = nc.value
+    out["ncells"] = k
+    out["cell_child"] = out["cell_child"][: 8 * k].reshape(k, 8)
+    for key in ("cell_start", "cell_count", "cell_level", "cell_x", "cell_y", "cell_z", "cell_m"):
+        out[key] = out[key][:k]
+    out["a"] = np.stack([out.pop("ax"), out.pop("ay"), out.pop("az")], 1)
+    out["state"] = (x, y, z, vx, vy, vz)
+    return out

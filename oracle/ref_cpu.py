@@ -1,0 +1,164 @@
+"""The reference's 3D/OpenMP tree code as the timed CPU baseline.
+
+TEST/BASELINE INFRASTRUCTURE ONLY.  ``stage()`` copies the reference's own
+sources (3D/OpenMP/OpenMP_NBody/src and include, minus the boost-dependent
+main.cpp / ConfigParser.cpp and the renderer) into the git-ignored
+``oracle/_ref/omp/`` and applies two documented changes:
+  * include/Constants.h is replaced by a shim with G = dt^2, TO_METERS = 1
+    (units of oracle/ref_shim/omp_harness.cpp);
+  * Interaction.cpp:130 initialises the bounding box it otherwise reads
+    uninitialised (`double xMin, ..., zMax = 0;`).
+The staged tree travels with the repository to the GPU host, where ``build()``
+compiles it (g++ -O3 -fopenmp) together with the harness.
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import shutil
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_ROOT = os.environ.get("NBX_REFERENCE_ROOT", "/root/reference")
+REF_OMP = os.path.join(REF_ROOT, "3D", "OpenMP", "OpenMP_NBody")
+STAGE = os.path.join(HERE, "_ref", "omp")
+RUNNER = os.path.join(STAGE, "runner")
+HARNESS = os.path.join(HERE, "ref_shim", "omp_harness.cpp")
+SKIP = {"main.cpp", "ConfigParser.cpp", "Renderer.cpp", "InitializeDistribution.cpp"}
+
+CONSTANTS_SHIM = """#ifndef CONSTANTS_H_
+#define CONSTANTS_H_
+/* staged shim: G = dt^2 and TO_METERS = 1 make one reference step one
+ * kick-drift step of length dt with G = 1 (see omp_harness.cpp) */
+#ifndef NBX_DT
+#define NBX_DT 5e-4
+#endif
+const double PI = 3.14159265358979323846;
+const double TO_METERS = 1.0;
+const double G = (NBX_DT) * (NBX_DT);
+extern int NUM_BODIES;
+extern int NUM_SUNS;
+extern double SYSTEM_SIZE;
+extern double SYSTEM_THICKNESS;
+extern double INNER_BOUND;
+extern double SOFTENING;
+extern double SOLAR_MASS;
+extern double EXTRA_MASS;
+extern double MAX_DISTANCE;
+extern int TIME_STEP;
+extern int STEP_COUNT;
+extern bool BINARY;
+extern double BINARY_SEPARATION;
+#define DEBUG_INFO false
+#endif
+"""
+
+
+def stage() -> bool:
+    """Copy the reference sources into oracle/_ref/omp (only where the checkout exists)."""
+    if not os.path.isdir(REF_OMP):
+        return os.path.isdir(os.path.join(STAGE, "src"))
+    for sub in ("src", "include"):
+        d = os.path.join(STAGE, sub)
+        os.makedirs(d, exist_ok=True)
+        for fn in os.listdir(os.path.join(REF_OMP, sub)):
+            if fn in SKIP or fn.startswith("cxxopts") or fn.startswith("ConfigParser"):
+                continue
+            shutil.copy(os.path.join(REF_OMP, sub, fn), os.path.join(d, fn))
+    with open(os.path.join(STAGE, "include", "Constants.h"), "w") as f:
+        f.write(CONSTANTS_SHIM)
+    p = os.path.join(STAGE, "src", "Interaction.cpp")
+    s = open(p).read()
+    s2 = re.sub(r"double xMin, xMax, yMin, yMax, zMin, zMax = 0;",
+                "double xMin = 0, xMax = 0, yMin = 0, yMax = 0, zMin = 0, zMax = 0;", s)
+    open(p, "w").write(s2)
+    return True
+
+
+def build(dt: float = 5e-4) -> str | None:
+    if not stage():
+        return None
+    srcs = sorted(os.path.join(STAGE, "src", f) for f in os.listdir(os.path.join(STAGE, "src"))
+                  if f.endswith(".cpp"))
+    stamp = os.path.join(STAGE, "dt.txt")
+    newest = max(os.path.getmtime(x) for x in srcs + [HARNESS])
+    if (os.path.exists(RUNNER) and os.path.getmtime(RUNNER) >= newest and os.path.exists(stamp)
+            and open(stamp).read() == repr(dt)):
+        return RUNNER
+    cmd = ["g++", "-O3", "-std=c++14", "-fopenmp", "-DNBX_DT=%r" % dt,
+           "-I", os.path.join(STAGE, "include"), HARNESS] + srcs + ["-o", RUNNER]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference OpenMP build failed:\n" + r.stderr[-3000:])
+    open(stamp, "w").write(repr(dt))
+    return RUNNER
+
+
+def _write_input(path, b, theta, eps, dt):
+    n = len(b.x)
+    with open(path, "wb") as f:
+        np.array([n], np.int32).tofile(f)
+        np.array([theta, eps], np.float32).tofile(f)
+        for a in (b.x, b.y, b.z):
+            np.asarray(a, np.float32).tofile(f)
+        for a in (b.vx, b.vy, b.vz):
+            (np.asarray(a, np.float64) * dt).astype(np.float32).tofile(f)
+        np.asarray(b.m, np.float32).tofile(f)
+
+
+def run(b, theta, eps, dt, steps, warmup, mode="sample", k=65536, threads=None, seed=1):
+    runner = build(dt)
+    if runner is None:
+        return None
+    env = dict(os.environ)
+    if threads:
+        env["OMP_NUM_THREADS"] = str(threads)
+    with tempfile.TemporaryDirectory() as td:
+        inp = os.path.join(td, "in.bin")
+        _write_input(inp, b, theta, eps, dt)
+        args = [runner, mode, inp, str(steps), str(warmup)]
+        if mode == "sample":
+            args += [str(k), str(seed)]
+        r = subprocess.run(args, capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError("reference runner failed: %s" % r.stderr[-2000:])
+    out = r.stdout[r.stdout.index("{"):]
+    return json.loads(out)
+
+
+def _workload(n):
+    from nns_gb300 import ic
+    return ic.binary_disk(n)
+
+
+def bench_openmp(n, steps, warmup, theta, eps, dt, k=16384):
+    """Reference arm: the reference's OpenMP code on all host cores.  The full
+    tree is built once (serially, as the reference does) and its time charged
+    to every step; each step runs the reference's parallel force loop on k
+    random bodies and its update; step time = build + force * n / k + update."""
+    b = _workload(n)
+    res = run(b, theta, eps, dt, steps, max(0, min(warmup, 1)), "sample", k)
+    if res is None:
+        return None
+    per = [sum(s) for s in res["steps"]]
+    t = float(np.median(per))
+    return {"steps_per_s": 1.0 / t, "cores": res["threads"],
+            "sample": "reference serial tree build over all %d bodies (timed once) + per step "
+                      "the reference OpenMP force loop over %d random bodies scaled by n/k + "
+                      "update; median of %d steps" % (n, k, len(per)),
+            "phases_s": {"build": float(np.median([s[0] for s in res["steps"]])),
+                         "force_scaled": float(np.median([s[1] for s in res["steps"]])),
+                         "update": float(np.median([s[2] for s in res["steps"]]))}}
+
+
+def cpu_baseline(n, theta, eps, dt, k=4096):
+    """One bounded sample (one step) for the cpu_baseline key of the GPU arm."""
+    r = bench_openmp(n, 1, 0, theta, eps, dt, k)
+    if r is None:
+        return {"unavailable": "reference CPU code not staged on this host"}
+    return {"value": r["steps_per_s"], "unit": "steps/s", "cores": r["cores"], "kind": "reference",
+            "sample": r["sample"], "phases_s": r["phases_s"]}

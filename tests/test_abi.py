@@ -1,0 +1,47 @@
+"""The C ABI library loads and exports every symbol include/nbx.h declares.
+
+CPU-only: no entry point that touches a GPU is called here."""
+import ctypes
+import os
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "nbx.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(nbx_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    from nns_gb300 import build
+    lib = ctypes.CDLL(build.build())
+    names = _declared()
+    assert len(names) >= 27
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header():
+    from nns_gb300 import _lib
+    assert set(_declared()) == set(_lib.SIGNATURES)
+
+
+def test_status_strings_without_gpu():
+    from nns_gb300 import _lib
+    L = _lib.lib()
+    assert L.nbx_status_string(3).decode().startswith("two bodies")
+    p = _lib.nbx_params()
+    L.nbx_params_default(ctypes.byref(p))
+    assert p.group == 32 and p.stack_depth >= 320 and abs(p.theta - 0.5) < 1e-7
+
+
+def test_create_rejects_bad_params_without_gpu():
+    from nns_gb300 import _lib
+    L = _lib.lib()
+    p = _lib.nbx_params()
+    L.nbx_params_default(ctypes.byref(p))
+    p.group = 16  # the walk group is a warp
+    h = ctypes.c_void_p()
+    assert L.nbx_create(ctypes.byref(p), ctypes.byref(h)) == 1

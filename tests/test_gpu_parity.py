@@ -1,0 +1,356 @@
+"""CUDA path (libnbx.so, through its C ABI) versus the oracle.
+
+Bit-exact: bounding box, keys order, sort permutation, canonical topology
+(child slots, cell start/count/level), FP64-summed centres of mass rounded to
+FP32, per-group interaction-list lengths and the update.
+Forces: the same interaction lists evaluated in FP32 (rsqrt and summation
+order differ) -- tolerance 1e-5 median / 1e-4 max relative error.
+"""
+import numpy as np
+import pytest
+
+from nns_gb300 import ic
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+MED_TOL, MAX_TOL = 1e-5, 1e-4
+
+
+def _ctx(n, nsys=1, **kw):
+    from nns_gb300.barnes_hut import Context
+    return Context(max_bodies=n, max_systems=nsys, **kw)
+
+
+def _state(b):
+    from nns_gb300.barnes_hut import State
+    return State.from_bodies(b)
+
+
+def _rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-30)
+
+
+def _check_tree(gt, ot):
+    assert np.array_equal(gt["perm"], ot.perm)
+    assert np.array_equal(gt["root_child"], ot.root_child)
+    assert gt["ncells"] == ot.ncells
+    assert np.array_equal(gt["cell_child"], ot.cell_child)
+    assert np.array_equal(gt["cell_start"], ot.cell_start)
+    assert np.array_equal(gt["cell_count"], ot.cell_count)
+    assert np.array_equal(gt["cell_level"], ot.cell_level)
+    for k in ("cell_x", "cell_y", "cell_z", "cell_m"):
+        assert np.array_equal(gt[k], getattr(ot, k)), k
+
+
+CASES = {
+    "disk64": lambda: ic.star_disk(64),
+    "disk1000": lambda: ic.star_disk(1000),
+    "disk16384": lambda: ic.star_disk(16384),
+    "plummer2048": lambda: ic.plummer(2048),
+    "binary4099": lambda: ic.binary_disk(4099),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("mac", ["theta0.5", "reference"])
+def test_build_and_forces_match_oracle(cuda, name, mac):
+    b = CASES[name]()
+    n = len(b.x)
+    kw = dict(theta=0.5, eps=0.01) if mac == "theta0.5" else dict(theta_ref=1.5, eps2=0.0025)
+    ctx = _ctx(n, **kw)
+    theta_ref, eps2 = ctx.constants()
+    ctx.set_systems([0, n])
+    s = _state(b)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    gt = ctx.export_tree(0)
+    ot = O.build(b.x, b.y, b.z, b.m)
+    _check_tree(gt, ot)
+    keys, perm = ctx.export_keys()
+    hi, _ = O.keys(b.x, b.y, b.z, ot.bbox, 21)
+    assert np.array_equal(perm, ot.perm)
+    assert np.array_equal(keys, hi[ot.perm])
+    f = O.forces(b.x, b.y, b.z, b.m, ot, theta_ref, eps2)
+    nl, no = ctx.walk_stats()
+    assert np.array_equal(nl, f.nlist)
+    assert np.array_equal(no, f.nopen)
+    rel = _rel(s.acc(), f.a)
+    assert np.median(rel) <= MED_TOL and rel.max() <= MAX_TOL, (np.median(rel), rel.max())
+    info = ctx.tree_info()
+    assert info["ncells"] == ot.ncells and info["status"] == 0
+    assert info["interactions"] == int(f.nlist.astype(np.int64).sum())
+
+
+def test_golden_reference_fixture(cuda):
+    """The reference's own kernels (tests/golden) against the CUDA path directly."""
+    import os
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "disk16384.npz")))
+    b = ic.Bodies(g["in_x"], g["in_y"], g["in_z"], g["in_vx"], g["in_vy"], g["in_vz"], g["in_m"])
+    n = len(b.x)
+    ctx = _ctx(n, theta_ref=1.5, eps2=0.0025)
+    ctx.set_systems([0, n])
+    s = _state(b)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    gt = ctx.export_tree(0)
+    for k in ("perm", "root_child", "cell_child", "cell_start", "cell_count", "cell_level"):
+        assert np.array_equal(gt[k], g[k]), k
+    # the reference's cell moments are FP32 atomic sums; ours are FP64 sums
+    rel = _rel(s.acc(), g["a"])
+    assert np.median(rel) < 1e-4, np.median(rel)
+
+
+def test_deep_refinement(cuda):
+    b = ic.star_disk(1024, seed=ic.SEED0 + 77)
+    x = b.x.copy()
+    for i in (100, 300, 500, 700, 900):
+        x[i + 1] = np.nextafter(np.nextafter(x[i], np.float32(2)), np.float32(2))
+        b.y[i + 1] = b.y[i]
+        b.z[i + 1] = b.z[i]
+    b = ic.Bodies(x, b.y, b.z, b.vx, b.vy, b.vz, b.m)
+    n = len(x)
+    ctx = _ctx(n, theta=0.5, eps=0.01)
+    ctx.set_systems([0, n])
+    s = _state(b)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    info = ctx.tree_info()
+    assert info["refined_runs"] >= 1 and info["max_level"] > 22
+    ot = O.build(b.x, b.y, b.z, b.m)
+    _check_tree(ctx.export_tree(0), ot)
+    t, e2 = ctx.constants()
+    f = O.forces(b.x, b.y, b.z, b.m, ot, t, e2)
+    rel = _rel(s.acc(), f.a)
+    assert np.median(rel) <= MED_TOL and rel.max() <= MAX_TOL
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 33, 100])
+def test_small_and_ragged(cuda, n):
+    b = ic.plummer(n, seed=ic.SEED0 + n)
+    ctx = _ctx(n, theta=0.5, eps=0.01)
+    ctx.set_systems([0, n])
+    s = _state(b)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    ot = O.build(b.x, b.y, b.z, b.m)
+    _check_tree(ctx.export_tree(0), ot)
+    t, e2 = ctx.constants()
+    f = O.forces(b.x, b.y, b.z, b.m, ot, t, e2)
+    rel = _rel(s.acc(), f.a)
+    if n > 1:
+        assert rel.max() <= MAX_TOL
+
+
+def test_split_planes(cuda):
+    g = np.arange(-8, 9) / 8.0
+    X, Y, Z = np.meshgrid(g, g, np.array([-0.25, 0.0, 0.25]), indexing="ij")
+    n = X.size
+    b = ic.Bodies(*(np.asarray(a, np.float32) for a in (X.ravel(), Y.ravel(), Z.ravel(), np.zeros(n),
+                                                        np.zeros(n), np.zeros(n), np.full(n, 1.0 / n))))
+    ctx = _ctx(n, theta=0.5, eps=0.01)
+    ctx.set_systems([0, n])
+    s = _state(b)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    ot = O.build(b.x, b.y, b.z, b.m)
+    _check_tree(ctx.export_tree(0), ot)
+
+
+def test_update_bit_exact(cuda):
+    b = ic.star_disk(5000)
+    n = len(b.x)
+    ctx = _ctx(n, theta=0.5, eps=0.01, dt=1e-3)
+    ctx.set_systems([0, n])
+    s = _state(b)
+    ctx.build(s)
+    ctx.forces(s)
+    a = s.acc()
+    ctx.integrate(s)
+    ctx.sync()
+    ref = O.update(b.x, b.y, b.z, b.vx, b.vy, b.vz, a, 1e-3)
+    for got, want in zip(s.host(), ref):
+        assert np.array_equal(got, want)
+
+
+def test_batched_equals_unbatched(cuda):
+    sizes = [1024, 37, 3000, 5, 2048, 777]
+    parts = [ic.star_disk(k, seed=ic.SEED0 + 1 + i) for i, k in enumerate(sizes)]
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    cat = lambda k: np.concatenate([getattr(p, k) for p in parts])  # noqa: E731
+    B = ic.Bodies(cat("x"), cat("y"), cat("z"), cat("vx"), cat("vy"), cat("vz"), cat("m"))
+    ctx = _ctx(int(off[-1]), nsys=len(sizes), theta=0.5, eps=0.01)
+    ctx.set_systems(off)
+    s = _state(B)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    accb = s.acc()
+    for i, p in enumerate(parts):
+        n = len(p.x)
+        c1 = _ctx(n, theta=0.5, eps=0.01)
+        c1.set_systems([0, n])
+        s1 = _state(p)
+        c1.build(s1)
+        c1.forces(s1)
+        c1.sync()
+        assert np.array_equal(accb[off[i]:off[i + 1]], s1.acc()), i
+        t1 = c1.export_tree(0)
+        tb = ctx.export_tree(i)
+        for k in ("perm", "root_child", "cell_child", "cell_m", "cell_x"):
+            assert np.array_equal(t1[k], tb[k]), (i, k)
+
+
+def test_graph_step_equals_eager(cuda):
+    b = ic.star_disk(4096)
+    n = len(b.x)
+    outs = []
+    for graph in (False, True):
+        ctx = _ctx(n, theta=0.5, eps=0.01, dt=1e-3)
+        ctx.set_systems([0, n])
+        s = _state(b)
+        if graph:
+            ctx.graph_step(s, 5)
+        else:
+            ctx.step(s, 5)
+        ctx.sync()
+        outs.append(s.host())
+    for a, c in zip(*outs):
+        assert np.array_equal(a, c)
+
+
+def test_trajectory_matches_oracle(cuda):
+    b = ic.star_disk(2048)
+    n = len(b.x)
+    ctx = _ctx(n, theta=0.5, eps=0.01, dt=1e-3)
+    ctx.set_systems([0, n])
+    s = _state(b)
+    x, y, z, vx, vy, vz = b.x, b.y, b.z, b.vx, b.vy, b.vz
+    t, e2 = ctx.constants()
+    for _ in range(10):
+        ctx.step(s, 1)
+        ot = O.build(x, y, z, b.m)
+        f = O.forces(x, y, z, b.m, ot, t, e2)
+        x, y, z, vx, vy, vz = O.update(x, y, z, vx, vy, vz, f.a, 1e-3)
+    ctx.sync()
+    gx = s.host()
+    err = np.abs(np.stack(gx[:3], 1) - np.stack([x, y, z], 1)).max()
+    assert err < 1e-5, err
+
+
+def test_compensated_close_to_plain(cuda):
+    b = ic.star_disk(8192)
+    n = len(b.x)
+    res = []
+    for comp in (False, True):
+        ctx = _ctx(n, theta=0.5, eps=0.01, compensated=comp)
+        ctx.set_systems([0, n])
+        s = _state(b)
+        ctx.build(s)
+        ctx.forces(s)
+        ctx.sync()
+        res.append(s.acc())
+    ot = O.build(b.x, b.y, b.z, b.m)
+    f = O.forces(b.x, b.y, b.z, b.m, ot, 0.25, 1e-4)
+    e_plain = _rel(res[0], f.a64)
+    e_comp = _rel(res[1], f.a64)
+    assert np.median(e_comp) <= np.median(e_plain) * 1.01
+    assert e_comp.max() <= MAX_TOL
+
+
+def test_direct_fp64_matches_oracle(cuda):
+    b = ic.plummer(3000)
+    ctx = _ctx(len(b.x))
+    ctx.set_systems([0, len(b.x)])
+    s = _state(b)
+    tg = np.arange(0, 3000, 7)
+    got = ctx.direct_fp64(s, tg, 1e-4).cpu().numpy()
+    want = O.direct_fp64(b.x, b.y, b.z, b.m, 1e-4, tg)
+    assert np.allclose(got, want, rtol=1e-12, atol=1e-14)
+
+
+def test_errors_are_reported(cuda):
+    from nns_gb300._lib import NbxError
+    b = ic.star_disk(300)
+    x = b.x.copy()
+    x[10] = x[11]
+    b.y[10] = b.y[11]
+    b.z[10] = b.z[11]
+    b2 = ic.Bodies(x, b.y, b.z, b.vx, b.vy, b.vz, b.m)
+    ctx = _ctx(300)
+    ctx.set_systems([0, 300])
+    s = _state(b2)
+    ctx.build(s)
+    ctx.forces(s)
+    with pytest.raises(NbxError) as e:
+        ctx.sync()
+    assert e.value.code == 3  # NBX_ERR_DEPTH
+    # NaN position
+    x = b.x.copy()
+    x[5] = np.nan
+    s = _state(ic.Bodies(x, b.y, b.z, b.vx, b.vy, b.vz, b.m))
+    ctx.build(s)
+    ctx.forces(s)
+    with pytest.raises(NbxError) as e:
+        ctx.sync()
+    assert e.value.code == 6  # NBX_ERR_NONFINITE
+    # the context stays usable
+    s = _state(b)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+
+
+def test_kernels_wrapper_sequence(cuda):
+    """The reference's BarnesHut::update sequence through the phase entry points."""
+    from nns_gb300.barnes_hut import BarnesHut
+    b = ic.star_disk(3000)
+    n = len(b.x)
+    bh = BarnesHut(b, theta_ref=1.5, eps2=0.0025, timestep=1e-3)
+    bh.update(0)
+    child = bh.d_child.cpu().numpy()
+    ot = O.build(b.x, b.y, b.z, b.m)
+    assert np.array_equal(child[:8], ot.root_child)
+    assert np.array_equal(child[8 * n:8 * (n + ot.ncells)].reshape(-1, 8), ot.cell_child)
+    assert int(bh.d_index.item()) == n + ot.ncells
+    assert np.array_equal(bh.d_sorted[:n].cpu().numpy(), ot.perm)
+    assert np.array_equal(bh.d_start[n:n + ot.ncells].cpu().numpy(), ot.cell_start)
+    assert np.array_equal(bh.d_count[n:n + ot.ncells].cpu().numpy(), ot.cell_count)
+    assert np.array_equal(bh.d_x[n:n + ot.ncells].cpu().numpy(), ot.cell_x)
+    assert np.array_equal(bh.d_mass[n:n + ot.ncells].cpu().numpy(), ot.cell_m)
+    f = O.forces(b.x, b.y, b.z, b.m, ot, 1.5, 0.0025)
+    acc = np.stack([bh.d_ax[:n].cpu().numpy(), bh.d_ay[:n].cpu().numpy(), bh.d_az[:n].cpu().numpy()], 1)
+    rel = _rel(acc, f.a)
+    assert rel.max() <= MAX_TOL
+    st = O.update(b.x, b.y, b.z, b.vx, b.vy, b.vz, acc, 1e-3)
+    assert np.array_equal(bh.h_x, st[0]) and np.array_equal(bh.h_vz, st[5])
+    assert set(bh.times) >= {"buildTree", "computeForces"}
+
+
+def test_plummer_2p20_properties(cuda):
+    """The 2^20-body Plummer workload: exact tree, forces on sampled groups."""
+    b = ic.plummer(1 << 20)
+    n = len(b.x)
+    ctx = _ctx(n, theta=0.6, eps=0.005)
+    ctx.set_systems([0, n])
+    s = _state(b)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    ot = O.build(b.x, b.y, b.z, b.m)
+    _check_tree(ctx.export_tree(0), ot)
+    t, e2 = ctx.constants()
+    groups = np.random.default_rng(1).choice(n // 32, 128, replace=False)
+    f = O.forces(b.x, b.y, b.z, b.m, ot, t, e2, groups=groups)
+    idx = np.concatenate([ot.perm[g * 32:(g + 1) * 32] for g in groups])
+    rel = _rel(s.acc()[idx], f.a[idx])
+    assert np.median(rel) <= MED_TOL and rel.max() <= MAX_TOL
+    nl, _ = ctx.walk_stats()
+    assert np.array_equal(nl[idx], f.nlist[idx])
