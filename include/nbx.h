@@ -59,13 +59,15 @@ typedef struct nbx_params {
     float gravity;     /* accepted for interface parity; the force uses G = 1 (Kernels.cu:462) */
     int group;         /* bodies sharing one walk (warp-coherent MAC vote): 32 */
     int stack_depth;   /* walk stack entries per warp */
-    int compensated;   /* 0 plain FP32 accumulation, 1 compensated FP32 */
+    int compensated;   /* 0 plain FP32; 1 split compensation (FP32 partial sums per
+                          walk round, Kahan across rounds); 2 Kahan on every term */
     int leaf_size;     /* bodies per leaf: 1 */
     int radix_bits;    /* radix digit width of the key sort: 8 */
     int walk_warps;    /* warps per block of the walk kernel (0 = autotuned default) */
     int device;        /* CUDA device ordinal */
     int block_size;    /* reference launch-shape hints (main.cu:30-31); informational */
     int grid_size;
+    int walk_variant;  /* 0 production walk; 2 one-cell-at-a-time walk (comparison) */
 } nbx_params;
 
 /* SoA device state of all systems; systems are contiguous ranges. */
@@ -98,6 +100,9 @@ const char *nbx_last_error(nbx_ctx *ctx);
 /* Current effective MAC constant and softening of the context. */
 int nbx_get_constants(nbx_ctx *ctx, float *theta_ref, float *eps2);
 int nbx_set_constants(nbx_ctx *ctx, float theta_ref, float eps2, int compensated);
+/* Launch shape of the walk: warps per block (4, 8 or 16) and variant; used by
+ * the autotuner (nns_gb300/autotune.py). */
+int nbx_set_walk_config(nbx_ctx *ctx, int warps_per_block, int variant);
 
 /* ---- reference-compatible phase entry points (KernelsWrapper.cu) ---- */
 /* KernelsWrapper::resetArrays (KernelsWrapper.cu:28; Kernels.cu:21-64) */
@@ -171,6 +176,9 @@ int nbx_export_walk_stats(nbx_ctx *ctx, int *nlist, int *nopen, void *stream);
  * [0,n): acc[3*t+k] += sum_j m_j d (|d|^2+eps2)^-3/2 in FP64. */
 int nbx_direct_fp64(nbx_ctx *ctx, const float *x, const float *y, const float *z, const float *m,
                     int n, const int *targets, int nt, double eps2, double *acc, void *stream);
+/* Per-body potential phi_i = -sum_j m_j / sqrt(|d|^2+eps2) over the walk's
+ * interaction lists (self term removed), original index order; needs eps2 > 0. */
+int nbx_potential(nbx_ctx *ctx, const nbx_state *s, float *phi, void *stream);
 /* FP64 diagnostics of bodies [0,n): out[0..2] momentum, out[3] kinetic energy,
  * out[4..6] angular momentum, out[7] total mass (device double[8]). */
 int nbx_diagnostics_fp64(nbx_ctx *ctx, const nbx_state *s, int n, double *out, void *stream);

@@ -25,7 +25,8 @@ class nbx_params(C.Structure):
                 ("dt", C.c_float), ("dampening", C.c_float), ("gravity", C.c_float),
                 ("group", C.c_int), ("stack_depth", C.c_int), ("compensated", C.c_int),
                 ("leaf_size", C.c_int), ("radix_bits", C.c_int), ("walk_warps", C.c_int),
-                ("device", C.c_int), ("block_size", C.c_int), ("grid_size", C.c_int)]
+                ("device", C.c_int), ("block_size", C.c_int), ("grid_size", C.c_int),
+                ("walk_variant", C.c_int)]
 
 
 class nbx_state(C.Structure):
@@ -60,6 +61,7 @@ SIGNATURES = {
     "nbx_sort": (_I, [_P] + [_P] * 5 + [_I, _P, _PF]),
     "nbx_compute_forces": (_I, [_P] + [_P] * 14 + [_I, _F, _P, _PF]),
     "nbx_update": (_I, [_P] + [_P] * 9 + [_I, _F, _F, _P, _PF]),
+    "nbx_set_walk_config": (_I, [_P, _I, _I]),
     "nbx_set_systems": (_I, [_P, _I, C.POINTER(C.c_int64)]),
     "nbx_build": (_I, [_P, C.POINTER(nbx_state), _P]),
     "nbx_forces": (_I, [_P, C.POINTER(nbx_state), _P]),
@@ -72,6 +74,7 @@ SIGNATURES = {
     "nbx_export_keys": (_I, [_P, _P, _P, _P]),
     "nbx_export_walk_stats": (_I, [_P, _P, _P, _P]),
     "nbx_direct_fp64": (_I, [_P, _P, _P, _P, _P, _I, _P, _I, C.c_double, _P, _P]),
+    "nbx_potential": (_I, [_P, C.POINTER(nbx_state), _P, _P]),
     "nbx_diagnostics_fp64": (_I, [_P, C.POINTER(nbx_state), _I, _P, _P]),
 }
 

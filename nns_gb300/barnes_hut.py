@@ -39,7 +39,7 @@ class Context:
 
     def __init__(self, max_bodies: int, max_systems: int = 1, theta: float = 0.5,
                  theta_ref: float | None = None, eps: float = 0.05, eps2: float | None = None,
-                 dt: float = 1e-3, dampening: float = 1.0, compensated: bool = False,
+                 dt: float = 1e-3, dampening: float = 1.0, compensated: int = 0,
                  stack_depth: int = 512, device: int = 0):
         p = L.nbx_params()
         lib().nbx_params_default(C.byref(p))
@@ -51,7 +51,7 @@ class Context:
         p.eps2 = eps2 or 0.0
         p.dt = dt
         p.dampening = dampening
-        p.compensated = 1 if compensated else 0
+        p.compensated = int(compensated)
         p.stack_depth = stack_depth
         p.device = device
         self.params = p
@@ -78,9 +78,15 @@ class Context:
         check(lib().nbx_get_constants(self.h, C.byref(t), C.byref(e)), "nbx_get_constants")
         return t.value, e.value
 
-    def set_constants(self, theta_ref: float, eps2: float, compensated: bool = False):
-        check(lib().nbx_set_constants(self.h, theta_ref, eps2, 1 if compensated else 0),
+    def set_constants(self, theta_ref: float, eps2: float, compensated: int = 0):
+        """compensated: 0 plain FP32, 1 split compensation, 2 Kahan on every term."""
+        check(lib().nbx_set_constants(self.h, theta_ref, eps2, int(compensated)),
               "nbx_set_constants", self.h)
+
+    def set_walk(self, warps_per_block: int = 8, variant: int = 0):
+        """Walk launch shape (4/8/16 warps per block) and variant (0 production, 2 simple)."""
+        check(lib().nbx_set_walk_config(self.h, warps_per_block, variant), "nbx_set_walk_config",
+              self.h)
 
     def set_systems(self, offsets):
         off = np.ascontiguousarray(offsets, dtype=np.int64)
@@ -166,6 +172,14 @@ class Context:
                                     _ptr(t), len(t), eps2, _ptr(acc), _stream_ptr(stream)),
               "nbx_direct_fp64", self.h)
         return acc.view(-1, 3)
+
+    def potential(self, s: "State", stream=None) -> np.ndarray:
+        """Per-body potential over the last build's interaction lists (original order)."""
+        n = int(self.offsets[-1])
+        phi = torch.empty(n, dtype=torch.float32, device=self.device)
+        check(lib().nbx_potential(self.h, C.byref(s.c), _ptr(phi), _stream_ptr(stream)),
+              "nbx_potential", self.h)
+        return phi.cpu().numpy()
 
     def diagnostics(self, s: "State", n: int | None = None, stream=None):
         out = torch.zeros(8, dtype=torch.float64, device=self.device)

@@ -165,7 +165,9 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     ctx->theta_ref = p->theta_ref > 0.f ? p->theta_ref : p->theta * p->theta;
     ctx->eps2 = p->eps2 > 0.f ? p->eps2 : p->eps * p->eps;
     ctx->compensated = p->compensated;
-    if (!(ctx->theta_ref > 0.f)) {
+    ctx->walk_variant = p->walk_variant;
+    if (p->walk_warps == 4 || p->walk_warps == 8 || p->walk_warps == 16) ctx->walk_warps = p->walk_warps;
+    if (!(ctx->theta_ref > 0.f) || p->compensated < 0 || p->compensated > 2) {
         delete ctx;
         return NBX_ERR_ARG;
     }
@@ -260,7 +262,22 @@ int nbx_set_constants(nbx_ctx *c, float theta_ref, float eps2, int compensated) 
     Ctx *ctx = C(c);
     ctx->theta_ref = theta_ref;
     ctx->eps2 = eps2;
-    ctx->compensated = compensated ? 1 : 0;
+    if (compensated < 0 || compensated > 2) return NBX_ERR_ARG;
+    ctx->compensated = compensated;
+    if (ctx->graph_exec) {
+        cudaGraphExecDestroy(ctx->graph_exec);
+        ctx->graph_exec = nullptr;
+    }
+    return NBX_OK;
+}
+
+int nbx_set_walk_config(nbx_ctx *c, int warps_per_block, int variant) {
+    if (!c || !(warps_per_block == 4 || warps_per_block == 8 || warps_per_block == 16) ||
+        !(variant == 0 || variant == 2))
+        return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    ctx->walk_warps = warps_per_block;
+    ctx->walk_variant = variant;
     if (ctx->graph_exec) {
         cudaGraphExecDestroy(ctx->graph_exec);
         ctx->graph_exec = nullptr;
@@ -584,6 +601,12 @@ int nbx_direct_fp64(nbx_ctx *c, const float *x, const float *y, const float *z, 
                     const int *targets, int nt, double eps2, double *acc, void *stream) {
     if (!c || !x || !y || !z || !m || !targets || !acc || n < 0 || nt < 0) return NBX_ERR_ARG;
     return nbx::direct_fp64(C(c), x, y, z, m, n, targets, nt, eps2, acc, S(stream));
+}
+
+int nbx_potential(nbx_ctx *c, const nbx_state *s, float *phi, void *stream) {
+    if (!c || !s || !phi) return NBX_ERR_ARG;
+    if (!(C(c)->eps2 > 0.f)) return NBX_ERR_ARG;
+    return nbx::walk_potential(C(c), s, phi, S(stream));
 }
 
 int nbx_diagnostics_fp64(nbx_ctx *c, const nbx_state *s, int n, double *out, void *stream) {

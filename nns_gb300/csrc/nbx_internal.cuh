@@ -32,7 +32,9 @@ struct DevStatus {
 struct Ctx {
     nbx_params p;
     float theta_ref, eps2;
-    int compensated;
+    int compensated;       // 0 plain, 1 split-compensated, 2 Kahan per term
+    int walk_variant = 0;  // 0 production walk (walk2.cu), 2 one-cell-at-a-time walk (walk.cu)
+    int walk_warps = 8;    // warps per block of the production walk
     std::string last_error;
 
     // capacity
@@ -166,6 +168,7 @@ int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox
 // walk.cu
 int walk_init(Ctx *ctx);
 int walk_forces(Ctx *ctx, const nbx_state *s, cudaStream_t st);
+int walk_potential(Ctx *ctx, const nbx_state *s, float *pot, cudaStream_t st);
 // integrate.cu
 int integrate(Ctx *ctx, const nbx_state *s, float dt, float d, int n, cudaStream_t st);
 

@@ -180,16 +180,25 @@ __global__ void __launch_bounds__(kWalkWarps * 32)
 
 }  // namespace
 
+int walk2_init(Ctx *ctx);
+int walk2_forces(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st);
+
 int walk_init(Ctx *ctx) {
     const int smem = kWalkWarps * ctx->p.stack_depth * (int)sizeof(int);
     NBX_CUDA(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->p.device));
     NBX_CUDA(cudaFuncSetAttribute(k_walk<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     NBX_CUDA(cudaFuncSetAttribute(k_walk<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    return NBX_OK;
+    return walk2_init(ctx);
+}
+
+int walk_potential(Ctx *ctx, const nbx_state *s, float *pot, cudaStream_t st) {
+    if (!ctx->built) return NBX_ERR_STATE;
+    return walk2_forces(ctx, s, pot, ctx->walk_warps, st);
 }
 
 int walk_forces(Ctx *ctx, const nbx_state *s, cudaStream_t st) {
     if (!ctx->built) return NBX_ERR_STATE;
+    if (ctx->walk_variant != 2) return walk2_forces(ctx, s, nullptr, ctx->walk_warps, st);
     const int cap = ctx->p.stack_depth;
     const size_t smem = (size_t)kWalkWarps * cap * sizeof(int);
     const int blocks_needed = ceil_div(ctx->ngroups, kWalkWarps);

@@ -45,6 +45,8 @@ def lib():
                                  _f32p, C.c_float, C.c_float]
         L.orc_direct_fp64.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_double, C.c_int,
                                       _i32p, _f64p, _f64p, _f64p]
+        L.orc_direct_pot_fp64.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_double, C.c_int,
+                                          _i32p, _f64p]
     return _lib
 
 
@@ -193,6 +195,14 @@ def direct_fp64(x, y, z, m, eps2, targets):
     lib().orc_direct_fp64(len(x), _f32(x), _f32(y), _f32(z), _f32(m), C.c_double(eps2), len(t),
                           t, ax, ay, az)
     return np.stack([ax, ay, az], 1)
+
+
+def direct_potential_fp64(x, y, z, m, eps2, targets):
+    t = np.ascontiguousarray(targets, np.int32)
+    phi = np.zeros(len(t))
+    lib().orc_direct_pot_fp64(len(x), _f32(x), _f32(y), _f32(z), _f32(m), C.c_double(eps2), len(t),
+                              t, phi)
+    return phi
 
 
 def ref_step(x, y, z, vx, vy, vz, m, dt, force_bounds=None, stack_size=4096):

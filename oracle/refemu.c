@@ -437,3 +437,20 @@ void orc_direct_fp64(int n, const float *x, const float *y, const float *z, cons
         ax[t] = sx; ay[t] = sy; az[t] = sz;
     }
 }
+
+/* FP64 direct-sum potential phi_i = -sum_{j != i} m_j / sqrt(|d|^2 + eps2) */
+void orc_direct_pot_fp64(int n, const float *x, const float *y, const float *z, const float *m,
+                         double eps2, int nt, const int *targets, double *phi)
+{
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int t = 0; t < nt; t++) {
+        int i = targets[t];
+        double xi = x[i], yi = y[i], zi = z[i], s = 0;
+        for (int j = 0; j < n; j++) {
+            if (j == i) continue;
+            double dx = (double)x[j] - xi, dy = (double)y[j] - yi, dz = (double)z[j] - zi;
+            s -= (double)m[j] / sqrt(dx * dx + dy * dy + dz * dz + eps2);
+        }
+        phi[t] = s;
+    }
+}

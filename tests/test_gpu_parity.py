@@ -56,11 +56,13 @@ CASES = {
 
 @pytest.mark.parametrize("name", list(CASES))
 @pytest.mark.parametrize("mac", ["theta0.5", "reference"])
-def test_build_and_forces_match_oracle(cuda, name, mac):
+@pytest.mark.parametrize("variant", [0, 2], ids=["walk2", "walk1"])
+def test_build_and_forces_match_oracle(cuda, name, mac, variant):
     b = CASES[name]()
     n = len(b.x)
     kw = dict(theta=0.5, eps=0.01) if mac == "theta0.5" else dict(theta_ref=1.5, eps2=0.0025)
     ctx = _ctx(n, **kw)
+    ctx.set_walk(8, variant)
     theta_ref, eps2 = ctx.constants()
     ctx.set_systems([0, n])
     s = _state(b)
@@ -245,11 +247,12 @@ def test_trajectory_matches_oracle(cuda):
     assert err < 1e-5, err
 
 
-def test_compensated_close_to_plain(cuda):
+@pytest.mark.parametrize("mode", [1, 2])
+def test_compensated_close_to_plain(cuda, mode):
     b = ic.star_disk(8192)
     n = len(b.x)
     res = []
-    for comp in (False, True):
+    for comp in (0, mode):
         ctx = _ctx(n, theta=0.5, eps=0.01, compensated=comp)
         ctx.set_systems([0, n])
         s = _state(b)
@@ -263,6 +266,40 @@ def test_compensated_close_to_plain(cuda):
     e_comp = _rel(res[1], f.a64)
     assert np.median(e_comp) <= np.median(e_plain) * 1.01
     assert e_comp.max() <= MAX_TOL
+
+
+@pytest.mark.parametrize("warps", [4, 8, 16])
+def test_walk_launch_shapes_agree(cuda, warps):
+    b = ic.plummer(5000)
+    n = len(b.x)
+    out = []
+    for w in (8, warps):
+        ctx = _ctx(n, theta=0.6, eps=0.005)
+        ctx.set_walk(w, 0)
+        ctx.set_systems([0, n])
+        s = _state(b)
+        ctx.build(s)
+        ctx.forces(s)
+        ctx.sync()
+        out.append(s.acc())
+    assert np.array_equal(out[0], out[1])
+
+
+def test_potential_energy(cuda):
+    b = ic.plummer(4096)
+    n = len(b.x)
+    ctx = _ctx(n, theta=0.5, eps=0.01)
+    ctx.set_systems([0, n])
+    s = _state(b)
+    ctx.build(s)
+    phi = ctx.potential(s)
+    ctx.sync()
+    want = O.direct_potential_fp64(b.x, b.y, b.z, b.m, 1e-4, np.arange(n))
+    rel = np.abs(phi - want) / np.abs(want)
+    assert np.median(rel) < 1e-3 and rel.max() < 2e-2
+    # Plummer sphere: W = -3 pi / 32 (G = M = a = 1), softened slightly
+    W = 0.5 * float((b.m.astype(np.float64) * phi).sum())
+    assert abs(W + 3 * np.pi / 32) < 0.02
 
 
 def test_direct_fp64_matches_oracle(cuda):
