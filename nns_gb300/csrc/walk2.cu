@@ -91,7 +91,7 @@ __device__ __forceinline__ void put_cand(WarpBuf &w, int slot, float4 q, float d
 }
 
 template <int Mode, bool Pot>
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(512, 1)
     k_walk2(const float4 *__restrict__ node4, const int *__restrict__ meta, const float4 *__restrict__ body4,
             const int *__restrict__ val, const int *__restrict__ groups, int ngroups,
             const int *__restrict__ body_sys, const int *__restrict__ sys_off, const float *__restrict__ depth0,
