@@ -123,7 +123,7 @@ void nbx_params_default(nbx_params *p) {
     p->dampening = 1.f;
     p->gravity = 1.f;
     p->group = 32;
-    p->stack_depth = 512;
+    p->stack_depth = 384;
     p->compensated = 0;
     p->leaf_size = 1;
     p->radix_bits = 8;

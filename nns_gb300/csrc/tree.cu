@@ -21,8 +21,8 @@
 //           same position.  The k-th first child in BFS order belongs to the k-th
 //           cell in BFS order (roots first), so two prefix counts give every cell's
 //           child block and every node's parent -- no search, no locks.
-//  moments  bottom-up FP64 sums in child order; the last child to arrive at a
-//           parent (one atomic per node) sums it, so results are deterministic.
+//  moments  bottom-up FP64 sums in child order, one BFS level per launch,
+//           deepest first; deterministic.
 #include "nbx_internal.cuh"
 
 namespace nbx {
@@ -361,50 +361,48 @@ __global__ void __launch_bounds__(kBlock) k_nodes_b(const unsigned *__restrict__
     }
 }
 
-// Bottom-up FP64 moments: the last child to arrive sums its parent in child order.
-__global__ void __launch_bounds__(kBlock) k_moments(int n, const int *__restrict__ body_node,
-                                                     const int *__restrict__ parent,
-                                                     const int *__restrict__ meta, float4 *node4,
-                                                     double4 *sums, int *count, int *arrive,
-                                                     const DevStatus *st) {
+// Bottom-up FP64 moments, one BFS level per launch (deepest first): a cell sums
+// its children -- contiguous, one level below, already final -- in child order,
+// so the result is deterministic.  Level L occupies BFS indices
+// [start(L), start(L+1)); start(L) is the scanned count of level-sort digit 4L.
+__global__ void __launch_bounds__(kBlock) k_moments_level(int level, const unsigned *__restrict__ lvl_off,
+                                                           int ntiles, const unsigned *__restrict__ totals,
+                                                           const int *__restrict__ meta, float4 *node4,
+                                                           double4 *sums, int *count, const DevStatus *st) {
     if (st->code != 0) return;  // an inconsistent tree is never summed
-    for (int p = grid_stride_start(); p < n; p += grid_stride()) {
-        int cur = body_node[p];
-        for (int guard = 0; guard < 64; guard++) {
-            const int par = parent[cur];
-            if (par < 0) break;
-            const int pm = meta[par];
-            const int first = pm & 0x0fffffff;
-            const int nch = ((pm >> 28) & 7) + 1;
-            __threadfence();
-            if (atomicAdd(&arrive[par], 1) != nch - 1) break;
-            __threadfence();
-            double sm = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
-            int cnt = 0;
-            for (int c = first; c < first + nch; c++) {
-                if (meta[c] < 0) {
-                    const float4 q = node4[c];
-                    const double mb = (double)q.w;
-                    sm += mb;
-                    sx += mb * (double)q.x;
-                    sy += mb * (double)q.y;
-                    sz += mb * (double)q.z;
-                    cnt += 1;
-                } else {
-                    const double2 a = __ldcg(reinterpret_cast<const double2 *>(&sums[c]));
-                    const double2 b = __ldcg(reinterpret_cast<const double2 *>(&sums[c]) + 1);
-                    sm += a.x;
-                    sx += a.y;
-                    sy += b.x;
-                    sz += b.y;
-                    cnt += __ldcg(&count[c]);
-                }
+    const unsigned T = totals[1];
+    unsigned beg = lvl_off[(size_t)(level << 2) * ntiles];
+    unsigned end = lvl_off[(size_t)((level + 1) << 2) * ntiles];
+    if (end > T) end = T;
+    if (beg > end) beg = end;
+    for (unsigned b = beg + grid_stride_start(); b < end; b += grid_stride()) {
+        const int pm = meta[b];
+        if (pm < 0) continue;  // body
+        const int first = pm & 0x0fffffff;
+        const int nch = ((pm >> 28) & 7) + 1;
+        double sm = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
+        int cnt = 0;
+        for (int c = first; c < first + nch; c++) {
+            if (meta[c] < 0) {
+                const float4 q = node4[c];
+                const double mb = (double)q.w;
+                sm += mb;
+                sx += mb * (double)q.x;
+                sy += mb * (double)q.y;
+                sz += mb * (double)q.z;
+                cnt += 1;
+            } else {
+                const double4 v = sums[c];
+                sm += v.x;
+                sx += v.y;
+                sy += v.z;
+                sz += v.w;
+                cnt += count[c];
             }
-            sums[par] = make_double4(sm, sx, sy, sz);
-            count[par] = cnt;
-            node4[par] = make_float4((float)(sx / sm), (float)(sy / sm), (float)(sz / sm), (float)sm);
-            cur = par;
         }
+        sums[b] = make_double4(sm, sx, sy, sz);
+        count[b] = cnt;
+        node4[b] = make_float4((float)(sx / sm), (float)(sy / sm), (float)(sz / sm), (float)sm);
     }
 }
 
@@ -467,9 +465,13 @@ int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox
                                      ctx->d_delta, ctx->d_flags, S, ctx->d_fcl, ctx->d_cl, ctx->d_meta,
                                      ctx->d_parent, ctx->d_root_first, ctx->d_root_nch, ctx->d_status);
     ++ctx->launches;
-    k_moments<<<gb, kBlock, 0, st>>>(n, ctx->d_body_node, ctx->d_parent, ctx->d_meta, ctx->d_node4,
-                                     ctx->d_sums, ctx->d_count, ctx->d_arrive, ctx->d_status);
-    ++ctx->launches;
+    // cells exist at levels 1..41 (two bodies share at most 41 levels without error)
+    for (int level = kMaxLevel - 2; level >= 1; level--) {
+        k_moments_level<<<ctx->nsm * 4, kBlock, 0, st>>>(level, ctx->d_hist, ctx->cap_tiles_node, ctx->d_totals,
+                                                         ctx->d_meta, ctx->d_node4, ctx->d_sums, ctx->d_count,
+                                                         ctx->d_status);
+        ++ctx->launches;
+    }
     NBX_CUDA(cudaGetLastError());
     ctx->built = true;
     return NBX_OK;

@@ -4,20 +4,19 @@
 //
 // Per warp (one aligned group of 32 sorted bodies), rounds of
 //   expand   up to P stack cells are popped at once, one per lane; their child
-//            blocks (contiguous in the BFS node array) are copied into a
-//            per-warp candidate buffer in shared memory, each candidate with its
-//            acceptance threshold dp (-inf for a body: bodies always interact;
-//            dp = depth0 * 0.25^(L-1) for a level-L cell);
-//   evaluate every lane streams the buffer with broadcast shared-memory loads;
+//            blocks (contiguous in the BFS node array) are copied into two
+//            per-warp shared-memory buffers: bodies (always interact, no MAC)
+//            and cells (carry their threshold dp = depth0 * 0.25^(L-1) and id);
+//   evaluate every lane streams the buffers with broadcast shared-memory loads,
 //            two candidates per instruction with the packed FP32 pair
-//            instructions (add/fma/mul .rn.f32x2, each lane an IEEE FP32 op, so r
-//            and the MAC decisions are bit-identical to the scalar form); one warp
-//            vote per candidate decides accept (interact) or reject (push to the
-//            stack); rejected cells are pushed 32 at a time with a ballot prefix.
-// P is bounded by the buffer (8 children per cell) and by the stack headroom
+//            instructions (add/fma/mul .rn.f32x2: each lane an IEEE FP32 op, so r
+//            and the MAC decisions are bit-identical to the scalar form).  Body
+//            pairs go straight to the accumulation; each cell takes one warp
+//            vote (dp <= r on every lane) and is accumulated or pushed.
+// P is bounded by the buffers (8 children per cell) and by the stack headroom
 // (a round grows the stack by at most 7 per popped cell), so the stack cannot
-// overflow unless a single depth-first path needs more than stack_cap entries,
-// which is reported as NBX_ERR_STACK.
+// overflow unless one depth-first path needs more than stack_cap entries, which
+// is reported as NBX_ERR_STACK.
 //
 // Accumulation modes: 0 plain FP32 (two packed partial sums), 1 split
 // compensation (plain FP32 within a round, Kahan across rounds), 2 Kahan on
@@ -28,7 +27,7 @@ namespace nbx {
 
 namespace {
 
-constexpr int kCB = 128;          // candidate slots per warp (even)
+constexpr int kCB = 128;          // slots per buffer (even): 16 cells x 8 children
 constexpr int kPairs = kCB / 2;
 
 typedef unsigned long long u64;
@@ -44,11 +43,6 @@ __device__ __forceinline__ void upk(u64 v, float &a, float &b) {
 __device__ __forceinline__ u64 sub2(u64 a, u64 b) {
     u64 r;
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ u64 add2(u64 a, u64 b) {
-    u64 r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     return r;
 }
 __device__ __forceinline__ u64 mul2(u64 a, u64 b) {
@@ -71,27 +65,53 @@ __device__ __forceinline__ void kahan(float &s, float &c, float v) {
 }
 
 struct WarpBuf {
-    ulonglong2 a[kPairs];  // (x0,x1) (y0,y1)
-    ulonglong2 b[kPairs];  // (z0,z1) (m0,m1)
-    u64 d[kPairs];         // (dp0,dp1)
-    int id[kCB];           // node | level << 26 (only read for rejected cells)
+    ulonglong2 ba[kPairs];  // bodies: (x0,x1) (y0,y1)
+    ulonglong2 bb[kPairs];  //         (z0,z1) (m0,m1)
+    ulonglong2 ca[kPairs];  // cells:  (x0,x1) (y0,y1)
+    ulonglong2 cb[kPairs];  //         (z0,z1) (m0,m1)
+    u64 cd[kPairs];         //         (dp0,dp1)
+    int cid[kCB];           //         node | level << 26
 };
 
-__device__ __forceinline__ void put_cand(WarpBuf &w, int slot, float4 q, float dp, int id) {
-    float *a = reinterpret_cast<float *>(&w.a[slot >> 1]);
-    float *b = reinterpret_cast<float *>(&w.b[slot >> 1]);
-    float *d = reinterpret_cast<float *>(&w.d[slot >> 1]);
+__device__ __forceinline__ void put4(ulonglong2 *a, ulonglong2 *b, int slot, float4 q) {
+    float *pa = reinterpret_cast<float *>(&a[slot >> 1]);
+    float *pb = reinterpret_cast<float *>(&b[slot >> 1]);
     const int h = slot & 1;
-    a[h] = q.x;
-    a[2 + h] = q.y;
-    b[h] = q.z;
-    b[2 + h] = q.w;
-    d[h] = dp;
-    w.id[slot] = id;
+    pa[h] = q.x;
+    pa[2 + h] = q.y;
+    pb[h] = q.z;
+    pb[2 + h] = q.w;
+}
+
+struct Sums {
+    u64 x = 0ull, y = 0ull, z = 0ull, p = 0ull;  // packed partial sums (+0.0f, +0.0f)
+    float kx = 0.f, ky = 0.f, kz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;  // Kahan totals
+};
+
+// Accumulate the packed force factor f = m*rsqrt(r)^3 of two candidates.
+template <int Mode, bool Pot>
+__device__ __forceinline__ void accumulate(Sums &a, u64 f, u64 mm, u64 ri, u64 dx, u64 dy, u64 dz) {
+    if (Mode == 2) {
+        float xa, xb, ya, yb, za, zb;
+        upk(mul2(f, dx), xa, xb);
+        upk(mul2(f, dy), ya, yb);
+        upk(mul2(f, dz), za, zb);
+        kahan(a.kx, a.cx, xa);
+        kahan(a.kx, a.cx, xb);
+        kahan(a.ky, a.cy, ya);
+        kahan(a.ky, a.cy, yb);
+        kahan(a.kz, a.cz, za);
+        kahan(a.kz, a.cz, zb);
+    } else {
+        a.x = fma2(f, dx, a.x);
+        a.y = fma2(f, dy, a.y);
+        a.z = fma2(f, dz, a.z);
+    }
+    if (Pot) a.p = fma2(mm, ri, a.p);
 }
 
 template <int Mode, bool Pot>
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(512, 2)
     k_walk2(const float4 *__restrict__ node4, const int *__restrict__ meta, const float4 *__restrict__ body4,
             const int *__restrict__ val, const int *__restrict__ groups, int ngroups,
             const int *__restrict__ body_sys, const int *__restrict__ sys_off, const float *__restrict__ depth0,
@@ -119,9 +139,8 @@ __global__ void __launch_bounds__(512, 1)
         const float4 me = body4[valid ? p : p0];
         const u64 px = pk(me.x, me.x), py = pk(me.y, me.y), pz = pk(me.z, me.z);
         const float d0 = depth0[s];
-        u64 sx = 0ull, sy = 0ull, sz = 0ull, sp = 0ull;  // packed partial sums (+0.0f, +0.0f)
-        float kx = 0.f, ky = 0.f, kz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;  // Kahan totals
-        int top = 0, ncand = 0, len = 0, opened = 0;
+        Sums acc;
+        int top = 0, nb = 0, len = 0, opened = 0;
         bool overflow = false;
 
         // root children: cells are opened unconditionally, bodies interact
@@ -135,22 +154,21 @@ __global__ void __launch_bounds__(512, 1)
             }
             const unsigned bodies = __ballot_sync(0xffffffffu, lane < rn && cm < 0);
             const unsigned cells = __ballot_sync(0xffffffffu, lane < rn && cm >= 0);
-            if (lane < rn && cm < 0) put_cand(buf, __popc(bodies & lt), q, -INFINITY, rf + lane);
+            if (lane < rn && cm < 0) put4(buf.ba, buf.bb, __popc(bodies & lt), q);
             if (lane < rn && cm >= 0) stack[__popc(cells & lt)] = (rf + lane) | (1 << kLevelShift);
-            ncand = __popc(bodies);
+            nb = __popc(bodies);
             top = __popc(cells);
             opened += top;
             __syncwarp();
         }
 
-        while (top > 0 || ncand > 0) {
-            // ---- expand
-            int P = min(min(top, 32), min((kCB - ncand) >> 3, (stack_cap - top) / 7));
-            if (P <= 0 && ncand == 0) {
+        while (top > 0 || nb > 0) {
+            // ---- expand: lane j pops stack[top-1-j] and copies its children
+            const int P = max(0, min(min(top, 32), min((kCB - nb) >> 3, (stack_cap - top) / 7)));
+            if (P == 0 && nb == 0) {
                 overflow = true;
                 break;
             }
-            if (P < 0) P = 0;
             int first = 0, nch = 0, lvl = 0;
             if (lane < P) {
                 const int e = stack[top - 1 - lane];
@@ -160,95 +178,123 @@ __global__ void __launch_bounds__(512, 1)
                 first = mb & 0x0fffffff;
                 nch = ((mb >> 28) & 7) + 1;
             }
-            int incl = nch;
+            int cmeta[8];
+            unsigned bmask = 0u;
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                cmeta[k] = k < nch ? meta[first + k] : 0;
+                bmask |= (k < nch && cmeta[k] < 0 ? 1u : 0u) << k;
+            }
+            const int mynb = __popc(bmask);
+            const int mync = nch - mynb;
+            int incl = mynb | (mync << 16);
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const int u = __shfl_up_sync(0xffffffffu, incl, o);
                 if (lane >= o) incl += u;
             }
-            const int T = __shfl_sync(0xffffffffu, incl, 31);
+            const int tot = __shfl_sync(0xffffffffu, incl, 31);
+            const int bbase = nb + (incl & 0xffff) - mynb;
+            const int cbase = (incl >> 16) - mync;
             __syncwarp();
             top -= P;
             if (nch > 0) {
                 const float dpc = ldexpf(d0, -2 * lvl);  // children are at level lvl+1
-                const int base = ncand + incl - nch;
-                for (int k = 0; k < nch; k++) {
-                    const int c = first + k;
-                    const int cm = meta[c];
-                    put_cand(buf, base + k, node4[c], cm < 0 ? -INFINITY : dpc, c | ((lvl + 1) << kLevelShift));
+                const int idl = (lvl + 1) << kLevelShift;
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    if (k < nch) {
+                        const float4 q = node4[first + k];
+                        const int below = __popc(bmask & ((1u << k) - 1u));
+                        if (cmeta[k] < 0) {
+                            put4(buf.ba, buf.bb, bbase + below, q);
+                        } else {
+                            const int slot = cbase + (k - below);
+                            put4(buf.ca, buf.cb, slot, q);
+                            reinterpret_cast<float *>(&buf.cd[slot >> 1])[slot & 1] = dpc;
+                            buf.cid[slot] = (first + k) | idl;
+                        }
+                    }
                 }
             }
-            const int nreal = ncand + T;
-            int npad = nreal;
-            if (nreal & 1) {
-                if (lane == 0) put_cand(buf, nreal, make_float4(1e18f, 1e18f, 1e18f, 0.f), -INFINITY, 0);
-                npad = nreal + 1;
+            const int nbody = nb + (tot & 0xffff);
+            const int ncell = tot >> 16;
+            // pad odd buffers with a massless far-away candidate that is accepted
+            if (lane == 0 && (nbody & 1)) put4(buf.ba, buf.bb, nbody, make_float4(1e18f, 1e18f, 1e18f, 0.f));
+            if (lane == 1 && (ncell & 1)) {
+                put4(buf.ca, buf.cb, ncell, make_float4(1e18f, 1e18f, 1e18f, 0.f));
+                reinterpret_cast<float *>(&buf.cd[ncell >> 1])[1] = -INFINITY;
             }
             __syncwarp();
 
-            // ---- evaluate
-            const int npairs = npad >> 1;
-            int nrej = 0;
-            for (int c0 = 0; c0 < npairs; c0 += 16) {
-                const int cnt = min(16, npairs - c0);
-                unsigned rej = 0u;
+            // ---- evaluate bodies: no MAC
+            const int nbp = (nbody + 1) >> 1;
 #pragma unroll 2
-                for (int q = 0; q < cnt; q++) {
-                    const ulonglong2 A = buf.a[c0 + q];
-                    const ulonglong2 B = buf.b[c0 + q];
-                    float dpa, dpb;
-                    upk(buf.d[c0 + q], dpa, dpb);
-                    const u64 dx = sub2(A.x, px);
-                    const u64 dy = sub2(A.y, py);
-                    const u64 dz = sub2(B.x, pz);
-                    u64 r = fma2(dx, dx, eps2x2);
-                    r = fma2(dy, dy, r);
-                    r = fma2(dz, dz, r);
-                    float ra, rb;
-                    upk(r, ra, rb);
-                    const bool oka = __all_sync(0xffffffffu, dpa <= ra);
-                    const bool okb = __all_sync(0xffffffffu, dpb <= rb);
-                    float ma, mb;
-                    upk(B.y, ma, mb);
-                    const u64 ri = pk(rsqrtf(ra), rsqrtf(rb));
-                    const u64 mm = pk(oka ? ma : 0.f, okb ? mb : 0.f);
-                    const u64 f = mul2(mul2(mul2(mm, ri), ri), ri);
-                    if (Mode == 2) {
-                        float xa, xb, ya, yb, za, zb;
-                        upk(mul2(f, dx), xa, xb);
-                        upk(mul2(f, dy), ya, yb);
-                        upk(mul2(f, dz), za, zb);
-                        kahan(kx, cx, xa); kahan(kx, cx, xb);
-                        kahan(ky, cy, ya); kahan(ky, cy, yb);
-                        kahan(kz, cz, za); kahan(kz, cz, zb);
-                    } else {
-                        sx = fma2(f, dx, sx);
-                        sy = fma2(f, dy, sy);
-                        sz = fma2(f, dz, sz);
-                    }
-                    if (Pot) sp = fma2(mm, ri, sp);
-                    rej |= (oka ? 0u : 1u) << (2 * q);
-                    rej |= (okb ? 0u : 1u) << (2 * q + 1);
+            for (int q = 0; q < nbp; q++) {
+                const ulonglong2 A = buf.ba[q];
+                const ulonglong2 B = buf.bb[q];
+                const u64 dx = sub2(A.x, px);
+                const u64 dy = sub2(A.y, py);
+                const u64 dz = sub2(B.x, pz);
+                u64 r = fma2(dx, dx, eps2x2);
+                r = fma2(dy, dy, r);
+                r = fma2(dz, dz, r);
+                float ra, rb;
+                upk(r, ra, rb);
+                const u64 ri = pk(rsqrtf(ra), rsqrtf(rb));
+                const u64 f = mul2(mul2(mul2(B.y, ri), ri), ri);
+                accumulate<Mode, Pot>(acc, f, B.y, ri, dx, dy, dz);
+            }
+            // ---- evaluate cells: one vote per cell, accept or push
+            const int ncp = (ncell + 1) >> 1;
+            int nrej = 0;
+#pragma unroll 2
+            for (int q = 0; q < ncp; q++) {
+                const ulonglong2 A = buf.ca[q];
+                const ulonglong2 B = buf.cb[q];
+                float dpa, dpb;
+                upk(buf.cd[q], dpa, dpb);
+                const u64 dx = sub2(A.x, px);
+                const u64 dy = sub2(A.y, py);
+                const u64 dz = sub2(B.x, pz);
+                u64 r = fma2(dx, dx, eps2x2);
+                r = fma2(dy, dy, r);
+                r = fma2(dz, dz, r);
+                float ra, rb;
+                upk(r, ra, rb);
+                const bool oka = __all_sync(0xffffffffu, dpa <= ra);
+                const bool okb = __all_sync(0xffffffffu, dpb <= rb);
+                float ma, mb;
+                upk(B.y, ma, mb);
+                const u64 ri = pk(rsqrtf(ra), rsqrtf(rb));
+                const u64 mm = pk(oka ? ma : 0.f, okb ? mb : 0.f);
+                const u64 f = mul2(mul2(mul2(mm, ri), ri), ri);
+                accumulate<Mode, Pot>(acc, f, mm, ri, dx, dy, dz);
+                if (!oka) {
+                    if (lane == 0) stack[top + nrej] = buf.cid[2 * q];
+                    nrej++;
                 }
-                if (rej) {
-                    const int nr = __popc(rej);
-                    if ((rej >> lane) & 1u) {
-                        const int pos = top + __popc(rej & lt);
-                        stack[pos] = buf.id[2 * c0 + lane];
-                    }
-                    top += nr;
-                    nrej += nr;
+                if (!okb) {
+                    if (lane == 0) stack[top + nrej] = buf.cid[2 * q + 1];
+                    nrej++;
                 }
             }
-            len += nreal - nrej;
+            top += nrej;
+            len += nbody + ncell - nrej;
             opened += nrej;
-            ncand = 0;
+            nb = 0;
             if (Mode == 1) {  // fold this round's partial sums into the compensated totals
                 float a0, a1;
-                upk(sx, a0, a1); kahan(kx, cx, a0); kahan(kx, cx, a1);
-                upk(sy, a0, a1); kahan(ky, cy, a0); kahan(ky, cy, a1);
-                upk(sz, a0, a1); kahan(kz, cz, a0); kahan(kz, cz, a1);
-                sx = sy = sz = 0ull;
+                upk(acc.x, a0, a1);
+                kahan(acc.kx, acc.cx, a0);
+                kahan(acc.kx, acc.cx, a1);
+                upk(acc.y, a0, a1);
+                kahan(acc.ky, acc.cy, a0);
+                kahan(acc.ky, acc.cy, a1);
+                upk(acc.z, a0, a1);
+                kahan(acc.kz, acc.cz, a0);
+                kahan(acc.kz, acc.cz, a1);
+                acc.x = acc.y = acc.z = 0ull;
             }
             __syncwarp();
         }
@@ -260,13 +306,16 @@ __global__ void __launch_bounds__(512, 1)
             float fx, fy, fz;
             if (Mode == 0) {
                 float a0, a1;
-                upk(sx, a0, a1); fx = a0 + a1;
-                upk(sy, a0, a1); fy = a0 + a1;
-                upk(sz, a0, a1); fz = a0 + a1;
+                upk(acc.x, a0, a1);
+                fx = a0 + a1;
+                upk(acc.y, a0, a1);
+                fy = a0 + a1;
+                upk(acc.z, a0, a1);
+                fz = a0 + a1;
             } else {
-                fx = kx - cx;
-                fy = ky - cy;
-                fz = kz - cz;
+                fx = acc.kx - acc.cx;
+                fy = acc.ky - acc.cy;
+                fz = acc.kz - acc.cz;
             }
             const int ob = val[p];
             ax[ob] = fx;
@@ -274,7 +323,7 @@ __global__ void __launch_bounds__(512, 1)
             az[ob] = fz;
             if (Pot) {
                 float a0, a1;
-                upk(sp, a0, a1);
+                upk(acc.p, a0, a1);
                 // remove the body's own term m * rsqrt(eps2), then phi = -sum
                 pot[ob] = -((a0 + a1) - me.w * rsqrtf(eps2));
             }
@@ -317,17 +366,14 @@ int set_attr(Ctx *ctx, int smem_max) {
 
 }  // namespace
 
-size_t walk2_smem_per_warp(int stack_cap) { return sizeof(WarpBuf) + (size_t)stack_cap * sizeof(int); }
-
 int walk2_init(Ctx *ctx) {
     int smem_optin = 0;
     NBX_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->p.device));
-    const int smem_max = smem_optin;
     int rc = 0;
-    rc |= set_attr<0, false>(ctx, smem_max);
-    rc |= set_attr<1, false>(ctx, smem_max);
-    rc |= set_attr<2, false>(ctx, smem_max);
-    rc |= set_attr<0, true>(ctx, smem_max);
+    rc |= set_attr<0, false>(ctx, smem_optin);
+    rc |= set_attr<1, false>(ctx, smem_optin);
+    rc |= set_attr<2, false>(ctx, smem_optin);
+    rc |= set_attr<0, true>(ctx, smem_optin);
     return rc;
 }
 
