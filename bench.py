@@ -185,7 +185,8 @@ def main():
         walk = sum(e[1].elapsed_time(e[2]) for e in ev)
         integ = sum(e[2].elapsed_time(e[3]) for e in ev)
         return dict(ms=total, build_ms=build, walk_ms=walk, integ_ms=integ,
-                    interactions=info["interactions"], launches=info["launches"] - launches0,
+                    interactions=info["interactions"], opened=info["opened"],
+                    launches=info["launches"] - launches0,
                     ncells=info["ncells"], max_level=info["max_level"])
 
     # ---- error at the initial state (outside any timed region)
@@ -282,6 +283,7 @@ def main():
                         "ratio_to_plain_time": round(ms_comp / ms_plain, 4)},
         "force_error_vs_fp64_direct": errs,
         "interactions_per_step": inter_per_step,
+        "opened_cells_per_step": plain["opened"],
         "interactions_per_s": inter_per_step * steps_per_s,
         "phase_ms": {"build": round(plain["build_ms"] / args.steps, 3), "walk": round(walk_ms, 3),
                      "integrate": round(plain["integ_ms"] / args.steps, 3)},

@@ -123,7 +123,7 @@ void nbx_params_default(nbx_params *p) {
     p->dampening = 1.f;
     p->gravity = 1.f;
     p->group = 32;
-    p->stack_depth = 384;
+    p->stack_depth = 1024;
     p->compensated = 0;
     p->leaf_size = 1;
     p->radix_bits = 8;
@@ -157,7 +157,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     *out = nullptr;
     if (p->max_bodies < 1 || p->max_bodies > (1 << 25) || p->max_systems < 1 ||
         p->max_systems > p->max_bodies || p->group != 32 || p->leaf_size != 1 || p->radix_bits != 8 ||
-        p->stack_depth < 64 || p->stack_depth > 4096)
+        p->stack_depth < 360 || p->stack_depth > 4096)
         return NBX_ERR_ARG;
     Ctx *ctx = new (std::nothrow) Ctx();
     if (!ctx) return NBX_ERR_NOMEM;

@@ -82,21 +82,34 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     for (int d = lane; d < kRadixBins; d += 32) cnt[w][d] = offs[hbase + (int64_t)d * hstride];
     __syncwarp();
     const unsigned lt = (1u << lane) - 1u;
-    for (int j = 0; j < len; j += 32) {
-        const int i = j + lane;
-        const bool valid = i < len;
-        K k = valid ? key_in[start + i] : K(0);
-        unsigned d = valid ? ((unsigned)(k >> shift) & 0xffu) : (0x100u + lane);
-        unsigned peers = __match_any_sync(0xffffffffu, d);
-        unsigned rank = __popc(peers & lt);
-        unsigned base = valid ? cnt[w][d] : 0u;
-        __syncwarp();
-        if (valid && rank == 0) cnt[w][d] = base + __popc(peers);
-        __syncwarp();
-        if (valid) {
-            unsigned dst = base + rank;
-            key_out[dst] = k;
-            if (val_in) val_out[dst] = val_in[start + i];
+    constexpr int kBatch = 8;  // rounds whose loads are in flight together
+    for (int j0 = 0; j0 < len; j0 += 32 * kBatch) {
+        K kk[kBatch];
+        V vv[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; u++) {
+            const int i = j0 + u * 32 + lane;
+            kk[u] = i < len ? key_in[start + i] : K(0);
+            if (val_in) vv[u] = i < len ? val_in[start + i] : V(0);
+        }
+#pragma unroll
+        for (int u = 0; u < kBatch; u++) {
+            const int j = j0 + u * 32;
+            if (j >= len) break;
+            const bool valid = j + lane < len;
+            const K k = kk[u];
+            unsigned d = valid ? ((unsigned)(k >> shift) & 0xffu) : (0x100u + lane);
+            unsigned peers = __match_any_sync(0xffffffffu, d);
+            unsigned rank = __popc(peers & lt);
+            unsigned base = valid ? cnt[w][d] : 0u;
+            __syncwarp();
+            if (valid && rank == 0) cnt[w][d] = base + __popc(peers);
+            __syncwarp();
+            if (valid) {
+                unsigned dst = base + rank;
+                key_out[dst] = k;
+                if (val_in) val_out[dst] = vv[u];
+            }
         }
     }
 }

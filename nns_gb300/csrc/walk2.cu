@@ -13,10 +13,10 @@
 //            and the MAC decisions are bit-identical to the scalar form).  Body
 //            pairs go straight to the accumulation; each cell takes one warp
 //            vote (dp <= r on every lane) and is accumulated or pushed.
-// P is bounded by the buffers (8 children per cell) and by the stack headroom
-// (a round grows the stack by at most 7 per popped cell), so the stack cannot
-// overflow unless one depth-first path needs more than stack_cap entries, which
-// is reported as NBX_ERR_STACK.
+// P is bounded by the buffers (8 children per cell).  Wide rounds run while the
+// stack keeps a depth-first reserve free (7 entries per level); beyond that the
+// walk pops one cell per round, which can never outgrow the reserve, so a stack
+// of at least kDfsReserve + 7*8 entries cannot overflow (NBX_ERR_STACK otherwise).
 //
 // Accumulation modes: 0 plain FP32 (two packed partial sums), 1 split
 // compensation (plain FP32 within a round, Kahan across rounds), 2 Kahan on
@@ -27,7 +27,11 @@ namespace nbx {
 
 namespace {
 
-constexpr int kCB = 128;          // slots per buffer (even): 16 cells x 8 children
+constexpr int kCB = 64;           // slots per buffer (even): 8 cells x 8 children
+// Stack entries kept free for depth-first descent: from any stack content a
+// depth-first walk (one cell per round) grows the stack by at most 7 entries per
+// level below the popped cell, i.e. by less than 7 * 42.
+constexpr int kDfsReserve = 7 * 42 + 8;
 constexpr int kPairs = kCB / 2;
 
 typedef unsigned long long u64;
@@ -164,7 +168,11 @@ __global__ void __launch_bounds__(512, 2)
 
         while (top > 0 || nb > 0) {
             // ---- expand: lane j pops stack[top-1-j] and copies its children
-            const int P = max(0, min(min(top, 32), min((kCB - nb) >> 3, (stack_cap - top) / 7)));
+            // wide rounds while the stack keeps the depth-first reserve free,
+            // else one cell per round (depth-first), which cannot outgrow it
+            int P = min(min(top, 32), (kCB - nb) >> 3);
+            if (top + 7 * P > stack_cap - kDfsReserve) P = min(P, 1);
+            if (top + 7 * P > stack_cap) P = 0;
             if (P == 0 && nb == 0) {
                 overflow = true;
                 break;
@@ -229,7 +237,7 @@ __global__ void __launch_bounds__(512, 2)
 
             // ---- evaluate bodies: no MAC
             const int nbp = (nbody + 1) >> 1;
-#pragma unroll 2
+#pragma unroll 4
             for (int q = 0; q < nbp; q++) {
                 const ulonglong2 A = buf.ba[q];
                 const ulonglong2 B = buf.bb[q];

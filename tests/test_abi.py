@@ -34,7 +34,7 @@ def test_status_strings_without_gpu():
     assert L.nbx_status_string(3).decode().startswith("two bodies")
     p = _lib.nbx_params()
     L.nbx_params_default(ctypes.byref(p))
-    assert p.group == 32 and p.stack_depth >= 320 and abs(p.theta - 0.5) < 1e-7
+    assert p.group == 32 and p.stack_depth >= 360 and abs(p.theta - 0.5) < 1e-7
 
 
 def test_create_rejects_bad_params_without_gpu():
