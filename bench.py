@@ -40,6 +40,9 @@ def parse():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--targets", type=int, default=8192)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--batched-systems", type=int, default=512)
     return ap.parse_args()
 
 
@@ -133,6 +136,82 @@ def run_reference(args, rank):
     return line
 
 
+def bench_batched(args, local):
+    """Batched form: independent star+disk systems (N_i = floor(2^U[10,17]), seed
+    20261203+1+i), theta 0.5, eps 0.01, dt 1e-3, all systems in one launch per phase,
+    each step replayed from a CUDA graph; against the same systems stepped one
+    at a time through single-system contexts with the same kernels."""
+    import torch
+    from nns_gb300 import autotune, ic
+    from nns_gb300.barnes_hut import Context, State
+    bodies, off = ic.batched_star_disks(args.batched_systems)
+    nsys = len(off) - 1
+    ntot = int(off[-1])
+    ctx = Context(max_bodies=ntot, max_systems=nsys, theta=0.5, eps=0.01, dt=1e-3, device=local)
+    ctx.set_systems(off)
+    s = State.from_bodies(bodies, device="cuda:%d" % local)
+    tune = autotune.tune_walk(ctx, s, use_cache=False)
+    # per-system forces of the batch against single-system runs (bit for bit)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    accb = s.acc()
+    checks = []
+    for i in range(min(4, nsys)):
+        a, b = int(off[i]), int(off[i + 1])
+        sub = ic.Bodies(*(arr[a:b] for arr in bodies.arrays()))
+        c1 = Context(max_bodies=b - a, theta=0.5, eps=0.01, dt=1e-3, device=local)
+        c1.set_walk(tune["warps"], tune["variant"])
+        c1.set_systems([0, b - a])
+        s1 = State.from_bodies(sub, device="cuda:%d" % local)
+        c1.build(s1)
+        c1.forces(s1)
+        c1.sync()
+        checks.append(bool(np.array_equal(accb[a:b], s1.acc())))
+        del c1, s1
+    steps = max(2, args.steps)
+    ctx.graph_step(s, max(1, args.warmup))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    ctx.graph_step(s, steps)
+    e1.record()
+    torch.cuda.synchronize()
+    ctx.sync()
+    t_batch = e0.elapsed_time(e1) / steps
+    inter = ctx.tree_info()["interactions"]
+    # one system at a time (eager launches, one context per system)
+    ctxs, states = [], []
+    for i in range(nsys):
+        a, b = int(off[i]), int(off[i + 1])
+        sub = ic.Bodies(*(arr[a:b] for arr in bodies.arrays()))
+        c1 = Context(max_bodies=b - a, theta=0.5, eps=0.01, dt=1e-3, device=local)
+        c1.set_walk(tune["warps"], tune["variant"])
+        c1.set_systems([0, b - a])
+        ctxs.append(c1)
+        states.append(State.from_bodies(sub, device="cuda:%d" % local))
+    for c1, s1 in zip(ctxs, states):
+        c1.step(s1, 1)
+    torch.cuda.synchronize()
+    single_steps = 2
+    e0.record()
+    for _ in range(single_steps):
+        for c1, s1 in zip(ctxs, states):
+            c1.step(s1, 1)
+    e1.record()
+    torch.cuda.synchronize()
+    t_single = e0.elapsed_time(e1) / single_steps
+    return {"systems": nsys, "bodies": ntot, "steps": steps,
+            "ms_per_step": round(t_batch, 3),
+            "systems_steps_per_s": round(nsys * 1000.0 / t_batch, 2),
+            "one_at_a_time_ms_per_step": round(t_single, 3),
+            "one_at_a_time_systems_steps_per_s": round(nsys * 1000.0 / t_single, 2),
+            "speedup_vs_one_at_a_time": round(t_single / t_batch, 3),
+            "interactions_per_step": inter,
+            "per_system_forces_bitwise_equal_unbatched": checks,
+            "walk_config": {"warps": tune["warps"], "variant": tune["variant"]}}
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
@@ -156,6 +235,10 @@ def main():
     ctx.set_systems([0, n])
     s = State.from_bodies(b, device="cuda:%d" % local)
     stream = torch.cuda.current_stream()
+    tune = None
+    if not args.no_tune:
+        from nns_gb300 import autotune
+        tune = autotune.tune_walk(ctx, s, use_cache=False)
 
     def timed(nsteps, phase=True):
         ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(nsteps)]
@@ -262,6 +345,12 @@ def main():
         ms_plain = float(t.item())
         steps_per_s = world * 1000.0 / ms_plain
 
+    batched = None
+    if not args.no_batched:
+        del ctx, s
+        torch.cuda.empty_cache()
+        batched = bench_batched(args, local)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
@@ -296,6 +385,8 @@ def main():
                              "kinetic_rel_change": float((diag1["kinetic"] - diag0["kinetic"]) / diag0["kinetic"])},
         "e2e": {"value": round(1000.0 / e2e_ms, 4), "unit": "steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
+        "batched": batched,
+        "autotune": tune,
         "gpu_launches": plain["launches"],
         "clocks": clocks,
         "cpu_baseline": cpu,

@@ -67,7 +67,8 @@ typedef struct nbx_params {
     int device;        /* CUDA device ordinal */
     int block_size;    /* reference launch-shape hints (main.cu:30-31); informational */
     int grid_size;
-    int walk_variant;  /* 0 production walk; 2 one-cell-at-a-time walk (comparison) */
+    int walk_variant;  /* 0 production walk, 64-slot candidate buffers; 1 the same with
+                          128-slot buffers; 2 one-cell-at-a-time walk (comparison) */
 } nbx_params;
 
 /* SoA device state of all systems; systems are contiguous ranges. */

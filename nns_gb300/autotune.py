@@ -1,0 +1,74 @@
+"""Autotuner for the launch parameters of the force walk.
+
+The interaction lists are fixed by the reference's semantics (group of 32,
+leaf bucket of one body, 8-bit radix digits are what the parity tests pin), so
+the tunable knobs are the ones that change only speed:
+  * warps per block of the walk (4, 8, 16) -- occupancy vs. shared memory,
+  * candidate buffer size of the walk (64 or 128 slots per warp).
+Candidates are timed with CUDA events on the caller's workload after one
+build; the winner is applied to the context and cached per (device, n, systems)
+in ``~/.cache/nbx_autotune.json`` (override with NBX_AUTOTUNE_CACHE).
+"""
+from __future__ import annotations
+
+import json
+import os
+
+import torch
+
+CANDIDATES = ((8, 0), (16, 0), (4, 0), (8, 1), (4, 1))
+
+
+def _cache_path():
+    return os.environ.get("NBX_AUTOTUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "nbx_autotune.json"))
+
+
+def _key(ctx, n):
+    name = torch.cuda.get_device_name(ctx.device)
+    nsys = 1 if ctx.offsets is None else len(ctx.offsets) - 1
+    return "%s|n=%d|sys=%d|comp=%d" % (name, n, nsys, int(ctx.params.compensated))
+
+
+def tune_walk(ctx, state, reps: int = 2, candidates=CANDIDATES, use_cache: bool = True) -> dict:
+    """Times each candidate walk configuration and applies the fastest."""
+    n = int(ctx.offsets[-1])
+    key = _key(ctx, n)
+    path = _cache_path()
+    cache = {}
+    if use_cache and os.path.exists(path):
+        try:
+            cache = json.load(open(path))
+        except (OSError, ValueError):
+            cache = {}
+    if use_cache and key in cache:
+        best = cache[key]
+        ctx.set_walk(best["warps"], best["variant"])
+        return dict(best, cached=True)
+    ctx.build(state)
+    ctx.sync()
+    times = {}
+    for warps, variant in candidates:
+        ctx.set_walk(warps, variant)
+        ctx.forces(state)  # warm-up
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(reps):
+            ctx.forces(state)
+        ev1.record()
+        torch.cuda.synchronize()
+        times["%d/%d" % (warps, variant)] = ev0.elapsed_time(ev1) / reps
+    ctx.sync()
+    wbest = min(times, key=times.get)
+    warps, variant = (int(v) for v in wbest.split("/"))
+    ctx.set_walk(warps, variant)
+    best = {"warps": warps, "variant": variant, "ms": times}
+    if use_cache:
+        cache[key] = best
+        try:
+            os.makedirs(os.path.dirname(path), exist_ok=True)
+            json.dump(cache, open(path, "w"), indent=1)
+        except OSError:
+            pass
+    return dict(best, cached=False)

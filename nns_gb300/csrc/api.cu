@@ -273,7 +273,7 @@ int nbx_set_constants(nbx_ctx *c, float theta_ref, float eps2, int compensated) 
 
 int nbx_set_walk_config(nbx_ctx *c, int warps_per_block, int variant) {
     if (!c || !(warps_per_block == 4 || warps_per_block == 8 || warps_per_block == 16) ||
-        !(variant == 0 || variant == 2))
+        !(variant == 0 || variant == 1 || variant == 2))
         return NBX_ERR_ARG;
     Ctx *ctx = C(c);
     ctx->walk_warps = warps_per_block;

@@ -4,9 +4,10 @@
 //
 // Per warp (one aligned group of 32 sorted bodies), rounds of
 //   expand   up to P stack cells are popped at once, one per lane; their child
-//            blocks (contiguous in the BFS node array) are copied into two
-//            per-warp shared-memory buffers: bodies (always interact, no MAC)
-//            and cells (carry their threshold dp = depth0 * 0.25^(L-1) and id);
+//            blocks (contiguous in the BFS node array) are spread over the lanes,
+//            one child per lane, and copied into two per-warp shared-memory
+//            buffers: bodies (always interact, no MAC) and cells (carry their
+//            threshold dp = depth0 * 0.25^(L-1) and id);
 //   evaluate every lane streams the buffers with broadcast shared-memory loads,
 //            two candidates per instruction with the packed FP32 pair
 //            instructions (add/fma/mul .rn.f32x2: each lane an IEEE FP32 op, so r
@@ -27,12 +28,10 @@ namespace nbx {
 
 namespace {
 
-constexpr int kCB = 64;           // slots per buffer (even): 8 cells x 8 children
 // Stack entries kept free for depth-first descent: from any stack content a
 // depth-first walk (one cell per round) grows the stack by at most 7 entries per
 // level below the popped cell, i.e. by less than 7 * 42.
 constexpr int kDfsReserve = 7 * 42 + 8;
-constexpr int kPairs = kCB / 2;
 
 typedef unsigned long long u64;
 
@@ -68,13 +67,16 @@ __device__ __forceinline__ void kahan(float &s, float &c, float v) {
     s = t;
 }
 
+// Per-warp candidate buffers of CB slots each (CB/8 cells expanded per round).
+template <int CB>
 struct WarpBuf {
+    static constexpr int kPairs = CB / 2;
     ulonglong2 ba[kPairs];  // bodies: (x0,x1) (y0,y1)
     ulonglong2 bb[kPairs];  //         (z0,z1) (m0,m1)
     ulonglong2 ca[kPairs];  // cells:  (x0,x1) (y0,y1)
     ulonglong2 cb[kPairs];  //         (z0,z1) (m0,m1)
     u64 cd[kPairs];         //         (dp0,dp1)
-    int cid[kCB];           //         node | level << 26
+    int cid[CB];            //         node | level << 26
 };
 
 __device__ __forceinline__ void put4(ulonglong2 *a, ulonglong2 *b, int slot, float4 q) {
@@ -114,7 +116,7 @@ __device__ __forceinline__ void accumulate(Sums &a, u64 f, u64 mm, u64 ri, u64 d
     if (Pot) a.p = fma2(mm, ri, a.p);
 }
 
-template <int Mode, bool Pot>
+template <int CB, int Mode, bool Pot>
 __global__ void __launch_bounds__(512, 2)
     k_walk2(const float4 *__restrict__ node4, const int *__restrict__ meta, const float4 *__restrict__ body4,
             const int *__restrict__ val, const int *__restrict__ groups, int ngroups,
@@ -126,8 +128,9 @@ __global__ void __launch_bounds__(512, 2)
     if (st->code != 0) return;
     const int warps = blockDim.x >> 5;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    WarpBuf &buf = reinterpret_cast<WarpBuf *>(smem_raw)[w];
-    int *stack = reinterpret_cast<int *>(smem_raw + sizeof(WarpBuf) * warps) + w * stack_cap;
+    constexpr int kCB = CB;
+    WarpBuf<CB> &buf = reinterpret_cast<WarpBuf<CB> *>(smem_raw)[w];
+    int *stack = reinterpret_cast<int *>(smem_raw + sizeof(WarpBuf<CB>) * warps) + w * stack_cap;
     const unsigned lt = (1u << lane) - 1u;
     const u64 eps2x2 = pk(eps2, eps2);
     unsigned long long tot_len = 0ull, tot_open = 0ull;
@@ -186,47 +189,47 @@ __global__ void __launch_bounds__(512, 2)
                 first = mb & 0x0fffffff;
                 nch = ((mb >> 28) & 7) + 1;
             }
-            int cmeta[8];
-            unsigned bmask = 0u;
-#pragma unroll
-            for (int k = 0; k < 8; k++) {
-                cmeta[k] = k < nch ? meta[first + k] : 0;
-                bmask |= (k < nch && cmeta[k] < 0 ? 1u : 0u) << k;
-            }
-            const int mynb = __popc(bmask);
-            const int mync = nch - mynb;
-            int incl = mynb | (mync << 16);
+            int incl = nch;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const int u = __shfl_up_sync(0xffffffffu, incl, o);
                 if (lane >= o) incl += u;
             }
-            const int tot = __shfl_sync(0xffffffffu, incl, 31);
-            const int bbase = nb + (incl & 0xffff) - mynb;
-            const int cbase = (incl >> 16) - mync;
+            const int excl = incl - nch;
+            const int T = __shfl_sync(0xffffffffu, incl, 31);
             __syncwarp();
             top -= P;
-            if (nch > 0) {
-                const float dpc = ldexpf(d0, -2 * lvl);  // children are at level lvl+1
-                const int idl = (lvl + 1) << kLevelShift;
+            // the T children are spread over the lanes, 32 at a time: lane t
+            // finds its popped cell j (largest j < P with excl_j <= t)
+            int nbody = nb, ncell = 0;
+            for (int t0 = 0; t0 < T; t0 += 32) {
+                const int t = t0 + lane;
+                int j = 0;
 #pragma unroll
-                for (int k = 0; k < 8; k++) {
-                    if (k < nch) {
-                        const float4 q = node4[first + k];
-                        const int below = __popc(bmask & ((1u << k) - 1u));
-                        if (cmeta[k] < 0) {
-                            put4(buf.ba, buf.bb, bbase + below, q);
-                        } else {
-                            const int slot = cbase + (k - below);
-                            put4(buf.ca, buf.cb, slot, q);
-                            reinterpret_cast<float *>(&buf.cd[slot >> 1])[slot & 1] = dpc;
-                            buf.cid[slot] = (first + k) | idl;
-                        }
-                    }
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int cand = j + step;
+                    const int e = __shfl_sync(0xffffffffu, excl, cand & 31);
+                    if (cand < P && e <= t) j = cand;
                 }
+                const int fj = __shfl_sync(0xffffffffu, first, j);
+                const int lj = __shfl_sync(0xffffffffu, lvl, j);
+                const int ej = __shfl_sync(0xffffffffu, excl, j);
+                const bool ok = t < T;
+                const int c = fj + (t - ej);
+                const int cm = ok ? meta[c] : 0;
+                const float4 q = ok ? node4[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const unsigned bm = __ballot_sync(0xffffffffu, ok && cm < 0);
+                const unsigned cmk = __ballot_sync(0xffffffffu, ok && cm >= 0);
+                if (ok && cm < 0) put4(buf.ba, buf.bb, nbody + __popc(bm & lt), q);
+                if (ok && cm >= 0) {
+                    const int slot = ncell + __popc(cmk & lt);
+                    put4(buf.ca, buf.cb, slot, q);
+                    reinterpret_cast<float *>(&buf.cd[slot >> 1])[slot & 1] = ldexpf(d0, -2 * lj);
+                    buf.cid[slot] = c | ((lj + 1) << kLevelShift);  // children are at level lj+1
+                }
+                nbody += __popc(bm);
+                ncell += __popc(cmk);
             }
-            const int nbody = nb + (tot & 0xffff);
-            const int ncell = tot >> 16;
             // pad odd buffers with a massless far-away candidate that is accepted
             if (lane == 0 && (nbody & 1)) put4(buf.ba, buf.bb, nbody, make_float4(1e18f, 1e18f, 1e18f, 0.f));
             if (lane == 1 && (ncell & 1)) {
@@ -347,17 +350,17 @@ __global__ void __launch_bounds__(512, 2)
     }
 }
 
-template <int Mode, bool Pot>
+template <int CB, int Mode, bool Pot>
 int launch(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st) {
     const int cap = ctx->p.stack_depth;
-    const size_t smem = (size_t)warps * (sizeof(WarpBuf) + (size_t)cap * sizeof(int));
+    const size_t smem = (size_t)warps * (sizeof(WarpBuf<CB>) + (size_t)cap * sizeof(int));
     const int blocks_needed = ceil_div(ctx->ngroups, warps);
     int per_sm = 1;
-    NBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk2<Mode, Pot>, warps * 32, smem));
+    NBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk2<CB, Mode, Pot>, warps * 32, smem));
     if (per_sm < 1) per_sm = 1;
     const int grid = blocks_needed < ctx->nsm * per_sm ? blocks_needed : ctx->nsm * per_sm;
     if (grid <= 0) return NBX_OK;
-    k_walk2<Mode, Pot><<<grid, warps * 32, smem, st>>>(
+    k_walk2<CB, Mode, Pot><<<grid, warps * 32, smem, st>>>(
         ctx->d_node4, ctx->d_meta, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
         ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay, s->az,
         pot, ctx->d_nlist, ctx->d_nopen, ctx->d_status);
@@ -366,10 +369,20 @@ int launch(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st)
     return NBX_OK;
 }
 
-template <int Mode, bool Pot>
+template <int CB, int Mode, bool Pot>
 int set_attr(Ctx *ctx, int smem_max) {
-    NBX_CUDA(cudaFuncSetAttribute(k_walk2<Mode, Pot>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
+    NBX_CUDA(cudaFuncSetAttribute(k_walk2<CB, Mode, Pot>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
     return NBX_OK;
+}
+
+template <int CB>
+int forces_cb(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st) {
+    if (pot) return launch<CB, 0, true>(ctx, s, pot, warps, st);
+    switch (ctx->compensated) {
+        case 1: return launch<CB, 1, false>(ctx, s, nullptr, warps, st);
+        case 2: return launch<CB, 2, false>(ctx, s, nullptr, warps, st);
+        default: return launch<CB, 0, false>(ctx, s, nullptr, warps, st);
+    }
 }
 
 }  // namespace
@@ -378,20 +391,21 @@ int walk2_init(Ctx *ctx) {
     int smem_optin = 0;
     NBX_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->p.device));
     int rc = 0;
-    rc |= set_attr<0, false>(ctx, smem_optin);
-    rc |= set_attr<1, false>(ctx, smem_optin);
-    rc |= set_attr<2, false>(ctx, smem_optin);
-    rc |= set_attr<0, true>(ctx, smem_optin);
+    rc |= set_attr<64, 0, false>(ctx, smem_optin);
+    rc |= set_attr<64, 1, false>(ctx, smem_optin);
+    rc |= set_attr<64, 2, false>(ctx, smem_optin);
+    rc |= set_attr<64, 0, true>(ctx, smem_optin);
+    rc |= set_attr<128, 0, false>(ctx, smem_optin);
+    rc |= set_attr<128, 1, false>(ctx, smem_optin);
+    rc |= set_attr<128, 2, false>(ctx, smem_optin);
+    rc |= set_attr<128, 0, true>(ctx, smem_optin);
     return rc;
 }
 
+// variant 0: 64-slot candidate buffers; variant 1: 128-slot buffers
 int walk2_forces(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st) {
-    if (pot) return launch<0, true>(ctx, s, pot, warps, st);
-    switch (ctx->compensated) {
-        case 1: return launch<1, false>(ctx, s, nullptr, warps, st);
-        case 2: return launch<2, false>(ctx, s, nullptr, warps, st);
-        default: return launch<0, false>(ctx, s, nullptr, warps, st);
-    }
+    if (ctx->walk_variant == 1) return forces_cb<128>(ctx, s, pot, warps, st);
+    return forces_cb<64>(ctx, s, pot, warps, st);
 }
 
 }  // namespace nbx

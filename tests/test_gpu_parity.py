@@ -56,7 +56,7 @@ CASES = {
 
 @pytest.mark.parametrize("name", list(CASES))
 @pytest.mark.parametrize("mac", ["theta0.5", "reference"])
-@pytest.mark.parametrize("variant", [0, 2], ids=["walk2", "walk1"])
+@pytest.mark.parametrize("variant", [0, 1, 2], ids=["walk64", "walk128", "walk1"])
 def test_build_and_forces_match_oracle(cuda, name, mac, variant):
     b = CASES[name]()
     n = len(b.x)
@@ -269,13 +269,14 @@ def test_compensated_close_to_plain(cuda, mode):
 
 
 @pytest.mark.parametrize("warps", [4, 8, 16])
-def test_walk_launch_shapes_agree(cuda, warps):
+@pytest.mark.parametrize("variant", [0, 1])
+def test_walk_launch_shapes_agree(cuda, warps, variant):
     b = ic.plummer(5000)
     n = len(b.x)
     out = []
     for w in (8, warps):
         ctx = _ctx(n, theta=0.6, eps=0.005)
-        ctx.set_walk(w, 0)
+        ctx.set_walk(w, variant)
         ctx.set_systems([0, n])
         s = _state(b)
         ctx.build(s)
@@ -391,3 +392,23 @@ def test_plummer_2p20_properties(cuda):
     assert np.median(rel) <= MED_TOL and rel.max() <= MAX_TOL
     nl, _ = ctx.walk_stats()
     assert np.array_equal(nl[idx], f.nlist[idx])
+
+
+def test_autotune_picks_a_valid_config(cuda, tmp_path, monkeypatch):
+    from nns_gb300 import autotune
+    monkeypatch.setenv("NBX_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    b = ic.star_disk(20000)
+    n = len(b.x)
+    ctx = _ctx(n, theta=0.5, eps=0.01)
+    ctx.set_systems([0, n])
+    s = _state(b)
+    r = autotune.tune_walk(ctx, s, reps=1)
+    assert (r["warps"], r["variant"]) in autotune.CANDIDATES and not r["cached"]
+    r2 = autotune.tune_walk(ctx, s, reps=1)
+    assert r2["cached"] and r2["warps"] == r["warps"]
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    ot = O.build(b.x, b.y, b.z, b.m)
+    f = O.forces(b.x, b.y, b.z, b.m, ot, 0.25, 1e-4)
+    assert _rel(s.acc(), f.a).max() <= MAX_TOL
