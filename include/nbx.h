@@ -180,6 +180,34 @@ int nbx_direct_fp64(nbx_ctx *ctx, const float *x, const float *y, const float *z
 /* Per-body potential phi_i = -sum_j m_j / sqrt(|d|^2+eps2) over the walk's
  * interaction lists (self term removed), original index order; needs eps2 > 0. */
 int nbx_potential(nbx_ctx *ctx, const nbx_state *s, float *phi, void *stream);
+/* ---- differentiation (no counterpart in the reference) -------------------
+ * Gradients of L = sum_i |x_i(T) - x*_i|^2 after T kick-drift steps with
+ * respect to the initial positions, velocities and masses, through the
+ * Barnes-Hut forces with the interaction lists frozen to the recorded ones.
+ * Checkpoints every `checkpoint_every` steps; each segment is recomputed with
+ * its trees and interaction lists recorded (list_capacity entries per walk
+ * group) and reversed.  tape_steps >= checkpoint_every slots are allocated
+ * (tape_steps >= nsteps also enables nbx_adjoint_record / _replay_fp64). */
+typedef struct nbx_adjoint nbx_adjoint;
+int nbx_adjoint_create(nbx_ctx *ctx, int nsteps, int checkpoint_every, int list_capacity,
+                       int tape_steps, nbx_adjoint **out);
+int nbx_adjoint_destroy(nbx_adjoint *adj);
+/* Runs the T forward steps from s (advancing it) and returns the loss against
+ * the target positions (device arrays of n floats). */
+int nbx_adjoint_forward(nbx_ctx *ctx, nbx_adjoint *adj, const nbx_state *s, const float *tx,
+                        const float *ty, const float *tz, double *loss, void *stream);
+/* Reverse pass after nbx_adjoint_forward: dL/dx0, dL/dv0, dL/dm (device, n each). */
+int nbx_adjoint_backward(nbx_ctx *ctx, nbx_adjoint *adj, const nbx_state *s, float *gx, float *gy,
+                         float *gz, float *gvx, float *gvy, float *gvz, float *gm, void *stream);
+/* Records all T steps from s (trees and lists) for nbx_adjoint_replay_fp64. */
+int nbx_adjoint_record(nbx_ctx *ctx, nbx_adjoint *adj, const nbx_state *s, void *stream);
+/* FP64 loss of the recorded trajectory from an FP64 initial state
+ * (device double[7*n]: x,y,z,vx,vy,vz,m), structure and lists frozen. */
+int nbx_adjoint_replay_fp64(nbx_ctx *ctx, nbx_adjoint *adj, const double *state0, double *loss,
+                            void *stream);
+/* Device bytes held by the adjoint, and the last forward / backward times. */
+int nbx_adjoint_stats(nbx_adjoint *adj, int64_t *bytes, float *forward_ms, float *backward_ms);
+
 /* FP64 diagnostics of bodies [0,n): out[0..2] momentum, out[3] kinetic energy,
  * out[4..6] angular momentum, out[7] total mass (device double[8]). */
 int nbx_diagnostics_fp64(nbx_ctx *ctx, const nbx_state *s, int n, double *out, void *stream);

@@ -76,6 +76,13 @@ SIGNATURES = {
     "nbx_direct_fp64": (_I, [_P, _P, _P, _P, _P, _I, _P, _I, C.c_double, _P, _P]),
     "nbx_potential": (_I, [_P, C.POINTER(nbx_state), _P, _P]),
     "nbx_diagnostics_fp64": (_I, [_P, C.POINTER(nbx_state), _I, _P, _P]),
+    "nbx_adjoint_create": (_I, [_P, _I, _I, _I, _I, C.POINTER(_P)]),
+    "nbx_adjoint_destroy": (_I, [_P]),
+    "nbx_adjoint_forward": (_I, [_P, _P, C.POINTER(nbx_state), _P, _P, _P, C.POINTER(C.c_double), _P]),
+    "nbx_adjoint_backward": (_I, [_P, _P, C.POINTER(nbx_state)] + [_P] * 7 + [_P]),
+    "nbx_adjoint_record": (_I, [_P, _P, C.POINTER(nbx_state), _P]),
+    "nbx_adjoint_replay_fp64": (_I, [_P, _P, _P, C.POINTER(C.c_double), _P]),
+    "nbx_adjoint_stats": (_I, [_P, C.POINTER(C.c_int64), _PF, _PF]),
 }
 
 _lib = None

@@ -1,0 +1,610 @@
+// adjoint.cu -- gradients of a trajectory loss through the Barnes-Hut pipeline.
+//
+// Forward (kick-drift, Kernels.cu:581-600):  v' = v + dt a(x, m);  x' = x + d dt v'
+// with a_i = sum_{c in L(i)} M_c d (|d|^2+eps2)^-3/2, d = X_c - x_i, over the
+// interaction list L(i) of i's walk group, X_c, M_c the cell's centre of mass and
+// mass (a body: its position and mass).  The lists (MAC decisions) are piecewise
+// constant in the state and are frozen to the ones the forward recorded.
+//
+// Reverse step (lx, lv: gradients w.r.t. the step's outputs x', v'):
+//   lv_tot = lv + d dt lx;  g = dt lv_tot                       (k_adj_prep)
+//   force VJP with cotangent g, J(d) = I s^-3 - 3 d d^T s^-5:     (k_adj_force)
+//     target term  lx_i -= sum_c M_c J(d_ic) g_i
+//     source terms Gx_c += sum_i M_c J(d_ic) g_i, Gm_c += sum_i g_i . d_ic s^-3
+//   through X_c = sum m_j x_j / M_c, M_c = sum m_j to every member body j:   (k_adj_bodies)
+//     lx_j += m_j sum_{c ∋ j} Gx_c / M_c + Gx_body(j)
+//     lm_j += x_j . sum_{c ∋ j} Gx_c / M_c + sum_{c ∋ j} (Gm_c - Gx_c . X_c / M_c) + Gm_body(j)
+//   lx = lx + (terms above);  lv = lv_tot.
+// Loss L = sum_i |x_i(T) - x*_i|^2, so lx(T) = 2 (x(T) - x*), lv(T) = 0.
+//
+// Memory: checkpoints of (x, v) every C steps; a segment of C steps is
+// recomputed (bit-identical: every kernel is deterministic) with each step's
+// tree and interaction lists recorded on a tape, then reversed.
+//
+// An FP64 replay of the recorded trajectory (same lists and tree structure,
+// centres of mass recomputed from the perturbed state) gives the FP64 loss
+// used for finite-difference checks of the gradients.
+#include <cstring>
+#include <vector>
+
+#include "nbx_internal.cuh"
+
+namespace nbx {
+
+int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox, const float *const *bbox_ptrs);
+int walk2_record(Ctx *ctx, const nbx_state *s, int *rec_list, int *rec_len, int rec_cap, cudaStream_t st);
+
+struct TapeStep {
+    float4 *node4 = nullptr;
+    int *meta = nullptr, *parent = nullptr, *val = nullptr, *body_node = nullptr;
+    float4 *body4 = nullptr;
+    int *lists = nullptr, *list_len = nullptr;
+    unsigned *lvl = nullptr;  // BFS level starts (kMaxLevel + 2 entries)
+};
+
+struct Adj {
+    int T = 0, C = 0, lcap = 0, nseg = 0, n = 0, ngroups = 0, tape_steps = 0;
+    float *ckpt = nullptr;   // [nseg][6][n]: x,y,z,vx,vy,vz at the start of each segment
+    float *work = nullptr;   // [9][n]: working state
+    float *target = nullptr; // [3][n]
+    double *lam = nullptr;   // [7][n]: lx,ly,lz,lvx,lvy,lvz,lm
+    float *gcot = nullptr;   // [3][n]
+    float *tdx = nullptr;    // [3][n] target terms
+    double *G = nullptr;     // [4][NC]: Gx,Gy,Gz,Gm
+    double *loss = nullptr;  // [1]
+    double *r64 = nullptr;   // FP64 replay: [10][n] state + [4][NC] moments
+    std::vector<TapeStep> tape;
+    size_t bytes = 0;
+    // saved context pointers (the tape steps are swapped in for recording)
+    float4 *ctx_node4 = nullptr, *ctx_body4 = nullptr;
+    int *ctx_meta = nullptr, *ctx_parent = nullptr, *ctx_val = nullptr, *ctx_body_node = nullptr;
+    float fwd_ms = 0.f, bwd_ms = 0.f;
+};
+
+namespace {
+
+constexpr int kB = 256;
+
+__global__ void k_copy_state(const float *x, const float *y, const float *z, const float *vx, const float *vy,
+                             const float *vz, float *dst, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        dst[i] = x[i];
+        dst[n + i] = y[i];
+        dst[2 * n + i] = z[i];
+        dst[3 * n + i] = vx[i];
+        dst[4 * n + i] = vy[i];
+        dst[5 * n + i] = vz[i];
+    }
+}
+
+__global__ void k_loss_init(const float *x, const float *y, const float *z, const float *target, int n,
+                            double *lam, double *loss) {
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double dx = (double)x[i] - target[i], dy = (double)y[i] - target[n + i],
+                     dz = (double)z[i] - target[2 * n + i];
+        acc += dx * dx + dy * dy + dz * dz;
+        lam[i] = 2.0 * dx;
+        lam[n + i] = 2.0 * dy;
+        lam[2 * n + i] = 2.0 * dz;
+        lam[3 * n + i] = 0.0;
+        lam[4 * n + i] = 0.0;
+        lam[5 * n + i] = 0.0;
+        lam[6 * n + i] = 0.0;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc);
+}
+
+// lv_tot = lv + d dt lx; g = dt lv_tot
+__global__ void k_adj_prep(double *lam, float *gcot, int n, double dt, double ddt) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const double lv = lam[(3 + k) * n + i] + ddt * lam[k * n + i];
+            lam[(3 + k) * n + i] = lv;
+            gcot[k * n + i] = (float)(dt * lv);
+        }
+    }
+}
+
+// Force VJP over the recorded lists, one warp per walk group.  Per-lane
+// contributions to each list entry are reduced through shared memory in
+// chunks of 8 entries (row stride 33 avoids bank conflicts) and added to the
+// FP64 source gradients with atomics.
+constexpr int kAdjWarps = 4;
+constexpr int kChunk = 8;
+
+__global__ void __launch_bounds__(kAdjWarps * 32)
+    k_adj_force(const float4 *__restrict__ node4, const float4 *__restrict__ body4, const int *__restrict__ val,
+                const int *__restrict__ body_node, const int *__restrict__ groups, int ngroups,
+                const int *__restrict__ body_sys, const int *__restrict__ sys_off, const int *__restrict__ lists,
+                const int *__restrict__ list_len, int lcap, const float *__restrict__ gcot, int n, float eps2,
+                double *__restrict__ G, int nc_cap, float *__restrict__ tdx) {
+    __shared__ float red[kAdjWarps][kChunk * 4][33];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int g = blockIdx.x * kAdjWarps + w; g < ngroups; g += gridDim.x * kAdjWarps) {
+        const int p0 = groups[g];
+        const int s = body_sys[p0];
+        const int end = min(sys_off[s + 1], p0 + 32);
+        const int p = p0 + lane;
+        const bool valid = p < end;
+        const float4 me = body4[valid ? p : p0];
+        const int mynode = valid ? body_node[p] : -1;
+        float gx = 0.f, gy = 0.f, gz = 0.f;
+        int ob = 0;
+        if (valid) {
+            ob = val[p];
+            gx = gcot[ob];
+            gy = gcot[n + ob];
+            gz = gcot[2 * n + ob];
+        }
+        float ox = 0.f, oy = 0.f, oz = 0.f;
+        const int len = list_len[g];
+        const int *L = lists + (size_t)g * lcap;
+        for (int base = 0; base < len; base += kChunk) {
+            const int cnt = min(kChunk, len - base);
+            const int cmine = lane < cnt ? L[base + lane] : 0;
+#pragma unroll
+            for (int e = 0; e < kChunk; e++) {
+                float vx = 0.f, vy = 0.f, vz = 0.f, vm = 0.f;
+                if (e < cnt) {
+                    const int c = __shfl_sync(0xffffffffu, cmine, e);
+                    const float4 q = node4[c];
+                    const float dx = q.x - me.x, dy = q.y - me.y, dz = q.z - me.z;
+                    const float s2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+                    const float inv = rsqrtf(s2);
+                    const float inv3 = inv * inv * inv;
+                    const float inv5 = inv3 * inv * inv;
+                    const float dg = fmaf(dz, gz, fmaf(dy, gy, dx * gx));
+                    const float t = 3.f * dg * inv5;
+                    const float jx = fmaf(gx, inv3, -dx * t);
+                    const float jy = fmaf(gy, inv3, -dy * t);
+                    const float jz = fmaf(gz, inv3, -dz * t);
+                    if (c != mynode) {  // a body's own entry has d = 0 and contributes nothing net
+                        vx = q.w * jx;
+                        vy = q.w * jy;
+                        vz = q.w * jz;
+                        vm = dg * inv3;
+                        ox += vx;
+                        oy += vy;
+                        oz += vz;
+                    }
+                }
+                red[w][4 * e + 0][lane] = vx;
+                red[w][4 * e + 1][lane] = vy;
+                red[w][4 * e + 2][lane] = vz;
+                red[w][4 * e + 3][lane] = vm;
+            }
+            __syncwarp();
+            // lane l reduces row l: entry l/4, component l%4
+            const int crow = __shfl_sync(0xffffffffu, cmine, (lane >> 2) & 7);
+            if (lane < 4 * cnt) {
+                float acc = 0.f;
+#pragma unroll 8
+                for (int k = 0; k < 32; k++) acc += red[w][lane][k];
+                if (crow < nc_cap) atomicAdd(&G[(size_t)(lane & 3) * nc_cap + crow], (double)acc);
+            }
+            __syncwarp();
+        }
+        if (valid) {
+            tdx[ob] = -ox;
+            tdx[n + ob] = -oy;
+            tdx[2 * n + ob] = -oz;
+        }
+    }
+}
+
+// Gradients through the centres of mass to every body, and the state update.
+__global__ void k_adj_bodies(const float4 *__restrict__ node4, const float4 *__restrict__ body4,
+                             const int *__restrict__ val, const int *__restrict__ body_node,
+                             const int *__restrict__ parent, const double *__restrict__ G, int nc_cap,
+                             const float *__restrict__ tdx, double *lam, int n) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const int i = val[p];
+        const int b = body_node[p];
+        const float4 me = body4[p];
+        double sax = 0.0, say = 0.0, saz = 0.0, sb = 0.0;
+        int cur = parent[b];
+        for (int guard = 0; guard < 64 && cur >= 0; guard++) {
+            const float4 q = node4[cur];
+            const double M = q.w;
+            const double gxc = G[cur], gyc = G[(size_t)nc_cap + cur], gzc = G[2 * (size_t)nc_cap + cur],
+                         gmc = G[3 * (size_t)nc_cap + cur];
+            sax += gxc / M;
+            say += gyc / M;
+            saz += gzc / M;
+            sb += gmc - (gxc * q.x + gyc * q.y + gzc * q.z) / M;
+            cur = parent[cur];
+        }
+        const double m = me.w;
+        lam[i] += tdx[i] + m * sax + G[b];
+        lam[n + i] += tdx[n + i] + m * say + G[(size_t)nc_cap + b];
+        lam[2 * n + i] += tdx[2 * n + i] + m * saz + G[2 * (size_t)nc_cap + b];
+        lam[6 * n + i] += (double)me.x * sax + (double)me.y * say + (double)me.z * saz + sb +
+                          G[3 * (size_t)nc_cap + b];
+    }
+}
+
+__global__ void k_lam_out(const double *lam, int n, float *gx, float *gy, float *gz, float *gvx, float *gvy,
+                          float *gvz, float *gm) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        gx[i] = (float)lam[i];
+        gy[i] = (float)lam[n + i];
+        gz[i] = (float)lam[2 * n + i];
+        gvx[i] = (float)lam[3 * n + i];
+        gvy[i] = (float)lam[4 * n + i];
+        gvz[i] = (float)lam[5 * n + i];
+        gm[i] = (float)lam[6 * n + i];
+    }
+}
+
+// ---- FP64 replay of a recorded trajectory ------------------------------
+// r64 layout: [0..2] x,y,z  [3..5] vx,vy,vz  [6] m  [7..9] a  (original order, n each)
+__global__ void k_r64_moments_level(int level, const unsigned *lvl, const int *__restrict__ meta,
+                                    const int *__restrict__ val, const double *__restrict__ r64, int n,
+                                    double *__restrict__ M64, int nc_cap) {
+    const unsigned beg = lvl[level], end = lvl[level + 1];
+    for (unsigned b = beg + blockIdx.x * blockDim.x + threadIdx.x; b < end; b += gridDim.x * blockDim.x) {
+        const int pm = meta[b];
+        if (pm < 0) continue;
+        const int first = pm & 0x0fffffff, nch = ((pm >> 28) & 7) + 1;
+        double sm = 0, sx = 0, sy = 0, sz = 0;
+        for (int c = first; c < first + nch; c++) {
+            const int cm = meta[c];
+            if (cm < 0) {
+                const int i = val[cm & 0x03ffffff];
+                const double mb = r64[6 * (size_t)n + i];
+                sm += mb;
+                sx += mb * r64[i];
+                sy += mb * r64[(size_t)n + i];
+                sz += mb * r64[2 * (size_t)n + i];
+            } else {
+                sm += M64[c];
+                sx += M64[c] * M64[(size_t)nc_cap + c];
+                sy += M64[c] * M64[2 * (size_t)nc_cap + c];
+                sz += M64[c] * M64[3 * (size_t)nc_cap + c];
+            }
+        }
+        M64[b] = sm;
+        M64[(size_t)nc_cap + b] = sx / sm;
+        M64[2 * (size_t)nc_cap + b] = sy / sm;
+        M64[3 * (size_t)nc_cap + b] = sz / sm;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_r64_force(const int *__restrict__ meta, const int *__restrict__ val,
+                                                  const int *__restrict__ groups, int ngroups,
+                                                  const int *__restrict__ body_sys, const int *__restrict__ sys_off,
+                                                  const int *__restrict__ lists, const int *__restrict__ list_len,
+                                                  int lcap, double *r64, int n, const double *__restrict__ M64,
+                                                  int nc_cap, double eps2) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+    for (int g = blockIdx.x * warps + w; g < ngroups; g += gridDim.x * warps) {
+        const int p0 = groups[g];
+        const int end = min(sys_off[body_sys[p0] + 1], p0 + 32);
+        const int p = p0 + lane;
+        const bool valid = p < end;
+        const int i = val[valid ? p : p0];
+        const double xi = r64[i], yi = r64[(size_t)n + i], zi = r64[2 * (size_t)n + i];
+        double ax = 0, ay = 0, az = 0;
+        const int len = list_len[g];
+        const int *L = lists + (size_t)g * lcap;
+        for (int e = 0; e < len; e++) {
+            const int c = L[e];
+            const int cm = meta[c];
+            double X, Y, Z, Mc;
+            if (cm < 0) {
+                const int j = val[cm & 0x03ffffff];
+                X = r64[j];
+                Y = r64[(size_t)n + j];
+                Z = r64[2 * (size_t)n + j];
+                Mc = r64[6 * (size_t)n + j];
+            } else {
+                Mc = M64[c];
+                X = M64[(size_t)nc_cap + c];
+                Y = M64[2 * (size_t)nc_cap + c];
+                Z = M64[3 * (size_t)nc_cap + c];
+            }
+            const double dx = X - xi, dy = Y - yi, dz = Z - zi;
+            const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+            const double f = Mc / (r2 * sqrt(r2));
+            ax += f * dx;
+            ay += f * dy;
+            az += f * dz;
+        }
+        if (valid) {
+            r64[7 * (size_t)n + i] = ax;
+            r64[8 * (size_t)n + i] = ay;
+            r64[9 * (size_t)n + i] = az;
+        }
+    }
+}
+
+__global__ void k_r64_update(double *r64, int n, double dt, double ddt) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        for (int k = 0; k < 3; k++) {
+            const double v = r64[(3 + k) * (size_t)n + i] + dt * r64[(7 + k) * (size_t)n + i];
+            r64[(3 + k) * (size_t)n + i] = v;
+            r64[k * (size_t)n + i] += ddt * v;
+        }
+    }
+}
+
+__global__ void k_r64_loss(const double *r64, const float *target, int n, double *loss) {
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double dx = r64[i] - target[i], dy = r64[(size_t)n + i] - target[n + i],
+                     dz = r64[2 * (size_t)n + i] - target[2 * n + i];
+        acc += dx * dx + dy * dy + dz * dz;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc);
+}
+
+__global__ void k_copy_lvl(const unsigned *hist, int ntiles, const unsigned *totals, unsigned *lvl) {
+    const int l = threadIdx.x;
+    if (l <= kMaxLevel + 1) {
+        const unsigned T = totals[1];
+        unsigned v = l >= 64 ? T : hist[(size_t)(l << 2) * ntiles];
+        lvl[l] = v < T ? v : T;
+    }
+}
+
+int grid_for(int n) {
+    int g = ceil_div(n, kB);
+    return g < 1 ? 1 : (g > 2048 ? 2048 : g);
+}
+
+void swap_in(Ctx *ctx, Adj *a, int j) {
+    TapeStep &t = a->tape[j];
+    ctx->d_node4 = t.node4;
+    ctx->d_meta = t.meta;
+    ctx->d_parent = t.parent;
+    ctx->d_val = t.val;
+    ctx->d_body_node = t.body_node;
+    ctx->d_body4 = t.body4;
+}
+
+void swap_out(Ctx *ctx, Adj *a) {
+    ctx->d_node4 = a->ctx_node4;
+    ctx->d_meta = a->ctx_meta;
+    ctx->d_parent = a->ctx_parent;
+    ctx->d_val = a->ctx_val;
+    ctx->d_body_node = a->ctx_body_node;
+    ctx->d_body4 = a->ctx_body4;
+}
+
+template <typename T>
+int amalloc(Ctx *ctx, Adj *a, T **p, size_t count) {
+    if (count == 0) count = 1;
+    if (cudaMalloc((void **)p, count * sizeof(T)) != cudaSuccess) {
+        ctx->last_error = "adjoint: device allocation failed";
+        *p = nullptr;
+        return NBX_ERR_NOMEM;
+    }
+    a->bytes += count * sizeof(T);
+    return NBX_OK;
+}
+
+// One recorded step j of the working state: build into tape slot j, walk with
+// list recording, integrate.
+int recorded_step(Ctx *ctx, Adj *a, const nbx_state *s, int j, cudaStream_t st) {
+    swap_in(ctx, a, j);
+    int rc = build_tree(ctx, s, st, false, nullptr);
+    if (!rc) {
+        k_copy_lvl<<<1, 64, 0, st>>>(ctx->d_hist, ctx->cap_tiles_node, ctx->d_totals, a->tape[j].lvl);
+        ++ctx->launches;
+        rc = walk2_record(ctx, s, a->tape[j].lists, a->tape[j].list_len, a->lcap, st);
+    }
+    if (!rc) rc = integrate(ctx, s, ctx->p.dt, ctx->p.dampening, a->n, st);
+    swap_out(ctx, a);
+    return rc;
+}
+
+nbx_state work_state(Adj *a, const nbx_state *s) {
+    const int n = a->n;
+    nbx_state w{};
+    w.x = a->work;
+    w.y = a->work + n;
+    w.z = a->work + 2 * n;
+    w.vx = a->work + 3 * n;
+    w.vy = a->work + 4 * n;
+    w.vz = a->work + 5 * n;
+    w.ax = a->work + 6 * n;
+    w.ay = a->work + 7 * n;
+    w.az = a->work + 8 * n;
+    w.m = s->m;
+    return w;
+}
+
+}  // namespace
+
+int adjoint_create(Ctx *ctx, int T, int C, int lcap, int tape_steps, Adj **out) {
+    *out = nullptr;
+    if (ctx->nsys < 1 || T < 1 || C < 1 || lcap < 64 || tape_steps < C) return NBX_ERR_ARG;
+    Adj *a = new Adj();
+    a->T = T;
+    a->C = C;
+    a->lcap = lcap;
+    a->n = (int)ctx->nbodies;
+    a->ngroups = ctx->ngroups;
+    a->nseg = ceil_div(T, C);
+    a->tape_steps = tape_steps;
+    const int n = a->n, NC = ctx->cap_nodes;
+    int rc = 0;
+    rc |= amalloc(ctx, a, &a->ckpt, (size_t)a->nseg * 6 * n);
+    rc |= amalloc(ctx, a, &a->work, (size_t)9 * n);
+    rc |= amalloc(ctx, a, &a->target, (size_t)3 * n);
+    rc |= amalloc(ctx, a, &a->lam, (size_t)7 * n);
+    rc |= amalloc(ctx, a, &a->gcot, (size_t)3 * n);
+    rc |= amalloc(ctx, a, &a->tdx, (size_t)3 * n);
+    rc |= amalloc(ctx, a, &a->G, (size_t)4 * NC);
+    rc |= amalloc(ctx, a, &a->loss, 2);
+    rc |= amalloc(ctx, a, &a->r64, (size_t)10 * n + (size_t)4 * NC);
+    a->tape.resize(tape_steps);
+    for (int j = 0; j < tape_steps && rc == 0; j++) {
+        TapeStep &t = a->tape[j];
+        rc |= amalloc(ctx, a, &t.node4, NC);
+        rc |= amalloc(ctx, a, &t.meta, NC);
+        rc |= amalloc(ctx, a, &t.parent, NC);
+        rc |= amalloc(ctx, a, &t.val, ctx->cap_bodies);
+        rc |= amalloc(ctx, a, &t.body_node, ctx->cap_bodies);
+        rc |= amalloc(ctx, a, &t.body4, ctx->cap_bodies);
+        rc |= amalloc(ctx, a, &t.lists, (size_t)a->ngroups * lcap);
+        rc |= amalloc(ctx, a, &t.list_len, a->ngroups);
+        rc |= amalloc(ctx, a, &t.lvl, kMaxLevel + 2);
+    }
+    a->ctx_node4 = ctx->d_node4;
+    a->ctx_meta = ctx->d_meta;
+    a->ctx_parent = ctx->d_parent;
+    a->ctx_val = ctx->d_val;
+    a->ctx_body_node = ctx->d_body_node;
+    a->ctx_body4 = ctx->d_body4;
+    *out = a;
+    return rc;
+}
+
+void adjoint_destroy(Adj *a) {
+    if (!a) return;
+    void *p[] = {a->ckpt, a->work, a->target, a->lam, a->gcot, a->tdx, a->G, a->loss, a->r64};
+    for (void *q : p)
+        if (q) cudaFree(q);
+    for (TapeStep &t : a->tape) {
+        void *r[] = {t.node4, t.meta, t.parent, t.val, t.body_node, t.body4, t.lists, t.list_len, t.lvl};
+        for (void *q : r)
+            if (q) cudaFree(q);
+    }
+    delete a;
+}
+
+size_t adjoint_bytes(const Adj *a) { return a->bytes; }
+
+// Forward T steps from s (x, v, m), checkpoints every C steps; s ends at x(T), v(T).
+int adjoint_forward(Ctx *ctx, Adj *a, const nbx_state *s, const float *tx, const float *ty, const float *tz,
+                    double *loss_host, cudaStream_t st) {
+    const int n = a->n;
+    if (n != ctx->nbodies) return NBX_ERR_STATE;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    NBX_CUDA(cudaMemcpyAsync(a->target, tx, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+    NBX_CUDA(cudaMemcpyAsync(a->target + n, ty, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+    NBX_CUDA(cudaMemcpyAsync(a->target + 2 * n, tz, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+    for (int k = 0; k < a->T; k++) {
+        if (k % a->C == 0) {
+            k_copy_state<<<grid_for(n), kB, 0, st>>>(s->x, s->y, s->z, s->vx, s->vy, s->vz,
+                                                     a->ckpt + (size_t)(k / a->C) * 6 * n, n);
+            ++ctx->launches;
+        }
+        int rc = build_tree(ctx, s, st, false, nullptr);
+        if (!rc) rc = walk_forces(ctx, s, st);
+        if (!rc) rc = integrate(ctx, s, ctx->p.dt, ctx->p.dampening, n, st);
+        if (rc) return rc;
+    }
+    NBX_CUDA(cudaMemsetAsync(a->loss, 0, sizeof(double), st));
+    k_loss_init<<<grid_for(n), kB, 0, st>>>(s->x, s->y, s->z, a->target, n, a->lam, a->loss);
+    ++ctx->launches;
+    cudaEventRecord(e1, st);
+    NBX_CUDA(cudaMemcpyAsync(loss_host, a->loss, sizeof(double), cudaMemcpyDeviceToHost, st));
+    NBX_CUDA(cudaStreamSynchronize(st));
+    cudaEventElapsedTime(&a->fwd_ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return NBX_OK;
+}
+
+// Reverse through all segments; writes dL/dx0, dL/dv0, dL/dm (original order).
+int adjoint_backward(Ctx *ctx, Adj *a, const nbx_state *s, float *gx, float *gy, float *gz, float *gvx, float *gvy,
+                     float *gvz, float *gm, cudaStream_t st) {
+    const int n = a->n;
+    const int NC = ctx->cap_nodes;
+    const double dt = ctx->p.dt, ddt = (double)ctx->p.dampening * ctx->p.dt;
+    nbx_state w = work_state(a, s);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    for (int seg = a->nseg - 1; seg >= 0; seg--) {
+        const int k0 = seg * a->C;
+        const int steps = (k0 + a->C <= a->T) ? a->C : a->T - k0;
+        NBX_CUDA(cudaMemcpyAsync(a->work, a->ckpt + (size_t)seg * 6 * n, sizeof(float) * 6 * n,
+                                 cudaMemcpyDeviceToDevice, st));
+        for (int j = 0; j < steps; j++) {
+            int rc = recorded_step(ctx, a, &w, j, st);
+            if (rc) return rc;
+        }
+        for (int j = steps - 1; j >= 0; j--) {
+            TapeStep &t = a->tape[j];
+            k_adj_prep<<<grid_for(n), kB, 0, st>>>(a->lam, a->gcot, n, dt, ddt);
+            NBX_CUDA(cudaMemsetAsync(a->G, 0, sizeof(double) * 4 * (size_t)NC, st));
+            const int blocks = ceil_div(a->ngroups, kAdjWarps);
+            k_adj_force<<<blocks < ctx->nsm * 16 ? blocks : ctx->nsm * 16, kAdjWarps * 32, 0, st>>>(
+                t.node4, t.body4, t.val, t.body_node, ctx->d_groups, a->ngroups, ctx->d_body_sys, ctx->d_sys_off,
+                t.lists, t.list_len, a->lcap, a->gcot, n, ctx->eps2, a->G, NC, a->tdx);
+            k_adj_bodies<<<grid_for(n), kB, 0, st>>>(t.node4, t.body4, t.val, t.body_node, t.parent, a->G, NC,
+                                                      a->tdx, a->lam, n);
+            ctx->launches += 3;
+        }
+    }
+    k_lam_out<<<grid_for(n), kB, 0, st>>>(a->lam, n, gx, gy, gz, gvx, gvy, gvz, gm);
+    ++ctx->launches;
+    cudaEventRecord(e1, st);
+    NBX_CUDA(cudaStreamSynchronize(st));
+    cudaEventElapsedTime(&a->bwd_ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    NBX_CUDA(cudaGetLastError());
+    return NBX_OK;
+}
+
+// Records the whole T-step trajectory from s (needs tape_steps >= T).
+int adjoint_record_all(Ctx *ctx, Adj *a, const nbx_state *s, cudaStream_t st) {
+    if (a->tape_steps < a->T) return NBX_ERR_ARG;
+    const int n = a->n;
+    nbx_state w = work_state(a, s);
+    k_copy_state<<<grid_for(n), kB, 0, st>>>(s->x, s->y, s->z, s->vx, s->vy, s->vz, a->work, n);
+    ++ctx->launches;
+    for (int k = 0; k < a->T; k++) {
+        int rc = recorded_step(ctx, a, &w, k, st);
+        if (rc) return rc;
+    }
+    NBX_CUDA(cudaStreamSynchronize(st));
+    return NBX_OK;
+}
+
+// FP64 loss of the recorded trajectory from an FP64 initial state (x0,v0,m as
+// double arrays [7][n] on the device), lists and tree structure frozen.
+int adjoint_replay_fp64(Ctx *ctx, Adj *a, const double *state0, double *loss_host, cudaStream_t st) {
+    if (a->tape_steps < a->T) return NBX_ERR_ARG;
+    const int n = a->n, NC = ctx->cap_nodes;
+    double *M64 = a->r64 + (size_t)10 * n;
+    NBX_CUDA(cudaMemcpyAsync(a->r64, state0, sizeof(double) * 7 * n, cudaMemcpyDeviceToDevice, st));
+    const double dt = ctx->p.dt, ddt = (double)ctx->p.dampening * ctx->p.dt;
+    for (int k = 0; k < a->T; k++) {
+        TapeStep &t = a->tape[k];
+        for (int level = kMaxLevel - 2; level >= 1; level--)
+            k_r64_moments_level<<<ctx->nsm * 2, kB, 0, st>>>(level, t.lvl, t.meta, t.val, a->r64, n, M64, NC);
+        const int blocks = ceil_div(a->ngroups, 4);
+        k_r64_force<<<blocks < ctx->nsm * 16 ? blocks : ctx->nsm * 16, 128, 0, st>>>(
+            t.meta, t.val, ctx->d_groups, a->ngroups, ctx->d_body_sys, ctx->d_sys_off, t.lists, t.list_len, a->lcap,
+            a->r64, n, M64, NC, (double)ctx->eps2);
+        k_r64_update<<<grid_for(n), kB, 0, st>>>(a->r64, n, dt, ddt);
+        ctx->launches += kMaxLevel - 2 + 2;
+    }
+    NBX_CUDA(cudaMemsetAsync(a->loss + 1, 0, sizeof(double), st));
+    k_r64_loss<<<grid_for(n), kB, 0, st>>>(a->r64, a->target, n, a->loss + 1);
+    ++ctx->launches;
+    NBX_CUDA(cudaMemcpyAsync(loss_host, a->loss + 1, sizeof(double), cudaMemcpyDeviceToHost, st));
+    NBX_CUDA(cudaStreamSynchronize(st));
+    NBX_CUDA(cudaGetLastError());
+    return NBX_OK;
+}
+
+void adjoint_times(const Adj *a, float *fwd_ms, float *bwd_ms) {
+    if (fwd_ms) *fwd_ms = a->fwd_ms;
+    if (bwd_ms) *bwd_ms = a->bwd_ms;
+}
+
+}  // namespace nbx

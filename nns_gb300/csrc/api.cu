@@ -20,6 +20,17 @@ int bbox_ref(Ctx *ctx, const float *x, const float *y, const float *z, float *mi
 int direct_fp64(Ctx *ctx, const float *x, const float *y, const float *z, const float *m, int n,
                 const int *targets, int nt, double eps2, double *acc, cudaStream_t st);
 int diagnostics_fp64(Ctx *ctx, const nbx_state *s, int n, double *out, cudaStream_t st);
+struct Adj;
+int adjoint_create(Ctx *ctx, int T, int C, int lcap, int tape_steps, Adj **out);
+void adjoint_destroy(Adj *a);
+size_t adjoint_bytes(const Adj *a);
+int adjoint_forward(Ctx *ctx, Adj *a, const nbx_state *s, const float *tx, const float *ty, const float *tz,
+                    double *loss_host, cudaStream_t st);
+int adjoint_backward(Ctx *ctx, Adj *a, const nbx_state *s, float *gx, float *gy, float *gz, float *gvx, float *gvy,
+                     float *gvz, float *gm, cudaStream_t st);
+int adjoint_record_all(Ctx *ctx, Adj *a, const nbx_state *s, cudaStream_t st);
+int adjoint_replay_fp64(Ctx *ctx, Adj *a, const double *state0, double *loss_host, cudaStream_t st);
+void adjoint_times(const Adj *a, float *fwd_ms, float *bwd_ms);
 
 namespace {
 
@@ -612,6 +623,70 @@ int nbx_potential(nbx_ctx *c, const nbx_state *s, float *phi, void *stream) {
 int nbx_diagnostics_fp64(nbx_ctx *c, const nbx_state *s, int n, double *out, void *stream) {
     if (!c || !s || !out || n < 0) return NBX_ERR_ARG;
     return nbx::diagnostics_fp64(C(c), s, n, out, S(stream));
+}
+
+/* ---------------- differentiation ---------------- */
+
+int nbx_adjoint_create(nbx_ctx *c, int nsteps, int checkpoint_every, int list_capacity, int tape_steps,
+                       nbx_adjoint **out) {
+    if (!c || !out) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    if (ctx->nsys < 1) return NBX_ERR_STATE;
+    nbx::Adj *a = nullptr;
+    int rc = nbx::adjoint_create(ctx, nsteps, checkpoint_every, list_capacity, tape_steps, &a);
+    if (rc) {
+        nbx::adjoint_destroy(a);
+        *out = nullptr;
+        return rc;
+    }
+    *out = reinterpret_cast<nbx_adjoint *>(a);
+    return NBX_OK;
+}
+
+int nbx_adjoint_destroy(nbx_adjoint *a) {
+    if (!a) return NBX_ERR_ARG;
+    cudaDeviceSynchronize();
+    nbx::adjoint_destroy(reinterpret_cast<nbx::Adj *>(a));
+    return NBX_OK;
+}
+
+int nbx_adjoint_forward(nbx_ctx *c, nbx_adjoint *a, const nbx_state *s, const float *tx, const float *ty,
+                        const float *tz, double *loss, void *stream) {
+    if (!c || !a || !s || !tx || !ty || !tz || !loss) return NBX_ERR_ARG;
+    int rc = nbx::adjoint_forward(C(c), reinterpret_cast<nbx::Adj *>(a), s, tx, ty, tz, loss, S(stream));
+    if (rc) return rc;
+    return nbx_sync_status(c, stream);
+}
+
+int nbx_adjoint_backward(nbx_ctx *c, nbx_adjoint *a, const nbx_state *s, float *gx, float *gy, float *gz,
+                         float *gvx, float *gvy, float *gvz, float *gm, void *stream) {
+    if (!c || !a || !s || !gx || !gy || !gz || !gvx || !gvy || !gvz || !gm) return NBX_ERR_ARG;
+    int rc = nbx::adjoint_backward(C(c), reinterpret_cast<nbx::Adj *>(a), s, gx, gy, gz, gvx, gvy, gvz, gm,
+                                   S(stream));
+    if (rc) return rc;
+    return nbx_sync_status(c, stream);
+}
+
+int nbx_adjoint_record(nbx_ctx *c, nbx_adjoint *a, const nbx_state *s, void *stream) {
+    if (!c || !a || !s) return NBX_ERR_ARG;
+    int rc = nbx::adjoint_record_all(C(c), reinterpret_cast<nbx::Adj *>(a), s, S(stream));
+    if (rc) return rc;
+    return nbx_sync_status(c, stream);
+}
+
+int nbx_adjoint_replay_fp64(nbx_ctx *c, nbx_adjoint *a, const double *state0, double *loss, void *stream) {
+    if (!c || !a || !state0 || !loss) return NBX_ERR_ARG;
+    int rc = nbx::adjoint_replay_fp64(C(c), reinterpret_cast<nbx::Adj *>(a), state0, loss, S(stream));
+    if (rc) return rc;
+    return nbx_sync_status(c, stream);
+}
+
+int nbx_adjoint_stats(nbx_adjoint *a, int64_t *bytes, float *forward_ms, float *backward_ms) {
+    if (!a) return NBX_ERR_ARG;
+    const nbx::Adj *p = reinterpret_cast<const nbx::Adj *>(a);
+    if (bytes) *bytes = (int64_t)nbx::adjoint_bytes(p);
+    nbx::adjoint_times(p, forward_ms, backward_ms);
+    return NBX_OK;
 }
 
 }  // extern "C"

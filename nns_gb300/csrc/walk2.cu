@@ -59,6 +59,19 @@ __device__ __forceinline__ u64 fma2(u64 a, u64 b, u64 c) {
     return r;
 }
 
+// Hardware reciprocal square root (MUFU); r >= eps^2 > 0 is never subnormal,
+// so flushing subnormals changes nothing and saves the scaling fix-up.
+__device__ __forceinline__ float rsq(float r) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(r));
+    return y;
+}
+
+// depth0 * 4^-k exactly (a power-of-two product is exact unless it underflows)
+__device__ __forceinline__ float scale4(float d0, int k) {
+    return d0 * __int_as_float((127 - 2 * k) << 23);
+}
+
 // Kahan step s += v with compensation c (scalar, explicit rounding).
 __device__ __forceinline__ void kahan(float &s, float &c, float v) {
     const float y = __fsub_rn(v, c);
@@ -77,6 +90,7 @@ struct WarpBuf {
     ulonglong2 cb[kPairs];  //         (z0,z1) (m0,m1)
     u64 cd[kPairs];         //         (dp0,dp1)
     int cid[CB];            //         node | level << 26
+    int bid[CB];            // body node ids (interaction-list recording only)
 };
 
 __device__ __forceinline__ void put4(ulonglong2 *a, ulonglong2 *b, int slot, float4 q) {
@@ -116,14 +130,23 @@ __device__ __forceinline__ void accumulate(Sums &a, u64 f, u64 mm, u64 ri, u64 d
     if (Pot) a.p = fma2(mm, ri, a.p);
 }
 
-template <int CB, int Mode, bool Pot>
-__global__ void __launch_bounds__(512, 2)
+// CB = 64: 64-register budget (two 16-warp or four 8-warp blocks per SM);
+// CB = 128: up to 85 registers for more loads in flight (three 8-warp blocks).
+template <int CB>
+struct WalkBounds {
+    static constexpr int kThreads = CB == 64 ? 512 : 256;
+    static constexpr int kMinBlocks = CB == 64 ? 2 : 3;
+};
+
+template <int CB, int Mode, bool Pot, bool Rec>
+__global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMinBlocks)
     k_walk2(const float4 *__restrict__ node4, const int *__restrict__ meta, const float4 *__restrict__ body4,
             const int *__restrict__ val, const int *__restrict__ groups, int ngroups,
             const int *__restrict__ body_sys, const int *__restrict__ sys_off, const float *__restrict__ depth0,
             const int *__restrict__ root_first, const int *__restrict__ root_nch, float eps2, int stack_cap,
             float *__restrict__ ax, float *__restrict__ ay, float *__restrict__ az, float *__restrict__ pot,
-            int *__restrict__ nlist, int *__restrict__ nopen, DevStatus *st) {
+            int *__restrict__ nlist, int *__restrict__ nopen, DevStatus *st, int *__restrict__ rec_list,
+            int *__restrict__ rec_len, int rec_cap) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     if (st->code != 0) return;
     const int warps = blockDim.x >> 5;
@@ -147,8 +170,9 @@ __global__ void __launch_bounds__(512, 2)
         const u64 px = pk(me.x, me.x), py = pk(me.y, me.y), pz = pk(me.z, me.z);
         const float d0 = depth0[s];
         Sums acc;
-        int top = 0, nb = 0, len = 0, opened = 0;
+        int top = 0, nb = 0, len = 0, opened = 0, nrec = 0;
         bool overflow = false;
+        int *rec = Rec ? rec_list + (size_t)g * rec_cap : nullptr;
 
         // root children: cells are opened unconditionally, bodies interact
         {
@@ -161,7 +185,10 @@ __global__ void __launch_bounds__(512, 2)
             }
             const unsigned bodies = __ballot_sync(0xffffffffu, lane < rn && cm < 0);
             const unsigned cells = __ballot_sync(0xffffffffu, lane < rn && cm >= 0);
-            if (lane < rn && cm < 0) put4(buf.ba, buf.bb, __popc(bodies & lt), q);
+            if (lane < rn && cm < 0) {
+                put4(buf.ba, buf.bb, __popc(bodies & lt), q);
+                if (Rec) buf.bid[__popc(bodies & lt)] = rf + lane;
+            }
             if (lane < rn && cm >= 0) stack[__popc(cells & lt)] = (rf + lane) | (1 << kLevelShift);
             nb = __popc(bodies);
             top = __popc(cells);
@@ -220,11 +247,14 @@ __global__ void __launch_bounds__(512, 2)
                 const float4 q = ok ? node4[c] : make_float4(0.f, 0.f, 0.f, 0.f);
                 const unsigned bm = __ballot_sync(0xffffffffu, ok && cm < 0);
                 const unsigned cmk = __ballot_sync(0xffffffffu, ok && cm >= 0);
-                if (ok && cm < 0) put4(buf.ba, buf.bb, nbody + __popc(bm & lt), q);
+                if (ok && cm < 0) {
+                    put4(buf.ba, buf.bb, nbody + __popc(bm & lt), q);
+                    if (Rec) buf.bid[nbody + __popc(bm & lt)] = c;
+                }
                 if (ok && cm >= 0) {
                     const int slot = ncell + __popc(cmk & lt);
                     put4(buf.ca, buf.cb, slot, q);
-                    reinterpret_cast<float *>(&buf.cd[slot >> 1])[slot & 1] = ldexpf(d0, -2 * lj);
+                    reinterpret_cast<float *>(&buf.cd[slot >> 1])[slot & 1] = scale4(d0, lj);
                     buf.cid[slot] = c | ((lj + 1) << kLevelShift);  // children are at level lj+1
                 }
                 nbody += __popc(bm);
@@ -252,9 +282,14 @@ __global__ void __launch_bounds__(512, 2)
                 r = fma2(dz, dz, r);
                 float ra, rb;
                 upk(r, ra, rb);
-                const u64 ri = pk(rsqrtf(ra), rsqrtf(rb));
+                const u64 ri = pk(rsq(ra), rsq(rb));
                 const u64 f = mul2(mul2(mul2(B.y, ri), ri), ri);
                 accumulate<Mode, Pot>(acc, f, B.y, ri, dx, dy, dz);
+            }
+            if (Rec) {  // every body candidate is an interaction
+                for (int t = lane; t < nbody; t += 32)
+                    if (nrec + t < rec_cap) rec[nrec + t] = buf.bid[t];
+                nrec += nbody;
             }
             // ---- evaluate cells: one vote per cell, accept or push
             const int ncp = (ncell + 1) >> 1;
@@ -277,17 +312,23 @@ __global__ void __launch_bounds__(512, 2)
                 const bool okb = __all_sync(0xffffffffu, dpb <= rb);
                 float ma, mb;
                 upk(B.y, ma, mb);
-                const u64 ri = pk(rsqrtf(ra), rsqrtf(rb));
+                const u64 ri = pk(rsq(ra), rsq(rb));
                 const u64 mm = pk(oka ? ma : 0.f, okb ? mb : 0.f);
                 const u64 f = mul2(mul2(mul2(mm, ri), ri), ri);
                 accumulate<Mode, Pot>(acc, f, mm, ri, dx, dy, dz);
                 if (!oka) {
                     if (lane == 0) stack[top + nrej] = buf.cid[2 * q];
                     nrej++;
+                } else if (Rec && 2 * q < ncell) {
+                    if (lane == 0 && nrec < rec_cap) rec[nrec] = buf.cid[2 * q] & ((1 << kLevelShift) - 1);
+                    nrec++;
                 }
                 if (!okb) {
                     if (lane == 0) stack[top + nrej] = buf.cid[2 * q + 1];
                     nrej++;
+                } else if (Rec && 2 * q + 1 < ncell) {
+                    if (lane == 0 && nrec < rec_cap) rec[nrec] = buf.cid[2 * q + 1] & ((1 << kLevelShift) - 1);
+                    nrec++;
                 }
             }
             top += nrej;
@@ -313,6 +354,10 @@ __global__ void __launch_bounds__(512, 2)
             if (lane == 0) set_status(st, NBX_ERR_STACK, g);
             continue;
         }
+        if (Rec && lane == 0) {
+            rec_len[g] = nrec < rec_cap ? nrec : rec_cap;
+            if (nrec > rec_cap) set_status(st, NBX_ERR_CAPACITY, g);
+        }
         if (valid) {
             float fx, fy, fz;
             if (Mode == 0) {
@@ -336,7 +381,7 @@ __global__ void __launch_bounds__(512, 2)
                 float a0, a1;
                 upk(acc.p, a0, a1);
                 // remove the body's own term m * rsqrt(eps2), then phi = -sum
-                pot[ob] = -((a0 + a1) - me.w * rsqrtf(eps2));
+                pot[ob] = -((a0 + a1) - me.w * rsq(eps2));
             }
             if (nlist) nlist[ob] = len;
             if (nopen) nopen[ob] = opened;
@@ -350,28 +395,29 @@ __global__ void __launch_bounds__(512, 2)
     }
 }
 
-template <int CB, int Mode, bool Pot>
-int launch(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st) {
+template <int CB, int Mode, bool Pot, bool Rec = false>
+int launch(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st, int *rec_list = nullptr,
+           int *rec_len = nullptr, int rec_cap = 0) {
     const int cap = ctx->p.stack_depth;
     const size_t smem = (size_t)warps * (sizeof(WarpBuf<CB>) + (size_t)cap * sizeof(int));
     const int blocks_needed = ceil_div(ctx->ngroups, warps);
     int per_sm = 1;
-    NBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk2<CB, Mode, Pot>, warps * 32, smem));
+    NBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk2<CB, Mode, Pot, Rec>, warps * 32, smem));
     if (per_sm < 1) per_sm = 1;
     const int grid = blocks_needed < ctx->nsm * per_sm ? blocks_needed : ctx->nsm * per_sm;
     if (grid <= 0) return NBX_OK;
-    k_walk2<CB, Mode, Pot><<<grid, warps * 32, smem, st>>>(
+    k_walk2<CB, Mode, Pot, Rec><<<grid, warps * 32, smem, st>>>(
         ctx->d_node4, ctx->d_meta, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
         ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay, s->az,
-        pot, ctx->d_nlist, ctx->d_nopen, ctx->d_status);
+        pot, ctx->d_nlist, ctx->d_nopen, ctx->d_status, rec_list, rec_len, rec_cap);
     ++ctx->launches;
     NBX_CUDA(cudaGetLastError());
     return NBX_OK;
 }
 
-template <int CB, int Mode, bool Pot>
+template <int CB, int Mode, bool Pot, bool Rec = false>
 int set_attr(Ctx *ctx, int smem_max) {
-    NBX_CUDA(cudaFuncSetAttribute(k_walk2<CB, Mode, Pot>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
+    NBX_CUDA(cudaFuncSetAttribute(k_walk2<CB, Mode, Pot, Rec>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
     return NBX_OK;
 }
 
@@ -399,12 +445,19 @@ int walk2_init(Ctx *ctx) {
     rc |= set_attr<128, 1, false>(ctx, smem_optin);
     rc |= set_attr<128, 2, false>(ctx, smem_optin);
     rc |= set_attr<128, 0, true>(ctx, smem_optin);
+    rc |= set_attr<64, 0, false, true>(ctx, smem_optin);
     return rc;
 }
 
-// variant 0: 64-slot candidate buffers; variant 1: 128-slot buffers
+// Plain walk that also records every group's interaction list (node ids, in
+// evaluation order) into rec_list[g * rec_cap ...], its length into rec_len[g].
+int walk2_record(Ctx *ctx, const nbx_state *s, int *rec_list, int *rec_len, int rec_cap, cudaStream_t st) {
+    return launch<64, 0, false, true>(ctx, s, nullptr, ctx->walk_warps, st, rec_list, rec_len, rec_cap);
+}
+
+// variant 0: 64-slot candidate buffers; variant 1: 128-slot buffers (<= 8 warps)
 int walk2_forces(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st) {
-    if (ctx->walk_variant == 1) return forces_cb<128>(ctx, s, pot, warps, st);
+    if (ctx->walk_variant == 1) return forces_cb<128>(ctx, s, pot, warps > 8 ? 8 : warps, st);
     return forces_cb<64>(ctx, s, pot, warps, st);
 }
 
