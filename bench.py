@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--batched-systems", type=int, default=512)
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--fd-directions", type=int, default=16)
     return ap.parse_args()
 
 
@@ -212,6 +214,70 @@ def bench_batched(args, local):
             "walk_config": {"warps": tune["warps"], "variant": tune["variant"]}}
 
 
+def bench_adjoint(args, local):
+    """Differentiation form: Plummer N=65536, theta 0.5, eps 0.01, dt 1e-3, 100 steps,
+    L = sum |x(T) - x*|^2 with x* = x(T) + N(0, 0.01^2); checkpoints every 10 steps.
+    Reports adjoint/forward time, device memory, and the gradient error against
+    FP64 central finite differences (h = 1e-6) of the FP64 replay of the same
+    trajectory (recorded interaction lists) along random unit directions."""
+    import torch
+    from nns_gb300 import ic
+    from nns_gb300.adjoint import Adjoint, random_directions
+    from nns_gb300.barnes_hut import Context, State
+    n, T, C = 65536, 100, 10
+    b = ic.plummer(n)
+    ctx = Context(max_bodies=n, theta=0.5, eps=0.01, dt=1e-3, device=local)
+    ctx.set_systems([0, n])
+    s = State.from_bodies(b, device="cuda:%d" % local)
+    ctx.step(s, T)
+    ctx.sync()
+    rng = np.random.default_rng(20261203)
+    xt = np.stack([t.cpu().numpy() for t in (s.x, s.y, s.z)])
+    target = torch.as_tensor((xt + 0.01 * rng.standard_normal(xt.shape)).astype(np.float32),
+                             device="cuda:%d" % local)
+    free0 = torch.cuda.mem_get_info(local)[0]
+    adj = Adjoint(ctx, T, C, 8192, C)
+    times = []
+    for _ in range(2):  # the second run is timed warm
+        s = State.from_bodies(b, device="cuda:%d" % local)
+        loss = adj.forward(s, target)
+        gx, gv, gm = adj.backward(s)
+        st = adj.stats()
+        times.append((st["forward_ms"], st["backward_ms"]))
+    free1 = torch.cuda.mem_get_info(local)[0]
+    fwd_ms, bwd_ms = times[-1]
+    g = np.concatenate([gx.cpu().numpy(), gv.cpu().numpy(), gm.cpu().numpy()[None]]).astype(np.float64)
+    out = {"n": n, "steps": T, "checkpoint_every": C, "loss": loss,
+           "forward_ms_per_step": round(fwd_ms / T, 3), "adjoint_ms_per_step": round(bwd_ms / T, 3),
+           "adjoint_to_forward_ratio": round(bwd_ms / fwd_ms, 3),
+           "adjoint_device_bytes": st["bytes"],
+           "device_bytes_in_use_delta": int(free0 - free1)}
+    del adj
+    torch.cuda.empty_cache()
+    if args.fd_directions > 0:
+        ver = Adjoint(ctx, T, C, 8192, T)
+        s = State.from_bodies(b, device="cuda:%d" % local)
+        ver.forward(s, target)
+        ver.record(State.from_bodies(b, device="cuda:%d" % local))
+        base = np.stack([b.x, b.y, b.z, b.vx, b.vy, b.vz, b.m]).astype(np.float64)
+        dev = lambda a: torch.as_tensor(a, device="cuda:%d" % local)  # noqa: E731
+        loss64 = ver.replay_fp64(dev(base))
+        h = 1e-6
+        gn = float(np.linalg.norm(g))
+        errs = []
+        for u in random_directions(n, args.fd_directions):
+            fd = (ver.replay_fp64(dev(base + h * u)) - ver.replay_fp64(dev(base - h * u))) / (2 * h)
+            errs.append(abs(fd - float((g * u).sum())) / gn)
+        out["fd_check"] = {"directions": args.fd_directions, "h": h,
+                           "max_err_over_grad_norm": float(max(errs)),
+                           "median_err_over_grad_norm": float(np.median(errs)),
+                           "loss_fp64_replay": loss64,
+                           "loss_rel_diff_fp32_vs_fp64": abs(loss64 - loss) / loss}
+        del ver
+        torch.cuda.empty_cache()
+    return out
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
@@ -346,10 +412,15 @@ def main():
         steps_per_s = world * 1000.0 / ms_plain
 
     batched = None
+    del ctx, s
+    torch.cuda.empty_cache()
     if not args.no_batched:
-        del ctx, s
-        torch.cuda.empty_cache()
         batched = bench_batched(args, local)
+        torch.cuda.empty_cache()
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = bench_adjoint(args, local)
+        torch.cuda.empty_cache()
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -386,6 +457,7 @@ def main():
         "e2e": {"value": round(1000.0 / e2e_ms, 4), "unit": "steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "batched": batched,
+        "adjoint": adjoint,
         "autotune": tune,
         "gpu_launches": plain["launches"],
         "clocks": clocks,

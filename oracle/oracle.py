@@ -47,6 +47,8 @@ def lib():
                                       _i32p, _f64p, _f64p, _f64p]
         L.orc_direct_pot_fp64.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_double, C.c_int,
                                           _i32p, _f64p]
+        L.orc_direct_adjoint.argtypes = [C.c_int, _f64p, _f64p, _f64p, _f64p, C.c_double, C.c_double,
+                                         C.c_double, C.c_int, C.POINTER(C.c_double), _f64p, _f64p, _f64p]
     return _lib
 
 
@@ -203,6 +205,20 @@ def direct_potential_fp64(x, y, z, m, eps2, targets):
     lib().orc_direct_pot_fp64(len(x), _f32(x), _f32(y), _f32(z), _f32(m), C.c_double(eps2), len(t),
                               t, phi)
     return phi
+
+
+def direct_adjoint_fp64(x0, v0, m, target, eps2, dt, T, d=1.0):
+    """FP64 direct-sum trajectory loss and its gradients (x0, v0, target: (3,n); m: (n,))."""
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+    x0, v0, m, target = f(x0), f(v0), f(m), f(target)
+    n = m.size
+    gx = np.zeros((3, n)); gv = np.zeros((3, n)); gm = np.zeros(n)
+    loss = C.c_double()
+    rc = lib().orc_direct_adjoint(n, x0, v0, m, target, C.c_double(eps2), C.c_double(dt),
+                                  C.c_double(d), T, C.byref(loss), gx, gv, gm)
+    if rc:
+        raise OracleError(rc, "orc_direct_adjoint")
+    return loss.value, gx, gv, gm
 
 
 def ref_step(x, y, z, vx, vy, vz, m, dt, force_bounds=None, stack_size=4096):

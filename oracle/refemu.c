@@ -454,3 +454,104 @@ void orc_direct_pot_fp64(int n, const float *x, const float *y, const float *z, 
         phi[t] = s;
     }
 }
+
+/* ------------------------------------------------------------------ FP64 direct-sum adjoint
+ * Kick-drift with direct-sum forces (G = 1, Plummer softening) in FP64 and the
+ * exact gradient of L = sum_i |x_i(T) - x*_i|^2 w.r.t. x0, v0, m.  Arrays are
+ * [3][n] (x0, v0, target, gx, gv) and [n] (m, gm).  Used to check the GPU
+ * adjoint (which differs by the Barnes-Hut approximation). */
+static void direct_acc64(int n, const double *x, const double *m, double eps2, double *a)
+{
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int i = 0; i < n; i++) {
+        double sx = 0, sy = 0, sz = 0;
+        for (int j = 0; j < n; j++) {
+            double dx = x[j] - x[i], dy = x[n + j] - x[n + i], dz = x[2 * n + j] - x[2 * n + i];
+            double r2 = dx * dx + dy * dy + dz * dz + eps2;
+            double f = m[j] / (r2 * sqrt(r2));
+            sx += f * dx; sy += f * dy; sz += f * dz;
+        }
+        a[i] = sx; a[n + i] = sy; a[2 * n + i] = sz;
+    }
+}
+
+int orc_direct_adjoint(int n, const double *x0, const double *v0, const double *m,
+                       const double *target, double eps2, double dt, double d, int T,
+                       double *loss, double *gx, double *gv, double *gm)
+{
+    size_t sz = (size_t)3 * n;
+    double *X = (double *)malloc(sizeof(double) * sz * (size_t)(T + 1));
+    double *v = (double *)malloc(sizeof(double) * sz);
+    double *a = (double *)malloc(sizeof(double) * sz);
+    double *lx = gx, *lv = gv;
+    double *g = (double *)malloc(sizeof(double) * sz);
+    double *tx = (double *)malloc(sizeof(double) * sz);
+    if (!X || !v || !a || !g || !tx) return ORC_ERR_CAPACITY;
+    memcpy(X, x0, sizeof(double) * sz);
+    memcpy(v, v0, sizeof(double) * sz);
+    for (int k = 0; k < T; k++) {
+        double *xk = X + sz * k, *xn = X + sz * (k + 1);
+        direct_acc64(n, xk, m, eps2, a);
+        for (size_t q = 0; q < sz; q++) {
+            v[q] += dt * a[q];
+            xn[q] = xk[q] + d * dt * v[q];
+        }
+    }
+    double L = 0;
+    double *xT = X + sz * T;
+    for (size_t q = 0; q < sz; q++) {
+        double e = xT[q] - target[q];
+        L += e * e;
+        lx[q] = 2 * e;
+        lv[q] = 0;
+    }
+    for (int i = 0; i < n; i++) gm[i] = 0;
+    *loss = L;
+    for (int k = T - 1; k >= 0; k--) {
+        double *x = X + sz * k;
+        for (size_t q = 0; q < sz; q++) {
+            lv[q] += d * dt * lx[q];
+            g[q] = dt * lv[q];
+        }
+        /* target terms: lx_i -= sum_j m_j J(d_ij) g_i */
+#pragma omp parallel for schedule(dynamic, 16)
+        for (int i = 0; i < n; i++) {
+            double ox = 0, oy = 0, oz = 0;
+            double gxi = g[i], gyi = g[n + i], gzi = g[2 * n + i];
+            for (int j = 0; j < n; j++) {
+                if (j == i) continue;
+                double dx = x[j] - x[i], dy = x[n + j] - x[n + i], dz = x[2 * n + j] - x[2 * n + i];
+                double r2 = dx * dx + dy * dy + dz * dz + eps2, s = sqrt(r2);
+                double i3 = 1.0 / (r2 * s), i5 = i3 / r2;
+                double dg = dx * gxi + dy * gyi + dz * gzi;
+                ox += m[j] * (gxi * i3 - 3 * dx * dg * i5);
+                oy += m[j] * (gyi * i3 - 3 * dy * dg * i5);
+                oz += m[j] * (gzi * i3 - 3 * dz * dg * i5);
+            }
+            tx[i] = -ox; tx[n + i] = -oy; tx[2 * n + i] = -oz;
+        }
+        /* source terms: lx_j += sum_i m_j J(d_ij) g_i, lm_j += sum_i g_i . d_ij |d_ij|^-3 */
+#pragma omp parallel for schedule(dynamic, 16)
+        for (int j = 0; j < n; j++) {
+            double sx = 0, sy = 0, sz2 = 0, sm = 0;
+            for (int i = 0; i < n; i++) {
+                if (j == i) continue;
+                double dx = x[j] - x[i], dy = x[n + j] - x[n + i], dz = x[2 * n + j] - x[2 * n + i];
+                double r2 = dx * dx + dy * dy + dz * dz + eps2, s = sqrt(r2);
+                double i3 = 1.0 / (r2 * s), i5 = i3 / r2;
+                double gxi = g[i], gyi = g[n + i], gzi = g[2 * n + i];
+                double dg = dx * gxi + dy * gyi + dz * gzi;
+                sx += gxi * i3 - 3 * dx * dg * i5;
+                sy += gyi * i3 - 3 * dy * dg * i5;
+                sz2 += gzi * i3 - 3 * dz * dg * i5;
+                sm += dg * i3;
+            }
+            lx[j] += tx[j] + m[j] * sx;
+            lx[n + j] += tx[n + j] + m[j] * sy;
+            lx[2 * n + j] += tx[2 * n + j] + m[j] * sz2;
+            gm[j] += sm;
+        }
+    }
+    free(X); free(v); free(a); free(g); free(tx);
+    return ORC_OK;
+}

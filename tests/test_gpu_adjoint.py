@@ -89,3 +89,21 @@ def test_autograd_function(cuda):
     tol = 1e-6 * np.abs(g).max()
     assert np.allclose(x0.grad.cpu().numpy(), g[0:3], rtol=1e-5, atol=tol)
     assert np.allclose(m.grad.cpu().numpy(), g[6], rtol=1e-5, atol=tol)
+
+
+def test_adjoint_against_fp64_direct_sum_adjoint(cuda):
+    """4096-body run: the Barnes-Hut adjoint against the exact gradient of the
+    FP64 direct-sum trajectory (they differ by the tree approximation only)."""
+    from oracle import oracle as O
+    n, T = 4096, 20
+    b, ctx, adj, target = _setup(n, T, 10)
+    _, g = _grads(b, adj, target)
+    x0 = np.stack([b.x, b.y, b.z]).astype(np.float64)
+    v0 = np.stack([b.vx, b.vy, b.vz]).astype(np.float64)
+    _, gx, gv, gm = O.direct_adjoint_fp64(x0, v0, b.m, target.cpu().numpy(), 1e-4, 1e-3, T)
+    want = np.concatenate([gx, gv, gm[None]])
+    rel = np.linalg.norm(g - want) / np.linalg.norm(want)
+    assert rel < 2e-2, rel
+    for k, (a, w) in enumerate(((g[0:3], gx), (g[3:6], gv), (g[6], gm))):
+        r = np.linalg.norm(a - w) / np.linalg.norm(w)
+        assert r < 5e-2, (k, r)
