@@ -342,7 +342,10 @@ def main():
     rng = np.random.default_rng(12345)
     targets = np.sort(rng.choice(n, size=min(args.targets, n), replace=False))
     acc64 = ctx.direct_fp64(s, targets, float(np.float32(EPS) * np.float32(EPS))).cpu().numpy()
-    errs = {}
+    errs, errs32 = {}, {}
+    lists64 = None
+    stat = lambda rel: {"median": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99)),  # noqa: E731
+                        "max": float(rel.max())}
     for comp in (False, True):
         t_ref, e2 = ctx.constants()
         ctx.set_constants(t_ref, e2, comp)
@@ -350,10 +353,12 @@ def main():
         ctx.forces(s)
         ctx.sync()
         a = s.acc()[targets].astype(np.float64)
+        if lists64 is None:
+            lists64 = ctx.forces_fp64_lists(targets)
         rel = np.linalg.norm(a - acc64, axis=1) / np.linalg.norm(acc64, axis=1)
-        errs["compensated" if comp else "plain"] = {"median": float(np.median(rel)),
-                                                    "p99": float(np.quantile(rel, 0.99)),
-                                                    "max": float(rel.max())}
+        errs["compensated" if comp else "plain"] = stat(rel)
+        rel32 = np.linalg.norm(a - lists64, axis=1) / np.linalg.norm(lists64, axis=1)
+        errs32["compensated" if comp else "plain"] = stat(rel32)
     t_ref, e2 = ctx.constants()
     ctx.set_constants(t_ref, e2, False)
     diag0 = ctx.diagnostics(s)
@@ -442,6 +447,7 @@ def main():
                         "ms_per_step": round(ms_comp, 3),
                         "ratio_to_plain_time": round(ms_comp / ms_plain, 4)},
         "force_error_vs_fp64_direct": errs,
+        "fp32_error_vs_fp64_same_lists": errs32,
         "interactions_per_step": inter_per_step,
         "opened_cells_per_step": plain["opened"],
         "interactions_per_s": inter_per_step * steps_per_s,

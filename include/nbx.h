@@ -177,6 +177,13 @@ int nbx_export_walk_stats(nbx_ctx *ctx, int *nlist, int *nopen, void *stream);
  * [0,n): acc[3*t+k] += sum_j m_j d (|d|^2+eps2)^-3/2 in FP64. */
 int nbx_direct_fp64(nbx_ctx *ctx, const float *x, const float *y, const float *z, const float *m,
                     int n, const int *targets, int nt, double eps2, double *acc, void *stream);
+/* The last walk's interaction lists of the given walk groups (device array of
+ * the groups' first sorted positions, multiples of 32 from each system's start)
+ * re-evaluated in FP64: acc is a device double[3*nbodies] ([3][n], original
+ * order; rows outside the groups are untouched).  Against the FP32 walk this
+ * isolates the FP32 arithmetic error from the tree approximation. */
+int nbx_forces_fp64_lists(nbx_ctx *ctx, const int *group_starts, int ngroups, double *acc,
+                          void *stream);
 /* Per-body potential phi_i = -sum_j m_j / sqrt(|d|^2+eps2) over the walk's
  * interaction lists (self term removed), original index order; needs eps2 > 0. */
 int nbx_potential(nbx_ctx *ctx, const nbx_state *s, float *phi, void *stream);

@@ -75,6 +75,7 @@ SIGNATURES = {
     "nbx_export_walk_stats": (_I, [_P, _P, _P, _P]),
     "nbx_direct_fp64": (_I, [_P, _P, _P, _P, _P, _I, _P, _I, C.c_double, _P, _P]),
     "nbx_potential": (_I, [_P, C.POINTER(nbx_state), _P, _P]),
+    "nbx_forces_fp64_lists": (_I, [_P, _P, _I, _P, _P]),
     "nbx_diagnostics_fp64": (_I, [_P, C.POINTER(nbx_state), _I, _P, _P]),
     "nbx_adjoint_create": (_I, [_P, _I, _I, _I, _I, C.POINTER(_P)]),
     "nbx_adjoint_destroy": (_I, [_P]),

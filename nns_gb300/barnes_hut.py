@@ -173,6 +173,25 @@ class Context:
               "nbx_direct_fp64", self.h)
         return acc.view(-1, 3)
 
+    def forces_fp64_lists(self, targets, stream=None) -> np.ndarray:
+        """FP64 re-evaluation of the last walk's interaction lists for the walk
+        groups holding `targets` (original indices); returns (len(targets), 3)."""
+        _, perm = self.export_keys(stream)
+        n = len(perm)
+        pos = np.empty(n, np.int64)
+        pos[perm] = np.arange(n)
+        off = self.offsets
+        t = np.asarray(targets, np.int64)
+        sysid = np.searchsorted(off, t, side="right") - 1
+        start = off[sysid] + ((pos[t] - off[sysid]) // 32) * 32
+        groups = np.unique(start).astype(np.int32)
+        g = torch.as_tensor(groups, device=self.device)
+        acc = torch.zeros(3 * n, dtype=torch.float64, device=self.device)
+        check(lib().nbx_forces_fp64_lists(self.h, _ptr(g), len(groups), _ptr(acc),
+                                          _stream_ptr(stream)), "nbx_forces_fp64_lists", self.h)
+        a = acc.view(3, n)[:, torch.as_tensor(t, device=self.device)]
+        return a.t().cpu().numpy()
+
     def potential(self, s: "State", stream=None) -> np.ndarray:
         """Per-body potential over the last build's interaction lists (original order)."""
         n = int(self.offsets[-1])

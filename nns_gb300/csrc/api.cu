@@ -614,6 +614,11 @@ int nbx_direct_fp64(nbx_ctx *c, const float *x, const float *y, const float *z, 
     return nbx::direct_fp64(C(c), x, y, z, m, n, targets, nt, eps2, acc, S(stream));
 }
 
+int nbx_forces_fp64_lists(nbx_ctx *c, const int *group_starts, int ngroups, double *acc, void *stream) {
+    if (!c || (ngroups > 0 && (!group_starts || !acc)) || ngroups < 0) return NBX_ERR_ARG;
+    return nbx::walk_fp64_lists(C(c), group_starts, ngroups, acc, S(stream));
+}
+
 int nbx_potential(nbx_ctx *c, const nbx_state *s, float *phi, void *stream) {
     if (!c || !s || !phi) return NBX_ERR_ARG;
     if (!(C(c)->eps2 > 0.f)) return NBX_ERR_ARG;

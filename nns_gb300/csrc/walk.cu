@@ -26,11 +26,14 @@ struct Acc {
     float x = 0.f, y = 0.f, z = 0.f;
 };
 
-template <bool Comp>
+// Mode 0: plain FP32; 1: Kahan per term; 2: the same interaction list
+// evaluated in FP64 (MAC decisions still from the FP32 r) -- the reference
+// for the FP32 arithmetic error of the walk.
+template <int Mode>
 struct Accum;
 
 template <>
-struct Accum<false> {
+struct Accum<0> {
     float x = 0.f, y = 0.f, z = 0.f;
     __device__ __forceinline__ void add(float f, float dx, float dy, float dz) {
         x = fmaf(f, dx, x);
@@ -42,7 +45,7 @@ struct Accum<false> {
 
 // Kahan-compensated accumulation per component.
 template <>
-struct Accum<true> {
+struct Accum<1> {
     float x = 0.f, y = 0.f, z = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
     __device__ __forceinline__ static void kadd(float &s, float &c, float v) {
         const float yv = __fsub_rn(v, c);
@@ -58,14 +61,38 @@ struct Accum<true> {
     __device__ __forceinline__ void get(float &ox, float &oy, float &oz) const { ox = x; oy = y; oz = z; }
 };
 
-template <bool Comp>
+template <>
+struct Accum<2> {
+    double x = 0.0, y = 0.0, z = 0.0;
+    __device__ __forceinline__ void add64(float4 c, float4 me, float eps2) {
+        const double dx = (double)c.x - me.x, dy = (double)c.y - me.y, dz = (double)c.z - me.z;
+        const double r = dx * dx + dy * dy + dz * dz + (double)eps2;
+        const double f = (double)c.w / (r * sqrt(r));
+        x += f * dx;
+        y += f * dy;
+        z += f * dz;
+    }
+};
+
+template <int Mode, typename A>
+__device__ __forceinline__ void interact(A &acc, float cx, float cy, float cz, float cw, float dx, float dy,
+                                         float dz, float r, float4 me, float eps2) {
+    if constexpr (Mode == 2) {
+        acc.add64(make_float4(cx, cy, cz, cw), me, eps2);
+    } else {
+        const float ri = rsqrtf(r);
+        acc.add(cw * ri * ri * ri, dx, dy, dz);
+    }
+}
+
+template <int Mode>
 __global__ void __launch_bounds__(kWalkWarps * 32)
     k_walk(const float4 *__restrict__ node4, const int *__restrict__ meta, const float4 *__restrict__ body4,
            const int *__restrict__ val, const int *__restrict__ groups, int ngroups,
            const int *__restrict__ body_sys, const int *__restrict__ sys_off, const float *__restrict__ depth0,
            const int *__restrict__ root_first, const int *__restrict__ root_nch, float eps2, int stack_cap,
            float *__restrict__ ax, float *__restrict__ ay, float *__restrict__ az, int *__restrict__ nlist,
-           int *__restrict__ nopen, DevStatus *st) {
+           int *__restrict__ nopen, DevStatus *st, double *__restrict__ a64, int n64) {
     extern __shared__ int smem_stack[];
     if (st->code != 0) return;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -79,7 +106,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32)
         const bool valid = p < end;
         const float4 me = body4[valid ? p : p0];
         const float d0 = depth0[s];
-        Accum<Comp> acc;
+        Accum<Mode> acc;
         int top = 0, len = 0, opened = 0;
         bool overflow = false;
 
@@ -101,8 +128,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32)
                 if (cmj < 0) {
                     const float dx = cx - me.x, dy = cy - me.y, dz = cz - me.z;
                     const float r = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-                    const float ri = rsqrtf(r);
-                    acc.add(cw * ri * ri * ri, dx, dy, dz);
+                    interact<Mode>(acc, cx, cy, cz, cw, dx, dy, dz, r, me, eps2);
                     len++;
                 } else {
                     if (lane == 0) stack[top] = (first + j) | (1 << kLevelShift);
@@ -139,8 +165,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32)
                 const float r = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
                 const bool accept = (cmj < 0) || __all_sync(0xffffffffu, !valid || dp <= r);
                 if (accept) {
-                    const float ri = rsqrtf(r);
-                    acc.add(cw * ri * ri * ri, dx, dy, dz);
+                    interact<Mode>(acc, cx, cy, cz, cw, dx, dy, dz, r, me, eps2);
                     len++;
                 } else {
                     if (top >= stack_cap) {
@@ -161,18 +186,24 @@ __global__ void __launch_bounds__(kWalkWarps * 32)
         }
         if (valid) {
             const int ob = val[p];
-            float fx, fy, fz;
-            acc.get(fx, fy, fz);
-            ax[ob] = fx;
-            ay[ob] = fy;
-            az[ob] = fz;
+            if constexpr (Mode == 2) {
+                a64[ob] = acc.x;
+                a64[(size_t)n64 + ob] = acc.y;
+                a64[2 * (size_t)n64 + ob] = acc.z;
+            } else {
+                float fx, fy, fz;
+                acc.get(fx, fy, fz);
+                ax[ob] = fx;
+                ay[ob] = fy;
+                az[ob] = fz;
+            }
             if (nlist) nlist[ob] = len;
             if (nopen) nopen[ob] = opened;
         }
         tot_len += (unsigned long long)len * (unsigned long long)(end - p0);
         tot_open += (unsigned long long)opened;
     }
-    if (lane == 0 && (tot_len | tot_open)) {
+    if (Mode != 2 && lane == 0 && (tot_len | tot_open)) {
         atomicAdd(&st->interactions, tot_len);
         atomicAdd(&st->opened, tot_open);
     }
@@ -186,8 +217,9 @@ int walk2_forces(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream
 int walk_init(Ctx *ctx) {
     const int smem = kWalkWarps * ctx->p.stack_depth * (int)sizeof(int);
     NBX_CUDA(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->p.device));
-    NBX_CUDA(cudaFuncSetAttribute(k_walk<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    NBX_CUDA(cudaFuncSetAttribute(k_walk<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    NBX_CUDA(cudaFuncSetAttribute(k_walk<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    NBX_CUDA(cudaFuncSetAttribute(k_walk<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    NBX_CUDA(cudaFuncSetAttribute(k_walk<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     return walk2_init(ctx);
 }
 
@@ -205,18 +237,37 @@ int walk_forces(Ctx *ctx, const nbx_state *s, cudaStream_t st) {
     const int grid = blocks_needed < ctx->nsm * 8 ? blocks_needed : ctx->nsm * 8;
     if (grid <= 0) return NBX_OK;
     if (ctx->compensated) {
-        k_walk<true><<<grid, kWalkWarps * 32, smem, st>>>(
+        k_walk<1><<<grid, kWalkWarps * 32, smem, st>>>(
             ctx->d_node4, ctx->d_meta, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
             ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay,
-            s->az, ctx->d_nlist, ctx->d_nopen, ctx->d_status);
+            s->az, ctx->d_nlist, ctx->d_nopen, ctx->d_status, nullptr, 0);
         ++ctx->launches;
     } else {
-        k_walk<false><<<grid, kWalkWarps * 32, smem, st>>>(
+        k_walk<0><<<grid, kWalkWarps * 32, smem, st>>>(
             ctx->d_node4, ctx->d_meta, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
             ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay,
-            s->az, ctx->d_nlist, ctx->d_nopen, ctx->d_status);
+            s->az, ctx->d_nlist, ctx->d_nopen, ctx->d_status, nullptr, 0);
         ++ctx->launches;
     }
+    NBX_CUDA(cudaGetLastError());
+    return NBX_OK;
+}
+
+// The last build's interaction lists of the given walk groups (first sorted
+// positions, device array) evaluated in FP64 into a64 [3][nbodies] (original
+// order; rows of bodies outside those groups are untouched).
+int walk_fp64_lists(Ctx *ctx, const int *group_starts, int ngroups, double *a64, cudaStream_t st) {
+    if (!ctx->built) return NBX_ERR_STATE;
+    if (ngroups <= 0) return NBX_OK;
+    const int cap = ctx->p.stack_depth;
+    const size_t smem = (size_t)kWalkWarps * cap * sizeof(int);
+    const int blocks_needed = ceil_div(ngroups, kWalkWarps);
+    const int grid = blocks_needed < ctx->nsm * 8 ? blocks_needed : ctx->nsm * 8;
+    k_walk<2><<<grid, kWalkWarps * 32, smem, st>>>(
+        ctx->d_node4, ctx->d_meta, ctx->d_body4, ctx->d_val, group_starts, ngroups, ctx->d_body_sys, ctx->d_sys_off,
+        ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, nullptr, nullptr, nullptr, nullptr,
+        nullptr, ctx->d_status, a64, (int)ctx->nbodies);
+    ++ctx->launches;
     NBX_CUDA(cudaGetLastError());
     return NBX_OK;
 }

@@ -412,3 +412,24 @@ def test_autotune_picks_a_valid_config(cuda, tmp_path, monkeypatch):
     ot = O.build(b.x, b.y, b.z, b.m)
     f = O.forces(b.x, b.y, b.z, b.m, ot, 0.25, 1e-4)
     assert _rel(s.acc(), f.a).max() <= MAX_TOL
+
+
+def test_fp64_list_evaluation_matches_oracle(cuda):
+    """FP64 re-evaluation of the walk's own lists equals the oracle's FP64
+    evaluation of the same lists; the FP32 walk is within 1e-5 of it."""
+    b = ic.binary_disk(8192)
+    n = len(b.x)
+    ctx = _ctx(n, theta=0.5, eps=0.005)
+    ctx.set_systems([0, n])
+    s = _state(b)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    tg = np.arange(0, n, 13)
+    a64 = ctx.forces_fp64_lists(tg)
+    ot = O.build(b.x, b.y, b.z, b.m)
+    t, e2 = ctx.constants()
+    f = O.forces(b.x, b.y, b.z, b.m, ot, t, e2)
+    assert np.allclose(a64, f.a64[tg], rtol=1e-10, atol=1e-14 * np.abs(f.a64).max())
+    rel = _rel(s.acc()[tg], a64)
+    assert np.median(rel) < 1e-6 and rel.max() < 1e-5
