@@ -31,6 +31,12 @@ THETA, EPS, DT = 0.5, 0.005, 5e-4
 FLOP_PER_INTERACTION = 20
 
 
+def workload_config(n, world):
+    return {"workload": "binary_disk_2^24 precision form", "n": n, "theta": THETA, "eps": EPS,
+            "dt": DT, "group": 32, "l2": "inputs larger than L2 (no flush)",
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -126,11 +132,10 @@ def run_reference(args, rank):
     if res is None:
         return {"impl": "reference", "unavailable": "reference CPU code was not staged/built on this host"}
     line = {"metric": METRIC, "impl": "reference", "value": res["steps_per_s"], "unit": "steps/s",
-            "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+            "n_gpus": int(os.environ.get("WORLD_SIZE", args.gpus)), "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 / res["steps_per_s"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (nns_gb300.ic binary_disk)",
-            "config": {"workload": "binary_disk_2^24", "n": args.n, "theta": THETA, "eps": EPS,
-                       "dt": DT},
+            "config": workload_config(args.n, int(os.environ.get("WORLD_SIZE", 1))),
             "cpu_baseline": {"value": res["steps_per_s"], "unit": "steps/s", "cores": res["cores"],
                              "kind": "reference", "sample": res["sample"]},
             "e2e": {"value": res["steps_per_s"], "unit": "steps/s", "h2d_bytes_per_step": 0,
@@ -410,10 +415,8 @@ def main():
     steps_per_s = 1000.0 / ms_plain
 
     if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms_plain], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_plain = float(t.item())
+        from nns_gb300.dist import max_over_ranks
+        ms_plain = max_over_ranks(ms_plain, device="cuda")
         steps_per_s = world * 1000.0 / ms_plain
 
     batched = None
@@ -440,9 +443,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_plain, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (nns_gb300.ic binary_disk, seed 20261203)",
-        "config": {"workload": "binary_disk_2^24 precision form", "n": n, "theta": THETA,
-                   "eps": EPS, "dt": DT, "group": 32, "l2": "inputs larger than L2 (no flush)",
-                   "parallelism": "replicas" if world > 1 else "single"},
+        "config": workload_config(n, world),
         "compensated": {"value": round(1000.0 / ms_comp, 4), "unit": "steps/s",
                         "ms_per_step": round(ms_comp, 3),
                         "ratio_to_plain_time": round(ms_comp / ms_plain, 4)},
