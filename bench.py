@@ -340,6 +340,7 @@ def main():
         integ = sum(e[2].elapsed_time(e[3]) for e in ev)
         return dict(ms=total, build_ms=build, walk_ms=walk, integ_ms=integ,
                     interactions=info["interactions"], opened=info["opened"],
+                    rounds=info["rounds"], candidates=info["candidates"],
                     launches=info["launches"] - launches0,
                     ncells=info["ncells"], max_level=info["max_level"])
 
@@ -451,6 +452,8 @@ def main():
         "fp32_error_vs_fp64_same_lists": errs32,
         "interactions_per_step": inter_per_step,
         "opened_cells_per_step": plain["opened"],
+        "walk_rounds_per_step": plain["rounds"],
+        "walk_candidates_per_step": plain["candidates"],
         "interactions_per_s": inter_per_step * steps_per_s,
         "phase_ms": {"build": round(plain["build_ms"] / args.steps, 3), "walk": round(walk_ms, 3),
                      "integrate": round(plain["integ_ms"] / args.steps, 3)},

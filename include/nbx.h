@@ -69,6 +69,9 @@ typedef struct nbx_params {
     int grid_size;
     int walk_variant;  /* 0 production walk, 64-slot candidate buffers; 1 the same with
                           128-slot buffers; 2 one-cell-at-a-time walk (comparison) */
+    int key_order;     /* 0: the reference's body order (Lebesgue keys; bit-exact parity);
+                          1: Hilbert keys -- same cells, siblings reordered, so walk groups
+                          are compact but the interaction lists differ from the reference */
 } nbx_params;
 
 /* SoA device state of all systems; systems are contiguous ranges. */
@@ -90,6 +93,8 @@ typedef struct nbx_tree_info {
     int32_t refined_runs;  /* runs of equal 21-level keys refined past level 21 */
     int32_t status;        /* sticky device error status */
     int64_t launches;      /* kernels launched by this context so far */
+    int64_t rounds;        /* walk rounds (expand + evaluate) over all groups, last walk */
+    int64_t candidates;    /* candidates evaluated by those rounds */
 } nbx_tree_info;
 
 /* ---- context -------------------------------------------------------- */

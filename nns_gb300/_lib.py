@@ -26,7 +26,7 @@ class nbx_params(C.Structure):
                 ("group", C.c_int), ("stack_depth", C.c_int), ("compensated", C.c_int),
                 ("leaf_size", C.c_int), ("radix_bits", C.c_int), ("walk_warps", C.c_int),
                 ("device", C.c_int), ("block_size", C.c_int), ("grid_size", C.c_int),
-                ("walk_variant", C.c_int)]
+                ("walk_variant", C.c_int), ("key_order", C.c_int)]
 
 
 class nbx_state(C.Structure):
@@ -37,7 +37,7 @@ class nbx_tree_info(C.Structure):
     _fields_ = [("nbodies", C.c_int64), ("ncells", C.c_int64), ("nnodes", C.c_int64),
                 ("max_level", C.c_int32), ("nsystems", C.c_int32), ("interactions", C.c_int64),
                 ("opened", C.c_int64), ("refined_runs", C.c_int32), ("status", C.c_int32),
-                ("launches", C.c_int64)]
+                ("launches", C.c_int64), ("rounds", C.c_int64), ("candidates", C.c_int64)]
 
 
 _P = C.c_void_p

@@ -177,6 +177,11 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     ctx->eps2 = p->eps2 > 0.f ? p->eps2 : p->eps * p->eps;
     ctx->compensated = p->compensated;
     ctx->walk_variant = p->walk_variant;
+    ctx->key_order = p->key_order;
+    if (p->key_order < 0 || p->key_order > 1) {
+        delete ctx;
+        return NBX_ERR_ARG;
+    }
     if (p->walk_warps == 4 || p->walk_warps == 8 || p->walk_warps == 16) ctx->walk_warps = p->walk_warps;
     if (!(ctx->theta_ref > 0.f) || p->compensated < 0 || p->compensated > 2) {
         delete ctx;
@@ -568,6 +573,8 @@ int nbx_get_tree_info(nbx_ctx *c, void *stream, nbx_tree_info *out) {
     out->refined_runs = ctx->h_status->refined_runs;
     out->status = ctx->h_status->code;
     out->launches = ctx->launches;
+    out->rounds = (int64_t)ctx->h_status->rounds;
+    out->candidates = (int64_t)ctx->h_status->candidates;
     return NBX_OK;
 }
 

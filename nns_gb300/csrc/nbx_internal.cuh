@@ -27,6 +27,8 @@ struct DevStatus {
     int max_level;
     unsigned long long interactions;
     unsigned long long opened;
+    unsigned long long rounds;      // walk expand/evaluate rounds (production walk)
+    unsigned long long candidates;  // candidates evaluated by the production walk
 };
 
 struct Ctx {
@@ -35,6 +37,7 @@ struct Ctx {
     int compensated;       // 0 plain, 1 split-compensated, 2 Kahan per term
     int walk_variant = 0;  // 0 production walk (walk2.cu), 2 one-cell-at-a-time walk (walk.cu)
     int walk_warps = 8;    // warps per block of the production walk
+    int key_order = 0;     // 0 the reference's (Lebesgue) order, 1 Hilbert
     std::string last_error;
 
     // capacity

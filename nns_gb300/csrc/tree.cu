@@ -42,6 +42,8 @@ __global__ void k_step_reset(unsigned *bbox_u, int nsys, DevStatus *st) {
         st->max_level = 0;
         st->interactions = 0ull;
         st->opened = 0ull;
+        st->rounds = 0ull;
+        st->candidates = 0ull;
     }
 }
 
@@ -115,13 +117,37 @@ __global__ void k_bbox_from_ptrs(const float *mnx, const float *mxx, const float
     st->max_level = 0;
 }
 
-__device__ __forceinline__ unsigned long long make_key(float px, float py, float pz, const float *bb) {
+// Optional Hilbert order (key_order = 1).  The 12-state Lebesgue-to-Hilbert
+// tables of the reference's domain-decomposition code
+// (MolecularDynamics/BarnesHutParallel/SpaceFillingCurves/src/Tree.cpp:70-104),
+// indexed by the Lebesgue child number b = [x>=mid] + 2[y>=mid] + 4[z>=mid]
+// = 7 - c.  Digits map one-to-one per level, so two keys share a Hilbert prefix
+// exactly when they share the Lebesgue one: the same cells, siblings reordered.
+__constant__ unsigned char kHilbertDigit[12][8] = {
+    {0, 7, 3, 4, 1, 6, 2, 5}, {4, 3, 7, 0, 5, 2, 6, 1}, {6, 1, 5, 2, 7, 0, 4, 3}, {2, 5, 1, 6, 3, 4, 0, 7},
+    {0, 1, 7, 6, 3, 2, 4, 5}, {6, 7, 1, 0, 5, 4, 2, 3}, {2, 3, 5, 4, 1, 0, 6, 7}, {4, 5, 3, 2, 7, 6, 0, 1},
+    {0, 3, 1, 2, 7, 4, 6, 5}, {2, 1, 3, 0, 5, 6, 4, 7}, {4, 7, 5, 6, 3, 0, 2, 1}, {6, 5, 7, 4, 1, 2, 0, 3}};
+__constant__ unsigned char kHilbertState[12][8] = {
+    {8, 10, 3, 3, 4, 5, 4, 5}, {2, 2, 11, 9, 4, 5, 4, 5}, {7, 6, 7, 6, 8, 10, 1, 1}, {7, 6, 7, 6, 0, 0, 11, 9},
+    {0, 8, 1, 11, 6, 8, 6, 11}, {10, 0, 9, 1, 10, 7, 9, 7}, {10, 4, 9, 4, 10, 2, 9, 3}, {5, 8, 5, 11, 2, 8, 3, 11},
+    {4, 9, 0, 0, 7, 9, 2, 2}, {1, 1, 8, 5, 3, 3, 8, 6}, {11, 5, 0, 0, 11, 6, 2, 2}, {1, 1, 4, 10, 3, 3, 7, 10}};
+
+__device__ __forceinline__ int to_digit(int c, int &state, int order) {
+    if (order == 0) return c;
+    const int b = 7 - c;
+    const int h = kHilbertDigit[state][b];
+    state = kHilbertState[state][b];
+    return h;
+}
+
+__device__ __forceinline__ unsigned long long make_key(float px, float py, float pz, const float *bb, int order) {
     float mnx = bb[0], mxx = bb[1], mny = bb[2], mxy = bb[3], mnz = bb[4], mxz = bb[5];
     unsigned long long key = 0ull;
+    int state = 0;
 #pragma unroll 3
     for (int l = 1; l <= 21; l++) {
         int c = split_axis(px, mnx, mxx) + 2 * split_axis(py, mny, mxy) + 4 * split_axis(pz, mnz, mxz);
-        key = (key << 3) | (unsigned long long)c;
+        key = (key << 3) | (unsigned long long)to_digit(c, state, order);
     }
     return key;
 }
@@ -130,7 +156,7 @@ __global__ void __launch_bounds__(kBlock) k_keys(const float *__restrict__ x, co
                                                   const float *__restrict__ z, const int *__restrict__ body_sys,
                                                   const float *__restrict__ bbox, int n,
                                                   unsigned long long *__restrict__ key, int *__restrict__ val,
-                                                  DevStatus *st) {
+                                                  DevStatus *st, int order) {
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         const float px = x[i], py = y[i], pz = z[i];
         if (!isfinite(px) || !isfinite(py) || !isfinite(pz)) set_status(st, NBX_ERR_NONFINITE, i);
@@ -138,7 +164,7 @@ __global__ void __launch_bounds__(kBlock) k_keys(const float *__restrict__ x, co
         float bb[6];
 #pragma unroll
         for (int k = 0; k < 6; k++) bb[k] = bbox[6 * s + k];
-        key[i] = make_key(px, py, pz, bb);
+        key[i] = make_key(px, py, pz, bb, order);
         val[i] = i;
     }
 }
@@ -149,7 +175,7 @@ __global__ void k_refine(const float *__restrict__ x, const float *__restrict__ 
                          const int *__restrict__ sys_off, const float *__restrict__ bbox, int n,
                          const unsigned long long *__restrict__ key,
                          unsigned long long *__restrict__ key_lo, int *__restrict__ val,
-                         DevStatus *st) {
+                         DevStatus *st, int order) {
     for (int p = grid_stride_start(); p < n; p += grid_stride()) {
         const int s = body_sys[p];
         const int beg = sys_off[s], end = sys_off[s + 1];
@@ -170,9 +196,11 @@ __global__ void k_refine(const float *__restrict__ x, const float *__restrict__ 
             float mnx = bb[0], mxx = bb[1], mny = bb[2], mxy = bb[3], mnz = bb[4], mxz = bb[5];
             unsigned long long lo = 0ull;
             const float px = x[b], py = y[b], pz = z[b];
+            int state = 0;
             for (int l = 1; l <= 42; l++) {
                 int c = split_axis(px, mnx, mxx) + 2 * split_axis(py, mny, mxy) + 4 * split_axis(pz, mnz, mxz);
-                if (l > 21) lo = (lo << 3) | (unsigned long long)c;
+                const int d = to_digit(c, state, order);
+                if (l > 21) lo = (lo << 3) | (unsigned long long)d;
             }
             key_lo[q] = lo;
         }
@@ -431,12 +459,12 @@ int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox
         ++ctx->launches;
     }
     k_keys<<<gb, kBlock, 0, st>>>(s->x, s->y, s->z, ctx->d_body_sys, ctx->d_bbox, n, ctx->d_key,
-                                  ctx->d_val, ctx->d_status);
+                                  ctx->d_val, ctx->d_status, ctx->key_order);
     ++ctx->launches;
     int rc = radix_sort_bodies(ctx, st);
     if (rc) return rc;
     k_refine<<<gb, kBlock, 0, st>>>(s->x, s->y, s->z, ctx->d_body_sys, ctx->d_sys_off, ctx->d_bbox, n,
-                                    ctx->d_key, ctx->d_key_lo, ctx->d_val, ctx->d_status);
+                                    ctx->d_key, ctx->d_key_lo, ctx->d_val, ctx->d_status, ctx->key_order);
     ++ctx->launches;
     k_delta<<<gb, kBlock, 0, st>>>(s->x, s->y, s->z, s->m, ctx->d_body_sys, ctx->d_sys_off, n, ctx->d_key,
                                    ctx->d_key_lo, ctx->d_val, ctx->d_body4, ctx->d_delta, ctx->d_ecount,
@@ -557,7 +585,7 @@ __global__ void k_perm_export(const int *val, int beg, int n, int *perm) {
 int export_tree_impl(Ctx *ctx, int sys, int *perm, int *root_child, int *cell_child, int *cell_start,
                      int *cell_count, int *cell_level, float *cx, float *cy, float *cz, float *cm,
                      int cap_cells, int64_t *ncells, cudaStream_t st, int sum_mode) {
-    if (!ctx->built) return NBX_ERR_STATE;
+    if (!ctx->built || ctx->key_order != 0) return NBX_ERR_STATE;
     if (sys < 0 || sys >= ctx->nsys) return NBX_ERR_ARG;
     int off[2];
     NBX_CUDA(cudaMemcpyAsync(off, ctx->d_sys_off + sys, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
     int *stack = reinterpret_cast<int *>(smem_raw + sizeof(WarpBuf<CB>) * warps) + w * stack_cap;
     const unsigned lt = (1u << lane) - 1u;
     const u64 eps2x2 = pk(eps2, eps2);
-    unsigned long long tot_len = 0ull, tot_open = 0ull;
+    unsigned long long tot_len = 0ull, tot_open = 0ull, tot_rounds = 0ull, tot_cand = 0ull;
 
     for (int g = blockIdx.x * warps + w; g < ngroups; g += gridDim.x * warps) {
         const int p0 = groups[g];
@@ -332,6 +332,8 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 }
             }
             top += nrej;
+            tot_rounds += 1ull;
+            tot_cand += (unsigned long long)(nbody + ncell);
             len += nbody + ncell - nrej;
             opened += nrej;
             nb = 0;
@@ -392,6 +394,8 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
     if (lane == 0 && (tot_len | tot_open)) {
         atomicAdd(&st->interactions, tot_len);
         atomicAdd(&st->opened, tot_open);
+        atomicAdd(&st->rounds, tot_rounds);
+        atomicAdd(&st->candidates, tot_cand);
     }
 }
 
