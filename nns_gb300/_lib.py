@@ -9,7 +9,7 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libnbx.so")
+LIB_PATH = os.environ.get("NBX_LIB_PATH", os.path.join(HERE, "libnbx.so"))
 
 NBX_OK = 0
 STATUS_NAMES = {

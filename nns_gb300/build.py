@@ -14,8 +14,11 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "_build")
-LIB = os.path.join(HERE, "libnbx.so")
+BUILD = os.environ.get("NBX_BUILD_DIR", os.path.join(HERE, "_build"))
+LIB = os.environ.get("NBX_LIB_PATH", os.path.join(HERE, "libnbx.so"))
+# extra nvcc flags (e.g. -D tuning macros of csrc/walk2.cu) and a separate
+# object directory, for building variants side by side
+EXTRA = os.environ.get("NBX_NVCC_EXTRA", "").split()
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-Xptxas", "-v"]
@@ -39,7 +42,7 @@ def _headers():
 
 def _compile(src: str) -> tuple[str, str]:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    cmd = [nvcc()] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj]
+    cmd = [nvcc()] + ARCH + NVCC_FLAGS + EXTRA + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed on %s:\n%s\n%s" % (src, r.stdout, r.stderr))

@@ -33,6 +33,17 @@ namespace {
 // level below the popped cell, i.e. by less than 7 * 42.
 constexpr int kDfsReserve = 7 * 42 + 8;
 
+// Build-time tuning knobs of the evaluation loops (defaults are the measured best).
+#ifndef NBX_BODY_UNROLL
+#define NBX_BODY_UNROLL 4
+#endif
+#ifndef NBX_CELL_UNROLL
+#define NBX_CELL_UNROLL 2
+#endif
+#ifndef NBX_WALK64_MINB
+#define NBX_WALK64_MINB 2
+#endif
+
 typedef unsigned long long u64;
 
 __device__ __forceinline__ u64 pk(float a, float b) {
@@ -135,7 +146,7 @@ __device__ __forceinline__ void accumulate(Sums &a, u64 f, u64 mm, u64 ri, u64 d
 template <int CB>
 struct WalkBounds {
     static constexpr int kThreads = CB == 64 ? 512 : 256;
-    static constexpr int kMinBlocks = CB == 64 ? 2 : 3;
+    static constexpr int kMinBlocks = CB == 64 ? NBX_WALK64_MINB : 3;
 };
 
 template <int CB, int Mode, bool Pot, bool Rec>
@@ -270,7 +281,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
 
             // ---- evaluate bodies: no MAC
             const int nbp = (nbody + 1) >> 1;
-#pragma unroll 4
+#pragma unroll NBX_BODY_UNROLL
             for (int q = 0; q < nbp; q++) {
                 const ulonglong2 A = buf.ba[q];
                 const ulonglong2 B = buf.bb[q];
@@ -294,7 +305,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             // ---- evaluate cells: one vote per cell, accept or push
             const int ncp = (ncell + 1) >> 1;
             int nrej = 0;
-#pragma unroll 2
+#pragma unroll NBX_CELL_UNROLL
             for (int q = 0; q < ncp; q++) {
                 const ulonglong2 A = buf.ca[q];
                 const ulonglong2 B = buf.cb[q];
@@ -308,8 +319,13 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 r = fma2(dz, dz, r);
                 float ra, rb;
                 upk(r, ra, rb);
+#ifdef NBX_REDUX_VOTE
+                const unsigned vab = __reduce_and_sync(0xffffffffu, (dpa <= ra ? 1u : 0u) | (dpb <= rb ? 2u : 0u));
+                const bool oka = vab & 1u, okb = (vab >> 1) & 1u;
+#else
                 const bool oka = __all_sync(0xffffffffu, dpa <= ra);
                 const bool okb = __all_sync(0xffffffffu, dpb <= rb);
+#endif
                 float ma, mb;
                 upk(B.y, ma, mb);
                 const u64 ri = pk(rsq(ra), rsq(rb));
