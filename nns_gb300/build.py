@@ -52,6 +52,8 @@ def _compile(src: str) -> tuple[str, str]:
 def up_to_date() -> bool:
     if not os.path.exists(LIB):
         return False
+    if LIB == os.path.join(HERE, "libnbx.so") and not os.path.exists(os.path.join(HERE, "nbx_runner")):
+        return False
     t = os.path.getmtime(LIB)
     return all(os.path.getmtime(f) <= t for f in _sources() + _headers())
 
@@ -77,7 +79,26 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    if LIB == os.path.join(HERE, "libnbx.so"):
+        build_runner()
     return LIB
+
+
+RUNNER = os.path.join(HERE, "nbx_runner")
+
+
+def build_runner() -> str:
+    """The command-line driver (driver/nbx_runner.cpp) linked against libnbx.so."""
+    src = os.path.join(HERE, "driver", "nbx_runner.cpp")
+    inc = os.path.join(HERE, "..", "include")
+    cuda = os.path.dirname(os.path.dirname(nvcc()))
+    cmd = ["g++", "-O2", "-std=c++17", "-I", inc, "-I", os.path.join(cuda, "include"), src, "-o", RUNNER,
+           "-L", HERE, "-lnbx", "-Wl,-rpath,$ORIGIN", "-L", os.path.join(cuda, "lib64"), "-lcudart",
+           "-Wl,-rpath," + os.path.join(cuda, "lib64")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nbx_runner build failed:\n%s" % r.stderr[-3000:])
+    return RUNNER
 
 
 if __name__ == "__main__":

@@ -43,6 +43,9 @@ constexpr int kDfsReserve = 7 * 42 + 8;
 #ifndef NBX_WALK64_MINB
 #define NBX_WALK64_MINB 2
 #endif
+// (#pragma arguments are not macro-expanded: the unroll factors go through constants)
+constexpr int kBodyUnroll = NBX_BODY_UNROLL;
+constexpr int kCellUnroll = NBX_CELL_UNROLL;
 
 typedef unsigned long long u64;
 
@@ -281,7 +284,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
 
             // ---- evaluate bodies: no MAC
             const int nbp = (nbody + 1) >> 1;
-#pragma unroll NBX_BODY_UNROLL
+#pragma unroll (kBodyUnroll)
             for (int q = 0; q < nbp; q++) {
                 const ulonglong2 A = buf.ba[q];
                 const ulonglong2 B = buf.bb[q];
@@ -305,7 +308,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             // ---- evaluate cells: one vote per cell, accept or push
             const int ncp = (ncell + 1) >> 1;
             int nrej = 0;
-#pragma unroll NBX_CELL_UNROLL
+#pragma unroll (kCellUnroll)
             for (int q = 0; q < ncp; q++) {
                 const ulonglong2 A = buf.ca[q];
                 const ulonglong2 B = buf.cb[q];

@@ -1,0 +1,206 @@
+// nbx_runner -- command-line driver with the reference driver's flags and
+// report (3D/CUDA/CUDA_NBody/src/main.cu:19-190), running the reference's
+// BarnesHut::update flow through libnbx (include/nbx/barnes_hut.hpp).
+//
+//   -i, --iterations N      number of iterations (100)
+//   -n, --particles N       number of particles (524288)
+//   -b, --blocksize N       block size hint (256)
+//   -g, --gridsize N        grid size hint (1024)
+//   -R, --renderinterval N  render interval (10); -r/--render is accepted, no frames are written
+//   -v                      verbosity (repeat)
+//   --model ref-disk|disk|plummer   initial conditions (ref-disk: the recipe of
+//                           BarnesHut::diskModel, BarnesHut.cu:356-415)
+//   --theta-ref X --eps2 X  MAC constant and squared softening (Kernels.cu:17-18 defaults)
+//   --seed N
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "nbx/barnes_hut.hpp"
+
+namespace {
+
+// Counter-based SplitMix64 stream, draw k of body i under seed s (the same
+// generator as nns_gb300/ic.py).
+uint64_t mix(uint64_t z) {
+    z ^= z >> 30;
+    z *= 0xBF58476D1CE4E5B9ull;
+    z ^= z >> 27;
+    z *= 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+double uniform(uint64_t seed, uint64_t i, uint64_t draw) {
+    const uint64_t base = mix(seed * 0x9E3779B97F4A7C15ull + draw * 0xD1B54A32D192ED03ull);
+    return (double)(mix(base + (i + 1) * 0x9E3779B97F4A7C15ull) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+struct Bodies {
+    std::vector<float> x, y, z, vx, vy, vz, m;
+    explicit Bodies(int n) : x(n), y(n), z(n), vx(n), vy(n), vz(n), m(n) {}
+};
+
+// BarnesHut::diskModel: a 1e5 central mass at the origin, bodies of mass 2e5/n
+// with radius in [1.5, 12), z = +-i*1e-7 and clockwise circular speed sqrt(M/r).
+Bodies ref_disk(int n, uint64_t seed) {
+    Bodies b(n);
+    const double pi = 3.14159265358979323846, sun = 100000.0;
+    for (int i = 0; i < n; i++) {
+        const double th = 2 * pi * uniform(seed, i, 0), r = 1.5 + 10.5 * uniform(seed, i, 1);
+        if (i == 0) {
+            b.m[i] = (float)sun;
+            continue;
+        }
+        b.m[i] = (float)(2 * sun / n);
+        b.x[i] = (float)(r * std::cos(th));
+        b.y[i] = (float)(r * std::sin(th));
+        b.z[i] = (float)((i % 2 == 0 ? 1e-7 : -1e-7) * i);
+        const double v = std::sqrt(sun / r);
+        b.vx[i] = (float)(v * std::sin(th));
+        b.vy[i] = (float)(-v * std::cos(th));
+    }
+    return b;
+}
+
+// The star + disk workload (mass-1 star, disk bodies of mass 1e-6, r in [0.1, 1]).
+Bodies star_disk(int n, uint64_t seed) {
+    Bodies b(n);
+    const double pi = 3.14159265358979323846;
+    b.m[0] = 1.f;
+    for (int i = 1; i < n; i++) {
+        const uint64_t k = (uint64_t)(i - 1);
+        const double r = 0.1 + 0.9 * uniform(seed, k, 0), ph = 2 * pi * uniform(seed, k, 1);
+        const double u1 = uniform(seed, k, 2), u2 = uniform(seed, k, 3);
+        const double g = std::sqrt(-2.0 * std::log1p(-u1)) * std::cos(2 * pi * u2);
+        const double v = std::sqrt(1.0 / r);
+        b.x[i] = (float)(r * std::cos(ph));
+        b.y[i] = (float)(r * std::sin(ph));
+        b.z[i] = (float)(0.01 * r * g);
+        b.vx[i] = (float)(v * std::sin(ph));
+        b.vy[i] = (float)(-v * std::cos(ph));
+        b.m[i] = 1e-6f;
+    }
+    return b;
+}
+
+Bodies plummer(int n, uint64_t seed) {
+    Bodies b(n);
+    const double pi = 3.14159265358979323846, umax = std::pow(1.0 + 1.0 / 400.0, -1.5);
+    for (int i = 0; i < n; i++) {
+        const double u = std::max(uniform(seed, i, 0) * umax, 1e-300);
+        const double r = 1.0 / std::sqrt(std::pow(u, -2.0 / 3.0) - 1.0);
+        const double ct = 2 * uniform(seed, i, 1) - 1, st = std::sqrt(std::max(0.0, 1 - ct * ct));
+        const double ph = 2 * pi * uniform(seed, i, 2);
+        b.x[i] = (float)(r * st * std::cos(ph));
+        b.y[i] = (float)(r * st * std::sin(ph));
+        b.z[i] = (float)(r * ct);
+        double q = 0;
+        for (int d = 3; d < 4000; d += 2) {
+            const double qq = uniform(seed, i, d), tt = 0.1 * uniform(seed, i, d + 1);
+            if (tt < qq * qq * std::pow(1 - qq * qq, 3.5)) {
+                q = qq;
+                break;
+            }
+        }
+        const double v = q * std::sqrt(2.0) * std::pow(1 + r * r, -0.25);
+        const double ct2 = 2 * uniform(seed, i, 1001) - 1, st2 = std::sqrt(std::max(0.0, 1 - ct2 * ct2));
+        const double ph2 = 2 * pi * uniform(seed, i, 1002);
+        b.vx[i] = (float)(v * st2 * std::cos(ph2));
+        b.vy[i] = (float)(v * st2 * std::sin(ph2));
+        b.vz[i] = (float)(v * ct2);
+        b.m[i] = (float)(1.0 / n);
+    }
+    return b;
+}
+
+void usage() {
+    std::printf("./nbx_runner [-i iterations] [-n particles] [-b blocksize] [-g gridsize] [-R renderinterval]\n"
+                "             [-r] [-v...] [--model ref-disk|disk|plummer] [--theta-ref X] [--eps2 X] [--seed N]\n");
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    nbx::SimulationParameters p;
+    std::string model = "ref-disk";
+    uint64_t seed = 20261203;
+    int verbosity = 0;
+    for (int a = 1; a < argc; a++) {
+        const std::string s = argv[a];
+        auto next = [&](const char *what) -> const char * {
+            if (a + 1 >= argc) {
+                std::fprintf(stderr, "missing value for %s\n", what);
+                std::exit(2);
+            }
+            return argv[++a];
+        };
+        if (s == "-h" || s == "--help") {
+            usage();
+            return 0;
+        } else if (s == "-i" || s == "--iterations") p.iterations = std::atoi(next("-i"));
+        else if (s == "-n" || s == "--particles") p.numberOfParticles = std::atoi(next("-n"));
+        else if (s == "-b" || s == "--blocksize") p.blockSize = std::atoi(next("-b"));
+        else if (s == "-g" || s == "--gridsize") p.gridSize = std::atoi(next("-g"));
+        else if (s == "-R" || s == "--renderinterval") p.renderInterval = std::atoi(next("-R"));
+        else if (s == "-r" || s == "--render") std::printf("rendering is not part of this build; continuing\n");
+        else if (s.size() >= 2 && s[0] == '-' && s[1] == 'v' && s.find_first_not_of('v', 1) == std::string::npos)
+            verbosity += (int)s.size() - 1;
+        else if (s == "--model") model = next("--model");
+        else if (s == "--theta-ref") p.theta_ref = (float)std::atof(next("--theta-ref"));
+        else if (s == "--eps2") p.eps_squared = (float)std::atof(next("--eps2"));
+        else if (s == "--seed") seed = std::strtoull(next("--seed"), nullptr, 10);
+        else {
+            std::fprintf(stderr, "unknown option %s\n", s.c_str());
+            usage();
+            return 2;
+        }
+    }
+    const int n = p.numberOfParticles;
+    if (n < 1 || p.iterations < 1) {
+        usage();
+        return 2;
+    }
+    Bodies b = model == "disk" ? star_disk(n, seed) : model == "plummer" ? plummer(n, seed) : ref_disk(n, seed);
+    try {
+        nbx::BarnesHut bh(p, b.x.data(), b.y.data(), b.z.data(), b.vx.data(), b.vy.data(), b.vz.data(),
+                          b.m.data());
+        for (int i = 0; i < p.iterations; i++) {
+            bh.update(i);
+            if (verbosity > 0) std::printf("Elapsed time for step %d : %g ms\n", i, bh.time_all.back());
+        }
+        auto total = [](const std::vector<float> &v) {
+            double t = 0;
+            for (float x : v) t += x;
+            return t;
+        };
+        const double it = p.iterations;
+        struct Row {
+            const char *name;
+            double t;
+        } rows[] = {{"reset arrays", total(bh.time_resetArrays)},
+                    {"compute bounding boxes", total(bh.time_computeBoundingBox)},
+                    {"build tree", total(bh.time_buildTree)},
+                    {"compute COM", total(bh.time_centreOfMass)},
+                    {"sort", total(bh.time_sort)},
+                    {"compute forces", total(bh.time_computeForces)},
+                    {"update bodies", total(bh.time_update)},
+                    {"copy from device to host", total(bh.time_copyDeviceToHost)}};
+        std::printf("----------------------FINISHED----------------------\n");
+        for (const Row &r : rows) std::printf("Time to %s: %gms\n\tper step: %gms\n", r.name, r.t, r.t / it);
+        const double all = total(bh.time_all), copy = total(bh.time_copyDeviceToHost);
+        std::printf("----------------------------------------------\n");
+        std::printf("TOTAL TIME: %gms\n\tper step: %gms\n", all, all / it);
+        std::printf("TOTAL TIME (without copying): %gms\n\tper step: %gms\n", all - copy, (all - copy) / it);
+        std::printf("----------------------------------------------\n");
+        std::printf("Number of particles: %d\nNumber of iterations: %d\n", n, p.iterations);
+        std::printf("final position of body 1: %.9g %.9g %.9g\n", bh.h_x[n > 1 ? 1 : 0], bh.h_y[n > 1 ? 1 : 0],
+                    bh.h_z[n > 1 ? 1 : 0]);
+    } catch (const nbx::Error &e) {
+        std::fprintf(stderr, "error: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
