@@ -35,10 +35,10 @@ constexpr int kDfsReserve = 7 * 42 + 8;
 
 // Build-time tuning knobs of the evaluation loops (defaults are the measured best).
 #ifndef NBX_BODY_UNROLL
-#define NBX_BODY_UNROLL 4
+#define NBX_BODY_UNROLL 8
 #endif
 #ifndef NBX_CELL_UNROLL
-#define NBX_CELL_UNROLL 2
+#define NBX_CELL_UNROLL 4
 #endif
 #ifndef NBX_WALK64_MINB
 #define NBX_WALK64_MINB 2
