@@ -42,6 +42,7 @@ extern "C" {
 #define NBX_ERR_TIMEOUT 8   /* a bounded device-side wait expired */
 #define NBX_ERR_STATE 9     /* call out of order (e.g. forces before a build) */
 #define NBX_ERR_NOMEM 10    /* device allocation failed */
+#define NBX_ERR_SCRATCH 11  /* request larger than the static scratch of a no-allocation entry point */
 
 typedef struct nbx_ctx nbx_ctx;
 
@@ -121,6 +122,20 @@ int nbx_reset_arrays(nbx_ctx *ctx, int *mutex, float *x, float *y, float *z, flo
 int nbx_compute_bounding_box(nbx_ctx *ctx, int *mutex, float *x, float *y, float *z, float *minX,
                              float *maxX, float *minY, float *maxY, float *minZ, float *maxZ,
                              int n, void *stream, float *ms);
+/* Context-free variant of nbx_compute_bounding_box that allocates nothing; it has
+ * no counterpart in the reference.  For callers that own their body arrays but
+ * cannot allocate device memory (a fixed memory budget, or an allocator that
+ * has already reserved the HBM) and so cannot create a context.  Same merge
+ * into *minX..*maxZ and, with grid_size 0 (the context path's grid), the same
+ * bits.  Its scratch is a static per-device array of 4096 block partials
+ * (128 KiB + 256 B) held by every GPU that loads the library: grid_size above
+ * 4096 returns NBX_ERR_SCRATCH.  All calls on a device share that array, so
+ * calls that overlap on the GPU race.  The first call on a device resolves the
+ * array's address (cudaGetSymbolAddress): make it before any stream capture.
+ * `mutex` is accepted for the reference signature and unused. */
+int nbx_compute_bounding_box_noalloc(int *mutex, const float *x, const float *y, const float *z,
+                                     float *minX, float *maxX, float *minY, float *maxY, float *minZ,
+                                     float *maxZ, int n, int grid_size, void *stream);
 /* KernelsWrapper::buildTree (KernelsWrapper.cu:81; Kernels.cu:157-377): keys, sort
  * and key-built octree; writes child[], count[] and mass[], x/y/z (= sum m*x) of
  * the cells, *index. */

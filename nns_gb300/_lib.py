@@ -15,7 +15,7 @@ NBX_OK = 0
 STATUS_NAMES = {
     0: "NBX_OK", 1: "NBX_ERR_ARG", 2: "NBX_ERR_CUDA", 3: "NBX_ERR_DEPTH", 4: "NBX_ERR_CAPACITY",
     5: "NBX_ERR_STACK", 6: "NBX_ERR_NONFINITE", 7: "NBX_ERR_CLUSTER", 8: "NBX_ERR_TIMEOUT",
-    9: "NBX_ERR_STATE", 10: "NBX_ERR_NOMEM",
+    9: "NBX_ERR_STATE", 10: "NBX_ERR_NOMEM", 11: "NBX_ERR_SCRATCH",
 }
 
 
@@ -56,6 +56,7 @@ SIGNATURES = {
     "nbx_set_constants": (_I, [_P, _F, _F, _I]),
     "nbx_reset_arrays": (_I, [_P] + [_P] * 16 + [_I, _I, _P, _PF]),
     "nbx_compute_bounding_box": (_I, [_P] + [_P] * 10 + [_I, _P, _PF]),
+    "nbx_compute_bounding_box_noalloc": (_I, [_P] * 10 + [_I, _I, _P]),
     "nbx_build_tree": (_I, [_P] + [_P] * 14 + [_I, _I, _P, _PF]),
     "nbx_centre_of_mass": (_I, [_P] + [_P] * 5 + [_I, _P, _PF]),
     "nbx_sort": (_I, [_P] + [_P] * 5 + [_I, _P, _PF]),

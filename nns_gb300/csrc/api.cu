@@ -157,6 +157,7 @@ const char *nbx_status_string(int s) {
         case NBX_ERR_TIMEOUT: return "bounded device wait expired";
         case NBX_ERR_STATE: return "call out of order or inconsistent tree";
         case NBX_ERR_NOMEM: return "device allocation failed";
+        case NBX_ERR_SCRATCH: return "request exceeds the static scratch of a no-allocation entry point";
         default: return "unknown status";
     }
 }
