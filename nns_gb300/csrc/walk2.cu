@@ -3,21 +3,25 @@
 // organised for throughput on sm_103a.
 //
 // Per warp (one aligned group of 32 sorted bodies), rounds of
-//   expand   up to P stack cells are popped at once, one per lane; their child
-//            blocks (contiguous in the BFS node array) are spread over the lanes,
-//            one child per lane, and copied into two per-warp shared-memory
-//            buffers: bodies (always interact, no MAC) and cells (carry their
-//            threshold dp = depth0 * 0.25^(L-1) and id);
+//   expand   the P top-of-stack cells whose children fit the buffers are popped
+//            at once, one per lane; their child blocks (contiguous in the BFS
+//            node array) are spread over the lanes, one child per lane.  Each
+//            lane classifies its child cell against the group's box and a few
+//            representative bodies (exactly, see below): surely accepted cells
+//            join the bodies in the body buffer, surely rejected cells are
+//            pushed at once, the rest go to the cell buffer with their
+//            threshold dp = depth0 * 0.25^(L-1) and id;
 //   evaluate every lane streams the buffers with broadcast shared-memory loads,
 //            two candidates per instruction with the packed FP32 pair
 //            instructions (add/fma/mul .rn.f32x2: each lane an IEEE FP32 op, so r
 //            and the MAC decisions are bit-identical to the scalar form).  Body
-//            pairs go straight to the accumulation; each cell takes one warp
-//            vote (dp <= r on every lane) and is accumulated or pushed.
-// P is bounded by the buffers (8 children per cell).  Wide rounds run while the
-// stack keeps a depth-first reserve free (7 entries per level); beyond that the
-// walk pops one cell per round, which can never outgrow the reserve, so a stack
-// of at least kDfsReserve + 7*8 entries cannot overflow (NBX_ERR_STACK otherwise).
+//            buffer pairs go straight to the accumulation; each cell of the cell
+//            buffer takes one warp vote (dp <= r on every lane) and is
+//            accumulated or pushed.
+// Wide rounds run while the stack keeps a depth-first reserve free (7 entries
+// per level); beyond that the walk pops one cell per round, which can never
+// outgrow the reserve, so a stack of at least kDfsReserve + 7*8 entries cannot
+// overflow (NBX_ERR_STACK otherwise).
 //
 // Accumulation modes: 0 plain FP32 (two packed partial sums), 1 split
 // compensation (plain FP32 within a round, Kahan across rounds), 2 Kahan on
@@ -43,6 +47,12 @@ constexpr int kDfsReserve = 7 * 42 + 8;
 #ifndef NBX_WALK64_MINB
 #define NBX_WALK64_MINB 2
 #endif
+// representative bodies of a group tested against each child cell in the expand
+#ifndef NBX_MAC_REPS
+#define NBX_MAC_REPS 4
+#endif
+static_assert(NBX_MAC_REPS >= 0 && NBX_MAC_REPS <= 4, "NBX_MAC_REPS must be 0..4");
+constexpr int kReps = NBX_MAC_REPS;
 // (#pragma arguments are not macro-expanded: the unroll factors go through constants)
 constexpr int kBodyUnroll = NBX_BODY_UNROLL;
 constexpr int kCellUnroll = NBX_CELL_UNROLL;
@@ -94,7 +104,7 @@ __device__ __forceinline__ void kahan(float &s, float &c, float v) {
     s = t;
 }
 
-// Per-warp candidate buffers of CB slots each (CB/8 cells expanded per round).
+// Per-warp candidate buffers of CB slots each.
 template <int CB>
 struct WarpBuf {
     static constexpr int kPairs = CB / 2;
@@ -105,6 +115,7 @@ struct WarpBuf {
     u64 cd[kPairs];         //         (dp0,dp1)
     int cid[CB];            //         node | level << 26
     int bid[CB];            // body node ids (interaction-list recording only)
+    float4 cls[2 + 4];      // group box lo, hi; representative bodies (x, y, z)
 };
 
 __device__ __forceinline__ void put4(ulonglong2 *a, ulonglong2 *b, int slot, float4 q) {
@@ -183,6 +194,36 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
         const float4 me = body4[valid ? p : p0];
         const u64 px = pk(me.x, me.x), py = pk(me.y, me.y), pz = pk(me.z, me.z);
         const float d0 = depth0[s];
+        {
+            // the group's box and representative bodies, for classifying children
+            float b[6] = {me.x, me.x, me.y, me.y, me.z, me.z};
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+                for (int k = 0; k < 6; k += 2) {
+                    b[k] = fminf(b[k], __shfl_xor_sync(0xffffffffu, b[k], o));
+                    b[k + 1] = fmaxf(b[k + 1], __shfl_xor_sync(0xffffffffu, b[k + 1], o));
+                }
+            }
+            // representatives: lane 0, the last body, the body nearest the box
+            // centre and the middle body (any lane's body is a valid choice)
+            const float ex = me.x - 0.5f * (b[0] + b[1]), ey = me.y - 0.5f * (b[2] + b[3]);
+            const float ez = me.z - 0.5f * (b[4] + b[5]);
+            const unsigned key = __float_as_uint(ex * ex + ey * ey + ez * ez);
+            const unsigned kmin = __reduce_min_sync(0xffffffffu, key);
+            const int lc = __ffs(__ballot_sync(0xffffffffu, key == kmin)) - 1;
+            const int nv = end - p0;
+            const int rl = lane == 0 ? 0 : lane == 1 ? nv - 1 : lane == 2 ? lc : nv >> 1;
+            const float rx = __shfl_sync(0xffffffffu, me.x, rl & 31);
+            const float ry = __shfl_sync(0xffffffffu, me.y, rl & 31);
+            const float rz = __shfl_sync(0xffffffffu, me.z, rl & 31);
+            if (lane < 4) buf.cls[2 + lane] = make_float4(rx, ry, rz, 0.f);
+            if (lane == 0) {
+                buf.cls[0] = make_float4(b[0], b[2], b[4], 0.f);
+                buf.cls[1] = make_float4(b[1], b[3], b[5], 0.f);
+            }
+            __syncwarp();
+        }
         Sums acc;
         int top = 0, nb = 0, len = 0, opened = 0, nrec = 0;
         bool overflow = false;
@@ -214,15 +255,10 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             // ---- expand: lane j pops stack[top-1-j] and copies its children
             // wide rounds while the stack keeps the depth-first reserve free,
             // else one cell per round (depth-first), which cannot outgrow it
-            int P = min(min(top, 32), (kCB - nb) >> 3);
-            if (top + 7 * P > stack_cap - kDfsReserve) P = min(P, 1);
-            if (top + 7 * P > stack_cap) P = 0;
-            if (P == 0 && nb == 0) {
-                overflow = true;
-                break;
-            }
+            // P = the most top-of-stack cells whose children fit the buffers
+            const int avail = min(top, 32);
             int first = 0, nch = 0, lvl = 0;
-            if (lane < P) {
+            if (lane < avail) {
                 const int e = stack[top - 1 - lane];
                 const int b = e & ((1 << kLevelShift) - 1);
                 lvl = e >> kLevelShift;
@@ -237,12 +273,34 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 if (lane >= o) incl += u;
             }
             const int excl = incl - nch;
-            const int T = __shfl_sync(0xffffffffu, incl, 31);
+            int P = __popc(__ballot_sync(0xffffffffu, lane < avail && incl <= kCB - nb));
+            int T = __shfl_sync(0xffffffffu, incl, (P + 31) & 31);
+            // the stack grows by at most T - P: wide rounds only while that keeps
+            // the depth-first reserve free, else one cell
+            if (P > 1 && top - P + T > stack_cap - kDfsReserve) {
+                P = 1;
+                T = __shfl_sync(0xffffffffu, incl, 0);
+            }
+            if (P > 0 && top - P + T > stack_cap) P = 0;
+            if (P == 0) T = 0;
+            if (P == 0 && nb == 0) {
+                overflow = true;
+                break;
+            }
             __syncwarp();
             top -= P;
             // the T children are spread over the lanes, 32 at a time: lane t
             // finds its popped cell j (largest j < P with excl_j <= t)
-            int nbody = nb, ncell = 0;
+            // Each child cell is classified by its lane before any warp-wide work:
+            //   sure accept: a lower bound of every lane's r (the gaps between the
+            //     cell and the group box, in the walk's own FP32 operation order;
+            //     rounding is monotone) is >= dp, so the vote would pass: the cell
+            //     goes to the body buffer (no vote);
+            //   sure reject: a representative body's r (computed exactly as its
+            //     lane does) is < dp, so the vote would fail: pushed at once;
+            //   otherwise it is voted on in the cell buffer.
+            // The interaction lists are unchanged; only their order differs.
+            int nbody = nb, ncell = 0, nsrej = 0;
             for (int t0 = 0; t0 < T; t0 += 32) {
                 const int t = t0 + lane;
                 int j = 0;
@@ -259,21 +317,44 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 const int c = fj + (t - ej);
                 const int cm = ok ? meta[c] : 0;
                 const float4 q = ok ? node4[c] : make_float4(0.f, 0.f, 0.f, 0.f);
-                const unsigned bm = __ballot_sync(0xffffffffu, ok && cm < 0);
-                const unsigned cmk = __ballot_sync(0xffffffffu, ok && cm >= 0);
-                if (ok && cm < 0) {
+                const bool isc = ok && cm >= 0;
+                const float dpc = scale4(d0, lj);
+                bool sacc = false, srej = false;
+                if (isc) {
+                    const float4 lo = buf.cls[0], hi = buf.cls[1];
+                    const float gx = fmaxf(0.f, fmaxf(__fsub_rn(lo.x, q.x), __fsub_rn(q.x, hi.x)));
+                    const float gy = fmaxf(0.f, fmaxf(__fsub_rn(lo.y, q.y), __fsub_rn(q.y, hi.y)));
+                    const float gz = fmaxf(0.f, fmaxf(__fsub_rn(lo.z, q.z), __fsub_rn(q.z, hi.z)));
+                    sacc = dpc <= __fmaf_rn(gz, gz, __fmaf_rn(gy, gy, __fmaf_rn(gx, gx, eps2)));
+#pragma unroll
+                    for (int k = 0; k < kReps; k++) {
+                        const float4 rp = buf.cls[2 + k];
+                        const float dx = __fsub_rn(q.x, rp.x), dy = __fsub_rn(q.y, rp.y), dz = __fsub_rn(q.z, rp.z);
+                        srej |= __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, eps2))) < dpc;
+                    }
+                }
+                const bool tob = ok && (cm < 0 || sacc);
+                const bool toc = isc && !sacc && !srej;
+                const bool tos = isc && !sacc && srej;
+                const unsigned bm = __ballot_sync(0xffffffffu, tob);
+                const unsigned cmk = __ballot_sync(0xffffffffu, toc);
+                const unsigned smk = __ballot_sync(0xffffffffu, tos);
+                if (tob) {
                     put4(buf.ba, buf.bb, nbody + __popc(bm & lt), q);
                     if (Rec) buf.bid[nbody + __popc(bm & lt)] = c;
                 }
-                if (ok && cm >= 0) {
+                if (toc) {
                     const int slot = ncell + __popc(cmk & lt);
                     put4(buf.ca, buf.cb, slot, q);
-                    reinterpret_cast<float *>(&buf.cd[slot >> 1])[slot & 1] = scale4(d0, lj);
+                    reinterpret_cast<float *>(&buf.cd[slot >> 1])[slot & 1] = dpc;
                     buf.cid[slot] = c | ((lj + 1) << kLevelShift);  // children are at level lj+1
                 }
+                if (tos) stack[top + nsrej + __popc(smk & lt)] = c | ((lj + 1) << kLevelShift);
                 nbody += __popc(bm);
                 ncell += __popc(cmk);
+                nsrej += __popc(smk);
             }
+            top += nsrej;
             // pad odd buffers with a massless far-away candidate that is accepted
             if (lane == 0 && (nbody & 1)) put4(buf.ba, buf.bb, nbody, make_float4(1e18f, 1e18f, 1e18f, 0.f));
             if (lane == 1 && (ncell & 1)) {
@@ -352,9 +433,9 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             }
             top += nrej;
             tot_rounds += 1ull;
-            tot_cand += (unsigned long long)(nbody + ncell);
+            tot_cand += (unsigned long long)(nbody + ncell + nsrej);
             len += nbody + ncell - nrej;
-            opened += nrej;
+            opened += nrej + nsrej;
             nb = 0;
             if (Mode == 1) {  // fold this round's partial sums into the compensated totals
                 float a0, a1;
