@@ -29,6 +29,7 @@ struct DevStatus {
     unsigned long long opened;
     unsigned long long rounds;      // walk expand/evaluate rounds (production walk)
     unsigned long long candidates;  // candidates evaluated by the production walk
+    unsigned walk_next;             // next group of the production walk (cleared per launch)
 };
 
 struct Ctx {

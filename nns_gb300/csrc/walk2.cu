@@ -115,7 +115,9 @@ struct WarpBuf {
     u64 cd[kPairs];         //         (dp0,dp1)
     int cid[CB];            //         node | level << 26
     int bid[CB];            // body node ids (interaction-list recording only)
-    float4 cls[2 + 4];      // group box lo, hi; representative bodies (x, y, z)
+    float4 cls[2];          // group box lo, hi
+    ulonglong2 rxy[2];      // representative bodies, in pairs: (x0,x1) (y0,y1)
+    u64 rz[2];              //                                  (z0,z1)
 };
 
 __device__ __forceinline__ void put4(ulonglong2 *a, ulonglong2 *b, int slot, float4 q) {
@@ -183,7 +185,12 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
     const u64 eps2x2 = pk(eps2, eps2);
     unsigned long long tot_len = 0ull, tot_open = 0ull, tot_rounds = 0ull, tot_cand = 0ull;
 
-    for (int g = blockIdx.x * warps + w; g < ngroups; g += gridDim.x * warps) {
+    // groups are handed out dynamically (costs vary widely between groups)
+    for (;;) {
+        int g = 0;
+        if (lane == 0) g = (int)atomicAdd(&st->walk_next, 1u);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= ngroups) break;
         const int p0 = groups[g];
         const int s = body_sys[p0];
         const int end = min(sys_off[s + 1], p0 + 32);
@@ -217,7 +224,12 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             const float rx = __shfl_sync(0xffffffffu, me.x, rl & 31);
             const float ry = __shfl_sync(0xffffffffu, me.y, rl & 31);
             const float rz = __shfl_sync(0xffffffffu, me.z, rl & 31);
-            if (lane < 4) buf.cls[2 + lane] = make_float4(rx, ry, rz, 0.f);
+            if (lane < 4) {
+                float *pxy = reinterpret_cast<float *>(&buf.rxy[lane >> 1]);
+                pxy[lane & 1] = rx;
+                pxy[2 + (lane & 1)] = ry;
+                reinterpret_cast<float *>(&buf.rz[lane >> 1])[lane & 1] = rz;
+            }
             if (lane == 0) {
                 buf.cls[0] = make_float4(b[0], b[2], b[4], 0.f);
                 buf.cls[1] = make_float4(b[1], b[3], b[5], 0.f);
@@ -290,7 +302,12 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             __syncwarp();
             top -= P;
             // the T children are spread over the lanes, 32 at a time: lane t
-            // finds its popped cell j (largest j < P with excl_j <= t)
+            // finds its popped cell j (largest j < P with excl_j <= t) by counting
+            // the segment starts at or below t in a bit mask of the starts
+            unsigned seg[kCB / 32];
+#pragma unroll
+            for (int k = 0; k < kCB / 32; k++)
+                seg[k] = __reduce_or_sync(0xffffffffu, (lane < P && (excl >> 5) == k) ? 1u << (excl & 31) : 0u);
             // Each child cell is classified by its lane before any warp-wide work:
             //   sure accept: a lower bound of every lane's r (the gaps between the
             //     cell and the group box, in the walk's own FP32 operation order;
@@ -301,15 +318,15 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             //   otherwise it is voted on in the cell buffer.
             // The interaction lists are unchanged; only their order differs.
             int nbody = nb, ncell = 0, nsrej = 0;
-            for (int t0 = 0; t0 < T; t0 += 32) {
-                const int t = t0 + lane;
-                int j = 0;
+            int jbase = -1;
 #pragma unroll
-                for (int step = 16; step > 0; step >>= 1) {
-                    const int cand = j + step;
-                    const int e = __shfl_sync(0xffffffffu, excl, cand & 31);
-                    if (cand < P && e <= t) j = cand;
-                }
+            for (int k = 0; k < kCB / 32; k++) {
+                const int t0 = 32 * k;
+                if (t0 >= T) break;
+                const int t = t0 + lane;
+                const unsigned le = lane == 31 ? 0xffffffffu : (2u << lane) - 1u;
+                const int j = jbase + __popc(seg[k] & le);
+                jbase += __popc(seg[k]);
                 const int fj = __shfl_sync(0xffffffffu, first, j);
                 const int lj = __shfl_sync(0xffffffffu, lvl, j);
                 const int ej = __shfl_sync(0xffffffffu, excl, j);
@@ -326,11 +343,17 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                     const float gy = fmaxf(0.f, fmaxf(__fsub_rn(lo.y, q.y), __fsub_rn(q.y, hi.y)));
                     const float gz = fmaxf(0.f, fmaxf(__fsub_rn(lo.z, q.z), __fsub_rn(q.z, hi.z)));
                     sacc = dpc <= __fmaf_rn(gz, gz, __fmaf_rn(gy, gy, __fmaf_rn(gx, gx, eps2)));
+                    // two representatives per packed instruction, same operations
+                    // and order as the evaluation (so r is their lanes' r exactly)
+                    const u64 qx = pk(q.x, q.x), qy = pk(q.y, q.y), qz = pk(q.z, q.z);
 #pragma unroll
-                    for (int k = 0; k < kReps; k++) {
-                        const float4 rp = buf.cls[2 + k];
-                        const float dx = __fsub_rn(q.x, rp.x), dy = __fsub_rn(q.y, rp.y), dz = __fsub_rn(q.z, rp.z);
-                        srej |= __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, eps2))) < dpc;
+                    for (int k = 0; k < (kReps + 1) / 2; k++) {
+                        const ulonglong2 R = buf.rxy[k];
+                        const u64 dx = sub2(qx, R.x), dy = sub2(qy, R.y), dz = sub2(qz, buf.rz[k]);
+                        float ra, rb;
+                        upk(fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, eps2x2))), ra, rb);
+                        srej |= ra < dpc;
+                        if (2 * k + 1 < kReps) srej |= rb < dpc;
                     }
                 }
                 const bool tob = ok && (cm < 0 || sacc);
@@ -510,6 +533,7 @@ int launch(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st,
     if (per_sm < 1) per_sm = 1;
     const int grid = blocks_needed < ctx->nsm * per_sm ? blocks_needed : ctx->nsm * per_sm;
     if (grid <= 0) return NBX_OK;
+    NBX_CUDA(cudaMemsetAsync(&ctx->d_status->walk_next, 0, sizeof(unsigned), st));
     k_walk2<CB, Mode, Pot, Rec><<<grid, warps * 32, smem, st>>>(
         ctx->d_node4, ctx->d_meta, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
         ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay, s->az,
