@@ -34,7 +34,9 @@ namespace {
 
 // Stack entries kept free for depth-first descent: from any stack content a
 // depth-first walk (one cell per round) grows the stack by at most 7 entries per
-// level below the popped cell, i.e. by less than 7 * 42.
+// level below the popped cell, i.e. by less than 7 * (deepest level) <= 7 * 42.
+// The walk uses the bound of the tree at hand (its deepest level, recorded by
+// the build); kDfsReserve is the bound for any tree.
 constexpr int kDfsReserve = 7 * 42 + 8;
 
 // Build-time tuning knobs of the evaluation loops (defaults are the measured best).
@@ -43,6 +45,9 @@ constexpr int kDfsReserve = 7 * 42 + 8;
 #endif
 #ifndef NBX_CELL_UNROLL
 #define NBX_CELL_UNROLL 4
+#endif
+#ifndef NBX_WALK64_THREADS
+#define NBX_WALK64_THREADS 512
 #endif
 #ifndef NBX_WALK64_MINB
 #define NBX_WALK64_MINB 2
@@ -161,7 +166,7 @@ __device__ __forceinline__ void accumulate(Sums &a, u64 f, u64 mm, u64 ri, u64 d
 // CB = 128: up to 85 registers for more loads in flight (three 8-warp blocks).
 template <int CB>
 struct WalkBounds {
-    static constexpr int kThreads = CB == 64 ? 512 : 256;
+    static constexpr int kThreads = CB == 64 ? NBX_WALK64_THREADS : 256;
     static constexpr int kMinBlocks = CB == 64 ? NBX_WALK64_MINB : 3;
 };
 
@@ -184,6 +189,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
     const unsigned lt = (1u << lane) - 1u;
     const u64 eps2x2 = pk(eps2, eps2);
     unsigned long long tot_len = 0ull, tot_open = 0ull, tot_rounds = 0ull, tot_cand = 0ull;
+    const int reserve = 7 * min(max(st->max_level, 1), 42) + 8;
 
     // groups are handed out dynamically (costs vary widely between groups)
     for (;;) {
@@ -289,7 +295,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             int T = __shfl_sync(0xffffffffu, incl, (P + 31) & 31);
             // the stack grows by at most T - P: wide rounds only while that keeps
             // the depth-first reserve free, else one cell
-            if (P > 1 && top - P + T > stack_cap - kDfsReserve) {
+            if (P > 1 && top - P + T > stack_cap - reserve) {
                 P = 1;
                 T = __shfl_sync(0xffffffffu, incl, 0);
             }
