@@ -283,6 +283,29 @@ def bench_adjoint(args, local):
     return out
 
 
+def bench_frame(ctx, s, b, reps: int = 5) -> dict:
+    """One headless frame of the current state with the reference renderer's
+    constants (1024 x 1024, dot 8; system size from the initial state, as
+    main.cu:93-95), timed with CUDA events on the current stream."""
+    import torch
+    from nns_gb300.render import Frame, default_params
+    half = float(max(np.abs(b.x).max(), np.abs(b.y).max(), np.abs(b.z).max()))
+    fr = Frame(default_params(system_size=float(np.float32(2.0) * np.float32(half))))
+    for _ in range(2):
+        fr.render(ctx, s)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        img = fr.render(ctx, s)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    n = s.x.numel()
+    return {"width": fr.p.width, "height": fr.p.height, "ms_per_frame": round(ms, 3),
+            "bodies_per_s": round(n / (ms * 1e-3), 1), "lit_bytes": int((img > 0).sum().item())}
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
@@ -402,6 +425,7 @@ def main():
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / args.steps
     ctx.sync()
+    frame = bench_frame(ctx, s, b)
 
     ms_plain = plain["ms"] / args.steps
     ms_comp = comp["ms"] / args.steps
@@ -450,6 +474,7 @@ def main():
                         "ratio_to_plain_time": round(ms_comp / ms_plain, 4)},
         "force_error_vs_fp64_direct": errs,
         "fp32_error_vs_fp64_same_lists": errs32,
+        "frame": frame,
         "interactions_per_step": inter_per_step,
         "opened_cells_per_step": plain["opened"],
         "walk_rounds_per_step": plain["rounds"],

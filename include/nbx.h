@@ -239,6 +239,30 @@ int nbx_adjoint_stats(nbx_adjoint *adj, int64_t *bytes, float *forward_ms, float
  * out[4..6] angular momentum, out[7] total mass (device double[8]). */
 int nbx_diagnostics_fp64(nbx_ctx *ctx, const nbx_state *s, int n, double *out, void *stream);
 
+/* ---- headless frame ------------------------------------------------------
+ * The reference renderer's velocity-coloured dot splat
+ * (3D/CUDA/CUDA_NBody/src/Renderer.cpp:54-147; constants Constants.h:31-38) into
+ * a device RGB buffer instead of a window or file: rgb[3*(x + width*y) + c],
+ * the payload of the reference's P6 frame.  Selection, colour ramp and pixel
+ * mapping are FP64 like the reference; the dot weights are FP32.  */
+typedef struct nbx_render_params {
+    int width, height;          /* WIDTH, HEIGHT */
+    double render_scale;        /* RENDER_SCALE */
+    double max_velocity_color;  /* MAX_VEL_COLOR */
+    double min_velocity_color;  /* MIN_VEL_COLOR */
+    double particle_brightness; /* PARTICLE_BRIGHTNESS */
+    double particle_sharpness;  /* PARTICLE_SHARPNESS */
+    int dot_size;               /* DOT_SIZE (<= 16) */
+    double system_size;         /* > 0; main.cu:95 passes 2 * BarnesHut::getSystemSize() */
+} nbx_render_params;
+void nbx_render_params_default(nbx_render_params *p);
+/* Renderer::createFrame without the file (Renderer.cpp:37-52): accum is device
+ * scratch of 3*width*height floats, rgb receives 3*width*height bytes.  Bodies
+ * [0,n) of s (x, y, vx, vy, vz) are drawn; the context's sorted order is used
+ * when its tree covers n bodies. */
+int nbx_render_frame(nbx_ctx *ctx, const nbx_state *s, int n, const nbx_render_params *p, float *accum,
+                     unsigned char *rgb, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -40,6 +40,13 @@ class nbx_tree_info(C.Structure):
                 ("launches", C.c_int64), ("rounds", C.c_int64), ("candidates", C.c_int64)]
 
 
+class nbx_render_params(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("render_scale", C.c_double),
+                ("max_velocity_color", C.c_double), ("min_velocity_color", C.c_double),
+                ("particle_brightness", C.c_double), ("particle_sharpness", C.c_double),
+                ("dot_size", C.c_int), ("system_size", C.c_double)]
+
+
 _P = C.c_void_p
 _I = C.c_int
 _F = C.c_float
@@ -78,6 +85,8 @@ SIGNATURES = {
     "nbx_potential": (_I, [_P, C.POINTER(nbx_state), _P, _P]),
     "nbx_forces_fp64_lists": (_I, [_P, _P, _I, _P, _P]),
     "nbx_diagnostics_fp64": (_I, [_P, C.POINTER(nbx_state), _I, _P, _P]),
+    "nbx_render_params_default": (None, [C.POINTER(nbx_render_params)]),
+    "nbx_render_frame": (_I, [_P, C.POINTER(nbx_state), _I, C.POINTER(nbx_render_params), _P, _P, _P]),
     "nbx_adjoint_create": (_I, [_P, _I, _I, _I, _I, C.POINTER(_P)]),
     "nbx_adjoint_destroy": (_I, [_P]),
     "nbx_adjoint_forward": (_I, [_P, _P, C.POINTER(nbx_state), _P, _P, _P, C.POINTER(C.c_double), _P]),

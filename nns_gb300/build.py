@@ -37,7 +37,9 @@ def _sources():
 
 def _headers():
     return sorted(glob.glob(os.path.join(CSRC, "*.cuh")) +
-                  glob.glob(os.path.join(HERE, "..", "include", "*.h")))
+                  glob.glob(os.path.join(HERE, "..", "include", "*.h")) +
+                  glob.glob(os.path.join(HERE, "..", "include", "nbx", "*.hpp")) +
+                  glob.glob(os.path.join(HERE, "driver", "*.cpp")))
 
 
 def _compile(src: str) -> tuple[str, str]:

@@ -6,12 +6,16 @@
 //   -n, --particles N       number of particles (524288)
 //   -b, --blocksize N       block size hint (256)
 //   -g, --gridsize N        grid size hint (1024)
-//   -R, --renderinterval N  render interval (10); -r/--render is accepted, no frames are written
+//   -R, --renderinterval N  render interval (10)
+//   -r, --render            write a frame every renderinterval steps to images/StepNNNNN.ppm
+//                           (Renderer::createFrame, Renderer.cpp:37-161, through nbx_render_frame)
 //   -v                      verbosity (repeat)
 //   --model ref-disk|disk|plummer   initial conditions (ref-disk: the recipe of
 //                           BarnesHut::diskModel, BarnesHut.cu:356-415)
 //   --theta-ref X --eps2 X  MAC constant and squared softening (Kernels.cu:17-18 defaults)
 //   --seed N
+#include <sys/stat.h>
+
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -128,6 +132,7 @@ int main(int argc, char **argv) {
     std::string model = "ref-disk";
     uint64_t seed = 20261203;
     int verbosity = 0;
+    bool render = false;
     for (int a = 1; a < argc; a++) {
         const std::string s = argv[a];
         auto next = [&](const char *what) -> const char * {
@@ -145,7 +150,7 @@ int main(int argc, char **argv) {
         else if (s == "-b" || s == "--blocksize") p.blockSize = std::atoi(next("-b"));
         else if (s == "-g" || s == "--gridsize") p.gridSize = std::atoi(next("-g"));
         else if (s == "-R" || s == "--renderinterval") p.renderInterval = std::atoi(next("-R"));
-        else if (s == "-r" || s == "--render") std::printf("rendering is not part of this build; continuing\n");
+        else if (s == "-r" || s == "--render") render = true;
         else if (s.size() >= 2 && s[0] == '-' && s[1] == 'v' && s.find_first_not_of('v', 1) == std::string::npos)
             verbosity += (int)s.size() - 1;
         else if (s == "--model") model = next("--model");
@@ -167,9 +172,48 @@ int main(int argc, char **argv) {
     try {
         nbx::BarnesHut bh(p, b.x.data(), b.y.data(), b.z.data(), b.vx.data(), b.vy.data(), b.vz.data(),
                           b.m.data());
+        // main.cu:93-95: the renderer's system size is twice BarnesHut::getSystemSize()
+        // of the initial state (BarnesHut.cu:417-445)
+        float half = 0.f;
+        for (int i = 0; i < n; i++)
+            half = std::max(half, std::max(std::fabs(b.x[i]), std::max(std::fabs(b.y[i]), std::fabs(b.z[i]))));
+        nbx_render_params rp;
+        nbx_render_params_default(&rp);
+        rp.system_size = 2.0 * (double)half;
+        const size_t npix = 3 * (size_t)rp.width * (size_t)rp.height;
+        float *d_accum = nullptr;
+        unsigned char *d_rgb = nullptr;
+        std::vector<unsigned char> h_rgb;
+        if (render) {
+            nbx::check(cudaMalloc(&d_accum, npix * sizeof(float)) == cudaSuccess ? NBX_OK : NBX_ERR_NOMEM,
+                       "cudaMalloc");
+            nbx::check(cudaMalloc(&d_rgb, npix) == cudaSuccess ? NBX_OK : NBX_ERR_NOMEM, "cudaMalloc");
+            h_rgb.resize(npix);
+            mkdir("images", 0755);
+        }
         for (int i = 0; i < p.iterations; i++) {
             bh.update(i);
             if (verbosity > 0) std::printf("Elapsed time for step %d : %g ms\n", i, bh.time_all.back());
+            if (render && i % p.renderInterval == 0) {
+                nbx_state st{};
+                st.x = bh.d_x; st.y = bh.d_y; st.z = bh.d_z;
+                st.vx = bh.d_vx; st.vy = bh.d_vy; st.vz = bh.d_vz;
+                nbx::check(nbx_render_frame(bh.ctx, &st, n, &rp, d_accum, d_rgb, nullptr), "nbx_render_frame");
+                nbx::check(cudaMemcpy(h_rgb.data(), d_rgb, npix, cudaMemcpyDeviceToHost) == cudaSuccess
+                               ? NBX_OK : NBX_ERR_CUDA, "cudaMemcpy");
+                char name[64];
+                std::snprintf(name, sizeof(name), "images/Step%05d.ppm", i / p.renderInterval + 1);
+                if (FILE *f = std::fopen(name, "wb")) {
+                    std::fprintf(f, "P6\n%d %d\n255\n", rp.width, rp.height);
+                    std::fwrite(h_rgb.data(), 1, npix, f);
+                    std::fclose(f);
+                }
+                if (verbosity > 0) std::printf("Writing frame %d\n", i);
+            }
+        }
+        if (render) {
+            cudaFree(d_accum);
+            cudaFree(d_rgb);
         }
         auto total = [](const std::vector<float> &v) {
             double t = 0;

@@ -5,6 +5,9 @@
   (3D/CUDA/CUDA_NBody/src/Kernels.cu) compiled unmodified with g++ against the
   CPU stand-in ``ref_shim/cuda.h``.  Built only where the reference checkout is
   present; its outputs go to ``oracle/_ref/`` only.
+* ``oracle/_ref/libref_render.so`` -- the reference's renderer
+  (3D/CUDA/CUDA_NBody/src/Renderer.cpp, Body.cpp, Logger.cpp) with the C entry
+  point ``ref_shim/render_harness.cpp``, for the headless-frame parity.
 * ``oracle/_ref/omp/`` -- the reference's 3D/OpenMP tree code, staged from the
   checkout (see ``ref_cpu.py``) and compiled against a harness for the timed
   CPU baseline.
@@ -58,9 +61,27 @@ def build_ref_kernels() -> str | None:
     return out
 
 
+def build_ref_renderer() -> str | None:
+    """Compile the reference's renderer sources with a C entry point (only where
+    the checkout exists)."""
+    if not reference_present():
+        return None
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "libref_render.so")
+    harness = os.path.join(HERE, "ref_shim", "render_harness.cpp")
+    if os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(harness):
+        return out
+    srcs = [os.path.join(REF_CUDA, "src", f) for f in ("Renderer.cpp", "Body.cpp", "Logger.cpp")]
+    _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+          "-I", os.path.join(REF_CUDA, "include")] + srcs + [harness, "-o", out])
+    return out
+
+
 def build_all() -> None:
     build_oracle()
     build_ref_kernels()
+    build_ref_renderer()
     from . import ref_cpu  # noqa: WPS433 -- staged reference CPU code
     ref_cpu.build()
 

@@ -261,3 +261,63 @@ def ref_step(x, y, z, vx, vy, vz, m, dt, force_bounds=None, stack_size=4096):
     out["a"] = np.stack([out.pop("ax"), out.pop("ay"), out.pop("az")], 1)
     out["state"] = (x, y, z, vx, vy, vz)
     return out
+
+
+# ---- headless frame (3D/CUDA/CUDA_NBody/src/Renderer.cpp) -------------------
+
+@dataclass
+class RenderParams:
+    """Renderer constants (3D/CUDA/CUDA_NBody/include/Constants.h:31-38); the
+    reference passes systemSize = 2 * BarnesHut::getSystemSize() (main.cu:93-95)."""
+    width: int = 1024
+    height: int = 1024
+    render_scale: float = 2.5
+    max_velocity_color: float = 1500.0
+    min_velocity_color: float = 0.0
+    particle_brightness: float = 0.35
+    particle_sharpness: float = 1.0
+    dot_size: int = 8
+    system_size: float = 1.0
+
+    def args(self):
+        return (C.c_int(self.width), C.c_int(self.height), C.c_double(self.render_scale),
+                C.c_double(self.max_velocity_color), C.c_double(self.min_velocity_color),
+                C.c_double(self.particle_brightness), C.c_double(self.particle_sharpness),
+                C.c_int(self.dot_size), C.c_double(self.system_size))
+
+
+def system_size(x, y, z) -> float:
+    """2 * BarnesHut::getSystemSize() (BarnesHut.cu:417-445): twice the largest
+    |coordinate|, in float."""
+    m = np.float32(max(np.abs(_f32(x)).max(), np.abs(_f32(y)).max(), np.abs(_f32(z)).max(), 0.0))
+    return float(np.float32(2.0) * m)
+
+
+def render(x, y, z, vx, vy, vz, p: RenderParams) -> np.ndarray:
+    """The oracle's frame: (height, width, 3) uint8."""
+    n = len(x)
+    hd = np.zeros(3 * p.width * p.height, np.float64)
+    rgb = np.zeros(3 * p.width * p.height, np.uint8)
+    L = lib()
+    L.orc_render.restype = C.c_int
+    rc = L.orc_render(C.c_int(n), *[_f32(a).ctypes.data_as(C.c_void_p) for a in (x, y, z, vx, vy, vz)],
+                      *p.args(), hd.ctypes.data_as(C.c_void_p), rgb.ctypes.data_as(C.c_void_p))
+    if rc:
+        raise OracleError(rc, "orc_render")
+    return rgb.reshape(p.height, p.width, 3)
+
+
+def ref_render(x, y, z, vx, vy, vz, p: RenderParams):
+    """The reference renderer's frame, or None where it was not built."""
+    path = os.path.join(os.path.dirname(__file__), "_ref", "libref_render.so")
+    if not os.path.exists(path):
+        path = _build.build_ref_renderer()
+    if not path or not os.path.exists(path):
+        return None
+    R = C.CDLL(path)
+    R.ref_render.restype = C.c_int
+    rgb = np.zeros(3 * p.width * p.height, np.uint8)
+    arrs = [_f32(a) for a in (x, y, z, vx, vy, vz)]
+    R.ref_render(C.c_int(len(x)), *[a.ctypes.data_as(C.c_void_p) for a in arrs], *p.args(),
+                 rgb.ctypes.data_as(C.c_void_p))
+    return rgb.reshape(p.height, p.width, 3)

@@ -555,3 +555,62 @@ int orc_direct_adjoint(int n, const double *x0, const double *v0, const double *
     free(X); free(v); free(a); free(g); free(tx);
     return ORC_OK;
 }
+
+/* ---------------------------------------------------------------------------
+ * Headless frame: restatement of the reference renderer's splat
+ * (3D/CUDA/CUDA_NBody/src/Renderer.cpp:54-147), bodies in input order, double
+ * precision throughout, as the reference.
+ *   px = (W/2) (1 + x / (systemSize renderScale))               (:86-89)
+ *   a body is drawn when dot < int(px) < W - dot (same for y)   (:66-71)
+ *   vPortion = sqrt((|v| - vmin) / vmax); colour ramp clamped   (:96-104)
+ *   dot: i, j in [-dot/2, dot/2), pixel (floor(px)+i, floor(py)+j) gains
+ *   colour * brightness / (pow(exp((s (floor(px)+i-px))^2)
+ *                             + exp((s (floor(py)+j-py))^2), 0.75) + 1)  (:106-128)
+ *   byte = int(255 clamp(sum))                                   (:144-147)
+ * hd (3 W H doubles) is scratch; rgb receives W*H*3 bytes.
+ * ------------------------------------------------------------------------- */
+static double clamp01(double v) { return fmax(fmin(v, 1.0), 0.0); }
+
+static double to_pixel(double p, int size, double system_size, double scale)
+{
+    return (size / 2.0) * (1.0 + p / (system_size * scale));
+}
+
+int orc_render(int n, const float *x, const float *y, const float *z, const float *vx,
+               const float *vy, const float *vz, int width, int height, double render_scale,
+               double vmax, double vmin, double brightness, double sharpness, int dot,
+               double system_size, double *hd, unsigned char *rgb)
+{
+    (void)z;
+    if (width < 1 || height < 1 || dot < 0) return ORC_ERR_ARG;
+    memset(hd, 0, sizeof(double) * 3 * (size_t)width * (size_t)height);
+    for (int b = 0; b < n; b++) {
+        const double bx = x[b], by = y[b];
+        const double pxs = to_pixel(bx, width, system_size, render_scale);
+        const double pys = to_pixel(by, height, system_size, render_scale);
+        const int xi = (int)pxs, yi = (int)pys;
+        if (!(xi > dot && xi < width - dot && yi > dot && yi < height - dot)) continue;
+        const double vxd = vx[b], vyd = vy[b], vzd = vz[b];
+        const double vmag = sqrt(vxd * vxd + vyd * vyd + vzd * vzd);
+        if (vmag < vmin) continue;
+        const double vp = sqrt((vmag - vmin) / vmax);
+        const double cr = clamp01(4 * (vp - 0.333));
+        const double cg = clamp01(fmin(4 * vp, 4.0 * (1.0 - vp)));
+        const double cb = clamp01(4 * (0.5 - vp));
+        for (int i = -dot / 2; i < dot / 2; i++) {
+            for (int j = -dot / 2; j < dot / 2; j++) {
+                const double xp = floor(pxs), yp = floor(pys);
+                const double f = brightness /
+                                 (pow(exp(pow(sharpness * (xp + i - pxs), 2.0)) +
+                                          exp(pow(sharpness * (yp + j - pys), 2.0)), 0.75) + 1.0);
+                const size_t pix = 3 * ((size_t)(int)(xp + i) + (size_t)width * (size_t)(int)(yp + j));
+                hd[pix + 0] += cr * f;
+                hd[pix + 1] += cg * f;
+                hd[pix + 2] += cb * f;
+            }
+        }
+    }
+    for (size_t k = 0; k < 3 * (size_t)width * (size_t)height; k++)
+        rgb[k] = (unsigned char)(int)(255.0 * clamp01(hd[k]));
+    return ORC_OK;
+}

@@ -93,9 +93,38 @@ def make(name, gen, with_tight):
     return path, len(b.x), ref["ncells"]
 
 
+# Headless frames of the reference renderer (3D/CUDA/CUDA_NBody/src/Renderer.cpp,
+# compiled from the checkout by oracle/build.py): inputs are regenerated from the
+# seeded initial conditions, only the frame bytes are stored.
+FRAMES = {
+    # name: (generator, n, width, height, max_velocity_color, render_scale)
+    "frame_disk4096": (ic.star_disk, 4096, 160, 128, 2.0, 2.5),
+    "frame_plummer3000": (ic.plummer, 3000, 128, 128, 1.0, 1.0),
+}
+
+
+def frame_params(name):
+    gen, n, w, h, vmax, scale = FRAMES[name]
+    b = gen(n)
+    p = O.RenderParams(width=w, height=h, render_scale=scale, max_velocity_color=vmax,
+                       system_size=O.system_size(b.x, b.y, b.z))
+    return b, p
+
+
+def make_frames():
+    for name in FRAMES:
+        b, p = frame_params(name)
+        rgb = O.ref_render(b.x, b.y, b.z, b.vx, b.vy, b.vz, p)
+        if rgb is None:
+            raise SystemExit("the reference renderer could not be built")
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), rgb=rgb)
+        print(name, rgb.shape, int((rgb > 0).sum()), "lit bytes")
+
+
 def main():
     if O.ref_lib() is None:
         raise SystemExit("the reference checkout is needed to generate fixtures")
+    make_frames()
     for name, (gen, tight) in CASES.items():
         path, n, nc = make(name, gen, tight)
         print("%-14s n=%-6d cells=%-6d %7.1f KB" % (name, n, nc, os.path.getsize(path) / 1024))
