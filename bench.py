@@ -283,6 +283,20 @@ def bench_adjoint(args, local):
     return out
 
 
+def walk_traffic(n: int):
+    """DRAM bytes (read + write) of one walk launch at this size, from the committed
+    ncu summary of the benchmark workload (profiles/), or None for other sizes."""
+    if n != N_DEFAULT:
+        return None
+    try:
+        for line in open(os.path.join(ROOT, "profiles", "k_walk2_traffic_binary_disk_2p24.md")):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(line.split(":")[1])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
 def bench_frame(ctx, s, b, reps: int = 5) -> dict:
     """One headless frame of the current state with the reference renderer's
     constants (1024 x 1024, dot 8; system size from the initial state, as
@@ -483,9 +497,9 @@ def main():
         "phase_ms": {"build": round(plain["build_ms"] / args.steps, 3), "walk": round(walk_ms, 3),
                      "integrate": round(plain["integ_ms"] / args.steps, 3)},
         "tree": {"cells": plain["ncells"], "max_level": plain["max_level"]},
-        "roofline": {"bound": "fp32", "kernel": "k_walk", "achieved": round(achieved, 3),
+        "roofline": {"bound": "fp32", "kernel": "k_walk2", "achieved": round(achieved, 3),
                      "peak": round(peak, 2), "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
-                     "traffic": None,
+                     "traffic": walk_traffic(n),
                      "peak_kind": "nominal FP32 FMA peak (SMs x 128 x 2 x max SM clock %g MHz)" % max_mhz},
         "diagnostics_fp64": {"momentum_drift": float(np.abs(diag1["momentum"] - diag0["momentum"]).max()),
                              "kinetic_rel_change": float((diag1["kinetic"] - diag0["kinetic"]) / diag0["kinetic"])},

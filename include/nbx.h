@@ -69,7 +69,8 @@ typedef struct nbx_params {
     int block_size;    /* reference launch-shape hints (main.cu:30-31); informational */
     int grid_size;
     int walk_variant;  /* 0 production walk, 64-slot candidate buffers; 1 the same with
-                          128-slot buffers; 2 one-cell-at-a-time walk (comparison) */
+                          128-slot buffers; 2 one-cell-at-a-time walk (comparison);
+                          3 production walk, 96-slot buffers */
     int key_order;     /* 0: the reference's body order (Lebesgue keys; bit-exact parity);
                           1: Hilbert keys -- same cells, siblings reordered, so walk groups
                           are compact but the interaction lists differ from the reference */

@@ -4,7 +4,7 @@ The interaction lists are fixed by the reference's semantics (group of 32,
 leaf bucket of one body, 8-bit radix digits are what the parity tests pin), so
 the tunable knobs are the ones that change only speed:
   * warps per block of the walk (4, 8, 16) -- occupancy vs. shared memory,
-  * candidate buffer size of the walk (64 or 128 slots per warp).
+  * candidate buffer size of the walk (64, 96 or 128 slots per warp).
 Candidates are timed with CUDA events on the caller's workload after one
 build; the winner is applied to the context and cached per (device, n, systems)
 in ``~/.cache/nbx_autotune.json`` (override with NBX_AUTOTUNE_CACHE).
@@ -16,7 +16,7 @@ import os
 
 import torch
 
-CANDIDATES = ((8, 0), (16, 0), (4, 0), (8, 1), (4, 1))
+CANDIDATES = ((8, 3), (16, 3), (4, 3), (8, 0), (16, 0), (8, 1), (4, 1))
 
 
 def _cache_path():

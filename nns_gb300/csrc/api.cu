@@ -134,11 +134,12 @@ void nbx_params_default(nbx_params *p) {
     p->dampening = 1.f;
     p->gravity = 1.f;
     p->group = 32;
-    p->stack_depth = 1024;
+    p->stack_depth = 512;
     p->compensated = 0;
     p->leaf_size = 1;
     p->radix_bits = 8;
     p->walk_warps = 0;
+    p->walk_variant = 3;  // 96-slot buffers: the fastest at 2^20 and 2^24 bodies
     p->device = 0;
     p->block_size = 256;
     p->grid_size = 1024;
@@ -169,7 +170,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     *out = nullptr;
     if (p->max_bodies < 1 || p->max_bodies > (1 << 25) || p->max_systems < 1 ||
         p->max_systems > p->max_bodies || p->group != 32 || p->leaf_size != 1 || p->radix_bits != 8 ||
-        p->stack_depth < 360 || p->stack_depth > 4096)
+        p->stack_depth < 360 || p->stack_depth > 4096 || p->walk_variant < 0 || p->walk_variant > 3)
         return NBX_ERR_ARG;
     Ctx *ctx = new (std::nothrow) Ctx();
     if (!ctx) return NBX_ERR_NOMEM;
@@ -290,7 +291,7 @@ int nbx_set_constants(nbx_ctx *c, float theta_ref, float eps2, int compensated) 
 
 int nbx_set_walk_config(nbx_ctx *c, int warps_per_block, int variant) {
     if (!c || !(warps_per_block == 4 || warps_per_block == 8 || warps_per_block == 16) ||
-        !(variant == 0 || variant == 1 || variant == 2))
+        !(variant >= 0 && variant <= 3))
         return NBX_ERR_ARG;
     Ctx *ctx = C(c);
     ctx->walk_warps = warps_per_block;

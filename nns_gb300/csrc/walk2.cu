@@ -52,6 +52,12 @@ constexpr int kDfsReserve = 7 * 42 + 8;
 #ifndef NBX_WALK64_MINB
 #define NBX_WALK64_MINB 2
 #endif
+#ifndef NBX_WALK128_THREADS
+#define NBX_WALK128_THREADS 256
+#endif
+#ifndef NBX_WALK128_MINB
+#define NBX_WALK128_MINB 3
+#endif
 // representative bodies of a group tested against each child cell in the expand
 #ifndef NBX_MAC_REPS
 #define NBX_MAC_REPS 4
@@ -162,12 +168,12 @@ __device__ __forceinline__ void accumulate(Sums &a, u64 f, u64 mm, u64 ri, u64 d
     if (Pot) a.p = fma2(mm, ri, a.p);
 }
 
-// CB = 64: 64-register budget (two 16-warp or four 8-warp blocks per SM);
+// CB = 64 and 96: 64-register budget (two 16-warp or four 8-warp blocks per SM);
 // CB = 128: up to 85 registers for more loads in flight (three 8-warp blocks).
 template <int CB>
 struct WalkBounds {
-    static constexpr int kThreads = CB == 64 ? NBX_WALK64_THREADS : 256;
-    static constexpr int kMinBlocks = CB == 64 ? NBX_WALK64_MINB : 3;
+    static constexpr int kThreads = CB <= 96 ? NBX_WALK64_THREADS : NBX_WALK128_THREADS;
+    static constexpr int kMinBlocks = CB <= 96 ? NBX_WALK64_MINB : NBX_WALK128_MINB;
 };
 
 template <int CB, int Mode, bool Pot, bool Rec>
@@ -579,6 +585,10 @@ int walk2_init(Ctx *ctx) {
     rc |= set_attr<128, 1, false>(ctx, smem_optin);
     rc |= set_attr<128, 2, false>(ctx, smem_optin);
     rc |= set_attr<128, 0, true>(ctx, smem_optin);
+    rc |= set_attr<96, 0, false>(ctx, smem_optin);
+    rc |= set_attr<96, 1, false>(ctx, smem_optin);
+    rc |= set_attr<96, 2, false>(ctx, smem_optin);
+    rc |= set_attr<96, 0, true>(ctx, smem_optin);
     rc |= set_attr<64, 0, false, true>(ctx, smem_optin);
     return rc;
 }
@@ -589,9 +599,10 @@ int walk2_record(Ctx *ctx, const nbx_state *s, int *rec_list, int *rec_len, int 
     return launch<64, 0, false, true>(ctx, s, nullptr, ctx->walk_warps, st, rec_list, rec_len, rec_cap);
 }
 
-// variant 0: 64-slot candidate buffers; variant 1: 128-slot buffers (<= 8 warps)
+// variant 0: 64-slot candidate buffers; 1: 128-slot buffers (<= 8 warps); 3: 96-slot buffers
 int walk2_forces(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st) {
     if (ctx->walk_variant == 1) return forces_cb<128>(ctx, s, pot, warps > 8 ? 8 : warps, st);
+    if (ctx->walk_variant == 3) return forces_cb<96>(ctx, s, pot, warps, st);
     return forces_cb<64>(ctx, s, pot, warps, st);
 }
 

@@ -56,7 +56,7 @@ CASES = {
 
 @pytest.mark.parametrize("name", list(CASES))
 @pytest.mark.parametrize("mac", ["theta0.5", "reference"])
-@pytest.mark.parametrize("variant", [0, 1, 2], ids=["walk64", "walk128", "walk1"])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3], ids=["walk64", "walk128", "walk1", "walk96"])
 def test_build_and_forces_match_oracle(cuda, name, mac, variant):
     b = CASES[name]()
     n = len(b.x)
@@ -269,7 +269,7 @@ def test_compensated_close_to_plain(cuda, mode):
 
 
 @pytest.mark.parametrize("warps", [4, 8, 16])
-@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("variant", [0, 1, 3])
 def test_walk_launch_shapes_agree(cuda, warps, variant):
     b = ic.plummer(5000)
     n = len(b.x)
