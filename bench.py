@@ -283,6 +283,15 @@ def bench_adjoint(args, local):
     return out
 
 
+def total_energy(ctx, s) -> float:
+    """K + W of the current state: K from the FP64 diagnostics, W = 1/2 sum m phi
+    with phi from a Barnes-Hut walk over a fresh tree (accumulated in FP64)."""
+    ctx.build(s)
+    phi = ctx.potential(s).astype(np.float64)
+    m = s.m.cpu().numpy().astype(np.float64)
+    return float(ctx.diagnostics(s)["kinetic"]) + 0.5 * float((m * phi).sum())
+
+
 def walk_traffic(n: int):
     """DRAM bytes (read + write) of one walk launch at this size, from the committed
     ncu summary of the benchmark workload (profiles/), or None for other sizes."""
@@ -405,18 +414,30 @@ def main():
     t_ref, e2 = ctx.constants()
     ctx.set_constants(t_ref, e2, False)
     diag0 = ctx.diagnostics(s)
+    energy0 = total_energy(ctx, s)
+    initial = [t.clone() for t in (s.x, s.y, s.z, s.vx, s.vy, s.vz)]
 
     # ---- plain FP32: warmup + timed
     timed(args.warmup)
     with Clocks(local) as clk:
         plain = timed(args.steps)
     clocks = clk.summary()
-    # ---- compensated FP32
+    energy1 = total_energy(ctx, s)
+    diag1 = ctx.diagnostics(s)
+    # ---- compensated FP32, the same steps from the same initial state
+    for t, c in zip((s.x, s.y, s.z, s.vx, s.vy, s.vz), initial):
+        t.copy_(c)
+    del initial
     ctx.set_constants(t_ref, e2, True)
-    timed(max(1, args.warmup // 2))
+    timed(args.warmup)
     comp = timed(args.steps)
     ctx.set_constants(t_ref, e2, False)
-    diag1 = ctx.diagnostics(s)
+    energy2 = total_energy(ctx, s)
+    nst = args.warmup + args.steps
+    energy = {"plain": {"steps": nst, "rel_drift": (energy1 - energy0) / abs(energy0)},
+              "compensated": {"steps": nst, "rel_drift": (energy2 - energy0) / abs(energy0)},
+              "e0": energy0, "how": "K (FP64 sum) + W = 1/2 sum m phi, phi from the Barnes-Hut walk; "
+                                    "both forms from the same initial state"}
 
     # ---- end to end through the public API with host buffers (pinned)
     host = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
@@ -476,6 +497,12 @@ def main():
             cpu = ref_cpu.cpu_baseline(n, THETA, EPS, DT)
         except Exception as e:  # noqa: BLE001 -- reported, never fatal
             cpu = {"unavailable": str(e)[:200]}
+        try:
+            cpu_serial = ref_cpu.bench_serial(n, THETA, EPS, DT, k=512)
+        except Exception as e:  # noqa: BLE001 -- reported, never fatal
+            cpu_serial = {"unavailable": str(e)[:200]}
+        if isinstance(cpu, dict) and cpu_serial is not None:
+            cpu["serial"] = cpu_serial
 
     line = {
         "metric": METRIC, "value": round(steps_per_s, 4), "unit": "steps/s", "n_gpus": world,
@@ -489,6 +516,7 @@ def main():
         "force_error_vs_fp64_direct": errs,
         "fp32_error_vs_fp64_same_lists": errs32,
         "frame": frame,
+        "energy_drift": energy,
         "interactions_per_step": inter_per_step,
         "opened_cells_per_step": plain["opened"],
         "walk_rounds_per_step": plain["rounds"],

@@ -1,4 +1,4 @@
-"""The reference's 3D/OpenMP tree code as the timed CPU baseline.
+"""The reference's 3D/OpenMP and 3D/Serial tree codes as the timed CPU baselines.
 
 TEST/BASELINE INFRASTRUCTURE ONLY.  ``stage()`` copies the reference's own
 sources (3D/OpenMP/OpenMP_NBody/src and include, minus the boost-dependent
@@ -9,7 +9,9 @@ main.cpp / ConfigParser.cpp and the renderer) into the git-ignored
   * Interaction.cpp:130 initialises the bounding box it otherwise reads
     uninitialised (`double xMin, ..., zMax = 0;`).
 The staged tree travels with the repository to the GPU host, where ``build()``
-compiles it (g++ -O3 -fopenmp) together with the harness.
+compiles it (g++ -O3 -fopenmp) together with the harness.  ``stage_serial()``
+does the same for 3D/Serial/NBody into ``oracle/_ref/serial/`` (Constants.h
+replaced by a shim with the same units), timed on one thread.
 """
 from __future__ import annotations
 
@@ -56,6 +58,67 @@ extern double BINARY_SEPARATION;
 #define DEBUG_INFO false
 #endif
 """
+
+
+REF_SERIAL = os.path.join(REF_ROOT, "3D", "Serial", "NBody")
+STAGE_SERIAL = os.path.join(HERE, "_ref", "serial")
+RUNNER_SERIAL = os.path.join(STAGE_SERIAL, "runner")
+HARNESS_SERIAL = os.path.join(HERE, "ref_shim", "serial_harness.cpp")
+
+SERIAL_CONSTANTS_SHIM = """#ifndef CONSTANTS_H_
+#define CONSTANTS_H_
+/* staged shim for 3D/Serial: G = dt^2 and TO_METERS = 1 make one reference
+ * step one kick-drift step of length dt with G = 1 (see serial_harness.cpp) */
+#ifndef NBX_DT
+#define NBX_DT 5e-4
+#endif
+const double PI = 3.14159265358979323846;
+const double TO_METERS = 1.0;
+const double G = (NBX_DT) * (NBX_DT);
+extern int NUM_BODIES;
+extern int NUM_SUNS;
+extern double SYSTEM_SIZE;
+extern double SOFTENING;
+extern double MAX_DISTANCE;
+const int TIME_STEP = 1;
+#define DEBUG_INFO false
+#endif
+"""
+
+
+def stage_serial() -> bool:
+    """Copy the reference's 3D/Serial sources into oracle/_ref/serial."""
+    if not os.path.isdir(REF_SERIAL):
+        return os.path.isdir(os.path.join(STAGE_SERIAL, "src"))
+    for sub in ("src", "include"):
+        d = os.path.join(STAGE_SERIAL, sub)
+        os.makedirs(d, exist_ok=True)
+        for fn in os.listdir(os.path.join(REF_SERIAL, sub)):
+            if fn in SKIP:
+                continue
+            shutil.copy(os.path.join(REF_SERIAL, sub, fn), os.path.join(d, fn))
+    with open(os.path.join(STAGE_SERIAL, "include", "Constants.h"), "w") as f:
+        f.write(SERIAL_CONSTANTS_SHIM)
+    return True
+
+
+def build_serial(dt: float = 5e-4) -> str | None:
+    if not stage_serial():
+        return None
+    srcs = sorted(os.path.join(STAGE_SERIAL, "src", f) for f in os.listdir(os.path.join(STAGE_SERIAL, "src"))
+                  if f.endswith(".cpp"))
+    stamp = os.path.join(STAGE_SERIAL, "dt.txt")
+    newest = max(os.path.getmtime(x) for x in srcs + [HARNESS_SERIAL])
+    if (os.path.exists(RUNNER_SERIAL) and os.path.getmtime(RUNNER_SERIAL) >= newest and os.path.exists(stamp)
+            and open(stamp).read() == repr(dt)):
+        return RUNNER_SERIAL
+    cmd = ["g++", "-O3", "-std=c++14", "-DNBX_DT=%r" % dt, "-I", os.path.join(STAGE_SERIAL, "include"),
+           HARNESS_SERIAL] + srcs + ["-o", RUNNER_SERIAL]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference Serial build failed:\n" + r.stderr[-3000:])
+    open(stamp, "w").write(repr(dt))
+    return RUNNER_SERIAL
 
 
 def stage() -> bool:
@@ -110,8 +173,8 @@ def _write_input(path, b, theta, eps, dt):
         np.asarray(b.m, np.float32).tofile(f)
 
 
-def run(b, theta, eps, dt, steps, warmup, mode="sample", k=65536, threads=None, seed=1):
-    runner = build(dt)
+def run(b, theta, eps, dt, steps, warmup, mode="sample", k=65536, threads=None, seed=1, code="omp"):
+    runner = build(dt) if code == "omp" else build_serial(dt)
     if runner is None:
         return None
     env = dict(os.environ)
@@ -153,6 +216,23 @@ def bench_openmp(n, steps, warmup, theta, eps, dt, k=16384):
             "phases_s": {"build": float(np.median([s[0] for s in res["steps"]])),
                          "force_scaled": float(np.median([s[1] for s in res["steps"]])),
                          "update": float(np.median([s[2] for s in res["steps"]]))}}
+
+
+def bench_serial(n, theta, eps, dt, k=1024, steps=1):
+    """The reference's 3D/Serial code on one core: serial tree build over all
+    bodies (timed once) + per step its force loop over k random bodies scaled by
+    n/k + its update."""
+    b = _workload(n)
+    res = run(b, theta, eps, dt, steps, 0, "sample", k, code="serial")
+    if res is None:
+        return None
+    per = [sum(x) for x in res["steps"]]
+    return {"value": 1.0 / float(np.median(per)), "unit": "steps/s", "cores": 1, "kind": "reference",
+            "sample": "reference 3D/Serial: tree build over all %d bodies (timed once) + force loop over %d "
+                      "random bodies scaled by n/k + update, one thread" % (n, k),
+            "phases_s": {"build": float(np.median([x[0] for x in res["steps"]])),
+                         "force_scaled": float(np.median([x[1] for x in res["steps"]])),
+                         "update": float(np.median([x[2] for x in res["steps"]]))}}
 
 
 def cpu_baseline(n, theta, eps, dt, k=4096):
