@@ -41,7 +41,7 @@ constexpr int kDfsReserve = 7 * 42 + 8;
 
 // Build-time tuning knobs of the evaluation loops (defaults are the measured best).
 #ifndef NBX_BODY_UNROLL
-#define NBX_BODY_UNROLL 8
+#define NBX_BODY_UNROLL 16
 #endif
 #ifndef NBX_CELL_UNROLL
 #define NBX_CELL_UNROLL 4
@@ -413,7 +413,8 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 float ra, rb;
                 upk(r, ra, rb);
                 const u64 ri = pk(rsq(ra), rsq(rb));
-                const u64 f = mul2(mul2(mul2(B.y, ri), ri), ri);
+                // no MAC depends on this product: (m ri)(ri ri) shortens its dependency chain
+                const u64 f = mul2(mul2(B.y, ri), mul2(ri, ri));
                 accumulate<Mode, Pot>(acc, f, B.y, ri, dx, dy, dz);
             }
             if (Rec) {  // every body candidate is an interaction
