@@ -241,7 +241,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     rc |= nbx::dmalloc(ctx, &ctx->d_arrive, NC);
     rc |= nbx::dmalloc(ctx, &ctx->d_fcl, (size_t)NC + Ss + 2);
     rc |= nbx::dmalloc(ctx, &ctx->d_cl, (size_t)NC + Ss + 2);
-    rc |= nbx::dmalloc(ctx, &ctx->d_hist, hist);
+    rc |= nbx::dmalloc(ctx, &ctx->d_hist, hist + 1);  // + the scanned total
     rc |= nbx::dmalloc(ctx, &ctx->d_scan_blk, ctx->cap_scan_blk);
     rc |= nbx::dmalloc(ctx, &ctx->d_totals, 8);
     rc |= nbx::dmalloc(ctx, &ctx->d_totals64, 4);
@@ -250,6 +250,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     if (rc == 0 && cudaMemset(ctx->d_status, 0, sizeof(nbx::DevStatus)) != cudaSuccess) rc = NBX_ERR_CUDA;
     if (rc == 0 && cudaMemset(ctx->d_totals, 0, 8 * sizeof(unsigned)) != cudaSuccess) rc = NBX_ERR_CUDA;
     if (rc == 0) rc = nbx::walk_init(ctx);
+    if (rc == 0) rc = nbx::radix_init(ctx);
     if (rc != 0) {
         nbx::free_all(ctx);
         delete ctx;

@@ -6,7 +6,8 @@
 //                   layout is segment-major, digit-major, tile-minor, the scan
 //                   value IS the absolute output offset of (segment, digit, tile)
 //   k_radix_scatter per-tile stable ranks (warp match + per-warp running
-//                   counters) and the scatter.
+//                   counters) into a shared-memory copy of the tile in output
+//                   order, then coalesced runs per digit.
 // Segments are the independent systems of a batch, so one launch sorts every
 // system's keys inside its own range; a single system is one segment.
 #include "nbx_internal.cuh"
@@ -66,20 +67,62 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     for (int d = lane; d < kRadixBins; d += 32) hist[hbase + (int64_t)d * hstride] = cnt[w][d];
 }
 
+// Scatter with the tile staged in shared memory in output order: every lane
+// ranks its key stably (warp match + running per-digit counters), writes it to
+// its tile-local sorted position, and the warp then streams the staged tile
+// out so that each digit's run is written by consecutive lanes to consecutive
+// addresses (coalesced, instead of one sector per key).  The tile's count of a
+// digit is the difference of adjacent entries of the scanned histogram (the
+// layout is tile-minor and the scan is continuous; offs[nh] holds the total).
+constexpr int kScatterWarps = 4;
+
+template <typename K, typename V>
+struct ScatterStage {
+    K key[kTile];
+    V val[kTile];
+    unsigned gbase[kRadixBins];   // output offset of (digit, tile)
+    unsigned lstart[kRadixBins];  // tile-local start of the digit
+    unsigned cnt[kRadixBins];     // running tile-local position
+};
+
 template <typename K, typename V, bool Seg>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+__global__ void __launch_bounds__(kScatterWarps * 32)
     k_radix_scatter(const K *__restrict__ key_in, K *__restrict__ key_out,
                     const V *__restrict__ val_in, V *__restrict__ val_out, TileMap tm, int shift,
                     const unsigned *__restrict__ offs) {
-    __shared__ unsigned cnt[kWarpsPerBlock][kRadixBins];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int t = blockIdx.x * kWarpsPerBlock + w;
+    const int t = blockIdx.x * kScatterWarps + w;
     if (t >= tm.ntiles) return;
     int start, len, hstride;
     int64_t hbase;
     tile_info<Seg>(tm, t, start, len, hbase, hstride);
     if (len <= 0) return;
-    for (int d = lane; d < kRadixBins; d += 32) cnt[w][d] = offs[hbase + (int64_t)d * hstride];
+    ScatterStage<K, V> &sg = reinterpret_cast<ScatterStage<K, V> *>(smem_raw)[w];
+    // lane owns digits 8*lane .. 8*lane+7: counts, then the tile-local starts
+    unsigned c[8], sum = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int d = 8 * lane + k;
+        const int64_t idx = hbase + (int64_t)d * hstride;
+        const unsigned g = offs[idx];
+        c[k] = offs[idx + 1] - g;
+        sg.gbase[d] = g;
+        sum += c[k];
+    }
+    unsigned incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    unsigned run = incl - sum;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        sg.lstart[8 * lane + k] = run;
+        sg.cnt[8 * lane + k] = run;
+        run += c[k];
+    }
     __syncwarp();
     const unsigned lt = (1u << lane) - 1u;
     constexpr int kBatch = 8;  // rounds whose loads are in flight together
@@ -98,20 +141,37 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
             if (j >= len) break;
             const bool valid = j + lane < len;
             const K k = kk[u];
-            unsigned d = valid ? ((unsigned)(k >> shift) & 0xffu) : (0x100u + lane);
-            unsigned peers = __match_any_sync(0xffffffffu, d);
-            unsigned rank = __popc(peers & lt);
-            unsigned base = valid ? cnt[w][d] : 0u;
+            const unsigned d = valid ? ((unsigned)(k >> shift) & 0xffu) : (0x100u + lane);
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            const unsigned rank = __popc(peers & lt);
+            const unsigned base = valid ? sg.cnt[d] : 0u;
             __syncwarp();
-            if (valid && rank == 0) cnt[w][d] = base + __popc(peers);
+            if (valid && rank == 0) sg.cnt[d] = base + __popc(peers);
             __syncwarp();
             if (valid) {
-                unsigned dst = base + rank;
-                key_out[dst] = k;
-                if (val_in) val_out[dst] = vv[u];
+                sg.key[base + rank] = k;
+                if (val_in) sg.val[base + rank] = vv[u];
             }
         }
     }
+    __syncwarp();
+    for (int j = lane; j < len; j += 32) {
+        const K k = sg.key[j];
+        const unsigned d = (unsigned)(k >> shift) & 0xffu;
+        const unsigned dst = sg.gbase[d] + ((unsigned)j - sg.lstart[d]);
+        key_out[dst] = k;
+        if (val_in) val_out[dst] = sg.val[j];
+    }
+}
+
+template <typename K, typename V, bool Seg>
+int launch_scatter(Ctx *ctx, int nt, const K *kin, K *kout, const V *vin, V *vout, const TileMap &tm, int shift,
+                   cudaStream_t st) {
+    const size_t smem = sizeof(ScatterStage<K, V>) * kScatterWarps;
+    k_radix_scatter<K, V, Seg><<<ceil_div(nt, kScatterWarps), kScatterWarps * 32, smem, st>>>(
+        kin, kout, vin, vout, tm, shift, ctx->d_hist);
+    ++ctx->launches;
+    return NBX_OK;
 }
 
 }  // namespace
@@ -131,11 +191,9 @@ int radix_sort_bodies(Ctx *ctx, cudaStream_t st) {
         k_radix_hist<unsigned long long, true>
             <<<grid, kWarpsPerBlock * 32, 0, st>>>(k0, tm, shift, ctx->d_hist);
         ++ctx->launches;
-        int rc = scan_exclusive_u32(ctx, ctx->d_hist, ctx->d_hist, nh, nullptr, nullptr, st);
+        int rc = scan_exclusive_u32(ctx, ctx->d_hist, ctx->d_hist, nh, nullptr, ctx->d_hist + nh, st);
         if (rc) return rc;
-        k_radix_scatter<unsigned long long, int, true>
-            <<<grid, kWarpsPerBlock * 32, 0, st>>>(k0, k1, v0, v1, tm, shift, ctx->d_hist);
-        ++ctx->launches;
+        launch_scatter<unsigned long long, int, true>(ctx, nt, k0, k1, v0, v1, tm, shift, st);
         std::swap(k0, k1);
         std::swap(v0, v1);
     }
@@ -153,12 +211,20 @@ int radix_sort_entries(Ctx *ctx, cudaStream_t st) {
     const int nh = nt * kRadixBins;
     k_radix_hist<unsigned, false><<<grid, kWarpsPerBlock * 32, 0, st>>>(ctx->d_ent, tm, 24, ctx->d_hist);
     ++ctx->launches;
-    int rc = scan_exclusive_u32(ctx, ctx->d_hist, ctx->d_hist, nh, nullptr, nullptr, st);
+    int rc = scan_exclusive_u32(ctx, ctx->d_hist, ctx->d_hist, nh, nullptr, ctx->d_hist + nh, st);
     if (rc) return rc;
-    k_radix_scatter<unsigned, int, false><<<grid, kWarpsPerBlock * 32, 0, st>>>(
-        ctx->d_ent, ctx->d_ent_alt, (const int *)nullptr, (int *)nullptr, tm, 24, ctx->d_hist);
-    ++ctx->launches;
+    launch_scatter<unsigned, int, false>(ctx, nt, ctx->d_ent, ctx->d_ent_alt, (const int *)nullptr, (int *)nullptr,
+                                         tm, 24, st);
     NBX_CUDA(cudaGetLastError());
+    return NBX_OK;
+}
+
+int radix_init(Ctx *ctx) {
+    NBX_CUDA(cudaFuncSetAttribute(k_radix_scatter<unsigned long long, int, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(sizeof(ScatterStage<unsigned long long, int>) * kScatterWarps)));
+    NBX_CUDA(cudaFuncSetAttribute(k_radix_scatter<unsigned, int, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(sizeof(ScatterStage<unsigned, int>) * kScatterWarps)));
     return NBX_OK;
 }
 

@@ -395,6 +395,9 @@ __global__ void __launch_bounds__(kBlock) k_nodes_b(const unsigned *__restrict__
 // [start(L), start(L+1)); start(L) is the scanned count of level-sort digit 4L.
 __global__ void __launch_bounds__(kBlock) k_moments_level(int level, const unsigned *__restrict__ lvl_off,
                                                            int ntiles, const unsigned *__restrict__ totals,
+                                                           const unsigned long long *__restrict__ totals64,
+                                                           const unsigned long long *__restrict__ flags_ex,
+                                                           const int *__restrict__ cl, int nsys,
                                                            const int *__restrict__ meta, float4 *node4,
                                                            double4 *sums, int *count, const DevStatus *st) {
     if (st->code != 0) return;  // an inconsistent tree is never summed
@@ -403,9 +406,15 @@ __global__ void __launch_bounds__(kBlock) k_moments_level(int level, const unsig
     unsigned end = lvl_off[(size_t)((level + 1) << 2) * ntiles];
     if (end > T) end = T;
     if (beg > end) beg = end;
-    for (unsigned b = beg + grid_stride_start(); b < end; b += grid_stride()) {
+    // the level's cells are a contiguous range of the BFS-ordered cell list:
+    // their ranks are the scanned cell flags at the level's first and end nodes
+    const unsigned ncell = (unsigned)(totals64[0] >> 32);
+    const unsigned cbeg = beg < T ? (unsigned)(flags_ex[beg] >> 32) : ncell;
+    const unsigned cend = end < T ? (unsigned)(flags_ex[end] >> 32) : ncell;
+    for (unsigned k = cbeg + grid_stride_start(); k < cend; k += grid_stride()) {
+        const int b = cl[nsys + k];
         const int pm = meta[b];
-        if (pm < 0) continue;  // body
+        if (pm < 0) continue;  // never: the list holds cells only
         const int first = pm & 0x0fffffff;
         const int nch = ((pm >> 28) & 7) + 1;
         double sm = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
@@ -496,8 +505,8 @@ int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox
     // cells exist at levels 1..41 (two bodies share at most 41 levels without error)
     for (int level = kMaxLevel - 2; level >= 1; level--) {
         k_moments_level<<<ctx->nsm * 4, kBlock, 0, st>>>(level, ctx->d_hist, ctx->cap_tiles_node, ctx->d_totals,
-                                                         ctx->d_meta, ctx->d_node4, ctx->d_sums, ctx->d_count,
-                                                         ctx->d_status);
+                                                         ctx->d_totals64, ctx->d_flags, ctx->d_cl, S, ctx->d_meta,
+                                                         ctx->d_node4, ctx->d_sums, ctx->d_count, ctx->d_status);
         ++ctx->launches;
     }
     NBX_CUDA(cudaGetLastError());
