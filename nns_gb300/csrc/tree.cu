@@ -152,13 +152,17 @@ __device__ __forceinline__ unsigned long long make_key(float px, float py, float
     return key;
 }
 
+// Also packs the bodies as float4 (x, y, z, m) in their original order, so that
+// the gather into sorted order reads one 16-byte record per body.
 __global__ void __launch_bounds__(kBlock) k_keys(const float *__restrict__ x, const float *__restrict__ y,
-                                                  const float *__restrict__ z, const int *__restrict__ body_sys,
+                                                  const float *__restrict__ z, const float *__restrict__ m,
+                                                  const int *__restrict__ body_sys,
                                                   const float *__restrict__ bbox, int n,
                                                   unsigned long long *__restrict__ key, int *__restrict__ val,
-                                                  DevStatus *st, int order) {
+                                                  float4 *__restrict__ pos4, DevStatus *st, int order) {
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         const float px = x[i], py = y[i], pz = z[i];
+        pos4[i] = make_float4(px, py, pz, m[i]);
         if (!isfinite(px) || !isfinite(py) || !isfinite(pz)) set_status(st, NBX_ERR_NONFINITE, i);
         const int s = body_sys[i];
         float bb[6];
@@ -231,8 +235,7 @@ __device__ __forceinline__ int delta_of(const unsigned long long *key, const uns
 }
 
 // Sorted bodies as float4 plus delta and the number of node entries per position.
-__global__ void __launch_bounds__(kBlock) k_delta(const float *__restrict__ x, const float *__restrict__ y,
-                                                   const float *__restrict__ z, const float *__restrict__ m,
+__global__ void __launch_bounds__(kBlock) k_delta(const float4 *__restrict__ pos4,
                                                    const int *__restrict__ body_sys, const int *__restrict__ sys_off,
                                                    int n, const unsigned long long *__restrict__ key,
                                                    const unsigned long long *__restrict__ key_lo,
@@ -247,8 +250,7 @@ __global__ void __launch_bounds__(kBlock) k_delta(const float *__restrict__ x, c
         const int dp = p > beg ? delta_of(key, key_lo, p - 1) : 0;
         delta[p] = (unsigned char)di;
         ecount[p] = (unsigned)((di > dp ? di - dp : 0) + 1);
-        const int b = val[p];
-        body4[p] = make_float4(x[b], y[b], z[b], m[b]);
+        body4[p] = pos4[val[p]];
         lvl_max = max(lvl_max, max(di, dp) + 1);
     }
     lvl_max = __reduce_max_sync(0xffffffffu, lvl_max);
@@ -467,15 +469,17 @@ int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox
                                            ctx->d_bbox64, ctx->d_depth0, ctx->d_status);
         ++ctx->launches;
     }
-    k_keys<<<gb, kBlock, 0, st>>>(s->x, s->y, s->z, ctx->d_body_sys, ctx->d_bbox, n, ctx->d_key,
-                                  ctx->d_val, ctx->d_status, ctx->key_order);
+    // the node array is free until the nodes are written: it holds the packed bodies
+    float4 *pos4 = ctx->d_node4;
+    k_keys<<<gb, kBlock, 0, st>>>(s->x, s->y, s->z, s->m, ctx->d_body_sys, ctx->d_bbox, n, ctx->d_key,
+                                  ctx->d_val, pos4, ctx->d_status, ctx->key_order);
     ++ctx->launches;
     int rc = radix_sort_bodies(ctx, st);
     if (rc) return rc;
     k_refine<<<gb, kBlock, 0, st>>>(s->x, s->y, s->z, ctx->d_body_sys, ctx->d_sys_off, ctx->d_bbox, n,
                                     ctx->d_key, ctx->d_key_lo, ctx->d_val, ctx->d_status, ctx->key_order);
     ++ctx->launches;
-    k_delta<<<gb, kBlock, 0, st>>>(s->x, s->y, s->z, s->m, ctx->d_body_sys, ctx->d_sys_off, n, ctx->d_key,
+    k_delta<<<gb, kBlock, 0, st>>>(pos4, ctx->d_body_sys, ctx->d_sys_off, n, ctx->d_key,
                                    ctx->d_key_lo, ctx->d_val, ctx->d_body4, ctx->d_delta, ctx->d_ecount,
                                    ctx->d_status);
     ++ctx->launches;

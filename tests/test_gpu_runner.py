@@ -1,0 +1,38 @@
+"""The command-line driver (nns_gb300/nbx_runner): the reference's main.cu flags,
+its TIME report (main.cu:125-181) and frames written like Renderer::createFrame
+(images/StepNNNNN.ppm every renderInterval steps, Renderer.cpp:149-158)."""
+import os
+import re
+import subprocess
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_runner_report_and_frames(cuda, tmp_path):
+    from nns_gb300 import build
+    build.build()
+    out = subprocess.run([build.RUNNER, "-n", "4096", "-i", "5", "-R", "2", "-r", "-v"], cwd=tmp_path,
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    text = out.stdout
+    for phase in ("reset arrays", "compute bounding boxes", "build tree", "compute COM", "sort",
+                  "compute forces", "update bodies", "copy from device to host"):
+        assert re.search(r"Time to %s: [0-9.e+-]+ms\n\tper step: [0-9.e+-]+ms" % phase, text), phase
+    assert "TOTAL TIME (without copying)" in text
+    assert "Number of particles: 4096" in text and "Number of iterations: 5" in text
+    assert len(re.findall(r"Elapsed time for step \d+", text)) == 5
+    frames = sorted(os.listdir(tmp_path / "images"))
+    assert frames == ["Step00001.ppm", "Step00002.ppm", "Step00003.ppm"]  # steps 0, 2, 4
+    data = open(tmp_path / "images" / "Step00001.ppm", "rb").read()
+    head = b"P6\n1024 1024\n255\n"
+    assert data.startswith(head) and len(data) == len(head) + 3 * 1024 * 1024
+    assert any(data[len(head):])  # something was drawn
+
+
+def test_runner_rejects_unknown_flag(cuda):
+    from nns_gb300 import build
+    build.build()
+    out = subprocess.run([build.RUNNER, "--no-such-flag"], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 2
