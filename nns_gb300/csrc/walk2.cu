@@ -60,7 +60,7 @@ constexpr int kDfsReserve = 7 * 42 + 8;
 #endif
 // representative bodies of a group tested against each child cell in the expand
 #ifndef NBX_MAC_REPS
-#define NBX_MAC_REPS 4
+#define NBX_MAC_REPS 2
 #endif
 static_assert(NBX_MAC_REPS >= 0 && NBX_MAC_REPS <= 4, "NBX_MAC_REPS must be 0..4");
 constexpr int kReps = NBX_MAC_REPS;
@@ -225,7 +225,8 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 }
             }
             // representatives: lane 0, the last body, the body nearest the box
-            // centre and the middle body (any lane's body is a valid choice)
+            // centre and the middle body, the first NBX_MAC_REPS of them tested
+            // (any lane's body is a valid choice)
             const float ex = me.x - 0.5f * (b[0] + b[1]), ey = me.y - 0.5f * (b[2] + b[3]);
             const float ez = me.z - 0.5f * (b[4] + b[5]);
             const unsigned key = __float_as_uint(ex * ex + ey * ey + ez * ez);
@@ -349,7 +350,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 const bool isc = ok && cm >= 0;
                 const float dpc = scale4(d0, lj);
                 bool sacc = false, srej = false;
-                if (isc) {
+                {  // on every lane, without a branch; the results are masked by isc below
                     const float4 lo = buf.cls[0], hi = buf.cls[1];
                     const float gx = fmaxf(0.f, fmaxf(__fsub_rn(lo.x, q.x), __fsub_rn(q.x, hi.x)));
                     const float gy = fmaxf(0.f, fmaxf(__fsub_rn(lo.y, q.y), __fsub_rn(q.y, hi.y)));
@@ -368,7 +369,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                         if (2 * k + 1 < kReps) srej |= rb < dpc;
                     }
                 }
-                const bool tob = ok && (cm < 0 || sacc);
+                const bool tob = ok && (cm < 0 || (isc && sacc));
                 const bool toc = isc && !sacc && !srej;
                 const bool tos = isc && !sacc && srej;
                 const unsigned bm = __ballot_sync(0xffffffffu, tob);
