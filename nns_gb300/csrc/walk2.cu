@@ -447,12 +447,14 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 const bool oka = __all_sync(0xffffffffu, dpa <= ra);
                 const bool okb = __all_sync(0xffffffffu, dpb <= rb);
 #endif
-                float ma, mb;
-                upk(B.y, ma, mb);
-                const u64 ri = pk(rsq(ra), rsq(rb));
-                const u64 mm = pk(oka ? ma : 0.f, okb ? mb : 0.f);
-                const u64 f = mul2(mul2(mul2(mm, ri), ri), ri);
-                accumulate<Mode, Pot>(acc, f, mm, ri, dx, dy, dz);
+                if (oka || okb) {  // warp-uniform: a pair of rejected cells adds nothing
+                    float ma, mb;
+                    upk(B.y, ma, mb);
+                    const u64 ri = pk(rsq(ra), rsq(rb));
+                    const u64 mm = pk(oka ? ma : 0.f, okb ? mb : 0.f);
+                    const u64 f = mul2(mul2(mul2(mm, ri), ri), ri);
+                    accumulate<Mode, Pot>(acc, f, mm, ri, dx, dy, dz);
+                }
                 if (!oka) {
                     if (lane == 0) stack[top + nrej] = buf.cid[2 * q];
                     nrej++;
