@@ -6,8 +6,7 @@
 // floor(py)+j), i, j in [-dot/2, dot/2), with weight
 //   brightness / ((exp((s a_i)^2) + exp((s b_j)^2))^0.75 + 1),
 //   a_i = floor(px)+i-px, b_j = floor(py)+j-py.
-// The weights are FP32 (an 8-bit output needs far less); the 2*dot
-// exponentials are shared by the dot's rows and columns and the power is
+// The weights are FP32 (an 8-bit output needs far less) and the power is
 // exp2(0.75 log2(.)).  Bodies are visited in the tree's sorted order when the
 // context holds a tree for them, so a block's 256 consecutive bodies cover a
 // small pixel window: that window is accumulated with shared-memory atomics
@@ -87,35 +86,24 @@ __global__ void __launch_bounds__(kSplatBlock) k_splat(const float *__restrict__
             for (int k = threadIdx.x; k < 3 * ww * wh; k += kSplatBlock) win[k] = 0.f;
         __syncthreads();
         if (draw) {
-            float ey[kMaxDot];
-#pragma unroll
-            for (int j = 0; j < kMaxDot; j++) {
-                if (j < nd) {
-                    const float t = rc.sharp * (float)((double)(yp - half + j) - pys);
-                    ey[j] = expf(t * t);
-                }
-            }
+            // lanes start their rows at different offsets, so lanes drawing the
+            // same dot centre (dense regions) add to different pixels at a time
+            const int rot = nd > 0 ? (threadIdx.x & 31) % nd : 0;
             for (int i = 0; i < nd; i++) {
-                const float t = rc.sharp * (float)((double)(xp - half + i) - pxs);
-                const float ex = expf(t * t);
+                const float tx = rc.sharp * (float)((double)(xp - half + i) - pxs);
+                const float ex = expf(tx * tx);
                 const int gx = xp - half + i;
-#pragma unroll
-                for (int j = 0; j < kMaxDot; j++) {
-                    if (j < nd) {
-                        const float f = rc.bright / (exp2f(0.75f * __log2f(ex + ey[j])) + 1.0f);
-                        const int gy = yp - half + j;
-                        if (local) {
-                            float *q = &win[3 * ((gy - wy0) * ww + (gx - wx0))];
-                            atomicAdd(q + 0, cr * f);
-                            atomicAdd(q + 1, cg * f);
-                            atomicAdd(q + 2, cb * f);
-                        } else {
-                            float *q = &accum[3 * ((size_t)gy * rc.w + gx)];
-                            atomicAdd(q + 0, cr * f);
-                            atomicAdd(q + 1, cg * f);
-                            atomicAdd(q + 2, cb * f);
-                        }
-                    }
+                int j = rot;
+                for (int jj = 0; jj < nd; jj++) {
+                    const float ty = rc.sharp * (float)((double)(yp - half + j) - pys);
+                    const float f = rc.bright / (exp2f(0.75f * __log2f(ex + expf(ty * ty))) + 1.0f);
+                    const int gy = yp - half + j;
+                    float *q = local ? &win[3 * ((gy - wy0) * ww + (gx - wx0))]
+                                     : &accum[3 * ((size_t)gy * rc.w + gx)];
+                    atomicAdd(q + 0, cr * f);
+                    atomicAdd(q + 1, cg * f);
+                    atomicAdd(q + 2, cb * f);
+                    j = j + 1 == nd ? 0 : j + 1;
                 }
             }
         }
