@@ -74,7 +74,7 @@ SERIAL_CONSTANTS_SHIM = """#ifndef CONSTANTS_H_
 #endif
 const double PI = 3.14159265358979323846;
 const double TO_METERS = 1.0;
-const double G = (NBX_DT) * (NBX_DT);
+extern double G;  /* dt^2 for timed steps, 1 for force checks (set by the harness) */
 extern int NUM_BODIES;
 extern int NUM_SUNS;
 extern double SYSTEM_SIZE;
@@ -233,6 +233,23 @@ def bench_serial(n, theta, eps, dt, k=1024, steps=1):
             "phases_s": {"build": float(np.median([x[0] for x in res["steps"]])),
                          "force_scaled": float(np.median([x[1] for x in res["steps"]])),
                          "update": float(np.median([x[2] for x in res["steps"]]))}}
+
+
+def serial_forces(b, theta, eps):
+    """Accelerations (n, 3) of the reference's 3D/Serial tree code with G = 1
+    (its MAC length/|d| < theta and softening (d^2+eps^2) d), or None where the
+    code is not staged."""
+    runner = build_serial()
+    if runner is None:
+        return None
+    n = len(b.x)
+    with tempfile.TemporaryDirectory() as td:
+        inp, out = os.path.join(td, "in.bin"), os.path.join(td, "acc.bin")
+        _write_input(inp, b, theta, eps, 1.0)
+        r = subprocess.run([runner, "forces", inp, out], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference serial runner failed: %s" % r.stderr[-2000:])
+        return np.fromfile(out, np.float64).reshape(n, 3)
 
 
 def cpu_baseline(n, theta, eps, dt, k=4096):

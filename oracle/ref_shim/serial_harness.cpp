@@ -10,6 +10,8 @@
  * code's root is the fixed cube 60 * SYSTEM_SIZE (Interaction.cpp:122-125);
  * SYSTEM_SIZE is set so that this cube is the bodies' extent.
  *
+ *   forces <in> <out>  the reference's tree build and force loop over all bodies
+ *          with G = 1; writes the accelerations (n x 3 float64) to <out>.
  *   sample <in> <steps> <warmup> <k> <seed>  the reference's serial tree build
  *          over ALL bodies (Interaction.cpp:122-134), timed once; then per step
  *          the reference's force loop (:153-160) over k sampled bodies and its
@@ -28,6 +30,10 @@
 #include <random>
 #include <vector>
 
+#ifndef NBX_DT
+#define NBX_DT 5e-4
+#endif
+double G = (NBX_DT) * (NBX_DT);
 int NUM_BODIES = 0;
 int NUM_SUNS = 0;
 double SYSTEM_SIZE = 1.0;
@@ -40,8 +46,9 @@ static double now() {
 }
 
 int main(int argc, char **argv) {
-    if (argc < 7 || std::strcmp(argv[1], "sample") != 0) {
-        std::fprintf(stderr, "usage: %s sample <in> <steps> <warmup> <k> <seed>\n", argv[0]);
+    const bool forces = argc == 4 && std::strcmp(argv[1], "forces") == 0;
+    if (!forces && (argc < 7 || std::strcmp(argv[1], "sample") != 0)) {
+        std::fprintf(stderr, "usage: %s sample <in> <steps> <warmup> <k> <seed> | forces <in> <out>\n", argv[0]);
         return 2;
     }
     FILE *f = std::fopen(argv[2], "rb");
@@ -53,9 +60,9 @@ int main(int argc, char **argv) {
     std::vector<float> a(7 * (size_t)n);
     if (std::fread(a.data(), sizeof(float), a.size(), f) != a.size()) return 3;
     std::fclose(f);
-    const int steps = std::atoi(argv[3]), warmup = std::atoi(argv[4]);
-    const int k = std::atoi(argv[5]);
-    const unsigned seed = (unsigned)std::atoi(argv[6]);
+    const int steps = forces ? 0 : std::atoi(argv[3]), warmup = forces ? 0 : std::atoi(argv[4]);
+    const int k = forces ? 0 : std::atoi(argv[5]);
+    const unsigned seed = forces ? 1u : (unsigned)std::atoi(argv[6]);
     NUM_BODIES = n;
     MAX_DISTANCE = hdr[0];
     SOFTENING = hdr[1];
@@ -78,6 +85,25 @@ int main(int argc, char **argv) {
     Interaction handler(false);
     LOGCFG.level = ERROR;
     LOGCFG.headers = false;
+    if (forces) {
+        /* Interaction.cpp:122-160 without the update: G = 1, accelerations of all
+         * bodies read before updateBodies would zero them */
+        G = 1.0;
+        Tree *tree = new Tree(Octant(0.0, 0.0, 0.0, 60.0 * SYSTEM_SIZE));
+        for (int i = 0; i < n; i++)
+            if (tree->getOctant().contains(bods[i].position)) tree->insert(&bods[i]);
+        for (int i = 0; i < n; i++)
+            if (tree->getOctant().contains(bods[i].position)) handler.treeInteraction(tree, &bods[i]);
+        delete tree;
+        FILE *o = std::fopen(argv[3], "wb");
+        if (!o) return 3;
+        for (int i = 0; i < n; i++) {
+            const double acc[3] = {bods[i].acceleration.x, bods[i].acceleration.y, bods[i].acceleration.z};
+            std::fwrite(acc, sizeof(double), 3, o);
+        }
+        std::fclose(o);
+        return 0;
+    }
     std::printf("{\"threads\": 1, \"n\": %d, \"mode\": \"sample\", \"steps\": [", n);
     std::mt19937 rng(seed);
     /* Interaction.cpp:122-134: fixed root cube, serial inserts; built once */

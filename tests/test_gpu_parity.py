@@ -373,7 +373,9 @@ def test_kernels_wrapper_sequence(cuda):
 
 
 def test_plummer_2p20_properties(cuda):
-    """The 2^20-body Plummer workload: exact tree, forces on sampled groups."""
+    """The 2^20-body Plummer workload (theta 0.6, eps 0.005): exact keys, permutation
+    and tree, forces and list lengths on sampled groups, and the error against an
+    FP64 direct sum on 4096 targets."""
     b = ic.plummer(1 << 20)
     n = len(b.x)
     ctx = _ctx(n, theta=0.6, eps=0.005)
@@ -392,6 +394,14 @@ def test_plummer_2p20_properties(cuda):
     assert np.median(rel) <= MED_TOL and rel.max() <= MAX_TOL
     nl, _ = ctx.walk_stats()
     assert np.array_equal(nl[idx], f.nlist[idx])
+    keys, perm = ctx.export_keys()
+    hi, _ = O.keys(b.x, b.y, b.z, ot.bbox, 21)
+    assert np.array_equal(perm, ot.perm) and np.array_equal(keys, hi[ot.perm])
+    # the Barnes-Hut error itself, against an FP64 direct sum on 4096 uniform targets
+    targets = np.random.default_rng(2).choice(n, 4096, replace=False).astype(np.int32)
+    direct = O.direct_fp64(b.x, b.y, b.z, b.m, e2, targets)
+    err = _rel(s.acc()[targets], direct)
+    assert np.median(err) < 5e-3 and np.percentile(err, 99) < 5e-2, (np.median(err), np.percentile(err, 99))
 
 
 def test_autotune_picks_a_valid_config(cuda, tmp_path, monkeypatch):
