@@ -43,6 +43,7 @@ extern "C" {
 #define NBX_ERR_STATE 9     /* call out of order (e.g. forces before a build) */
 #define NBX_ERR_NOMEM 10    /* device allocation failed */
 #define NBX_ERR_SCRATCH 11  /* request larger than the static scratch of a no-allocation entry point */
+#define NBX_ERR_FORMAT 12   /* checkpoint header, size or checksum mismatch */
 
 typedef struct nbx_ctx nbx_ctx;
 
@@ -74,6 +75,8 @@ typedef struct nbx_params {
     int key_order;     /* 0: the reference's body order (Lebesgue keys; bit-exact parity);
                           1: Hilbert keys -- same cells, siblings reordered, so walk groups
                           are compact but the interaction lists differ from the reference */
+    int node_capacity; /* node pool (cells + bodies); 0: 2*max_bodies + 65536.  A tree that
+                          needs more nodes reports NBX_ERR_CAPACITY */
 } nbx_params;
 
 /* SoA device state of all systems; systems are contiguous ranges. */
@@ -239,6 +242,24 @@ int nbx_adjoint_stats(nbx_adjoint *adj, int64_t *bytes, float *forward_ms, float
 /* FP64 diagnostics of bodies [0,n): out[0..2] momentum, out[3] kinetic energy,
  * out[4..6] angular momentum, out[7] total mass (device double[8]). */
 int nbx_diagnostics_fp64(nbx_ctx *ctx, const nbx_state *s, int n, double *out, void *stream);
+
+/* ---- checkpoint / resume -------------------------------------------------
+ * The reference has none (it only writes frames).  A checkpoint is a raw dump
+ * of every system's bodies (x, y, z, vx, vy, vz, m: the state a kick-drift step
+ * needs) plus the system offsets and the step's constants (MAC constant,
+ * softening, dt, dampening, compensation, key order), into a caller-owned host
+ * buffer: a versioned header, the offsets, the seven float arrays, and 64-bit
+ * checksums of header and payload.  Restoring it into a context (capacity
+ * permitting) sets the systems and constants and copies the bodies into the
+ * caller's device state, so that the run continues bit for bit. */
+int64_t nbx_checkpoint_bytes(int64_t nbodies, int nsystems);
+/* Synchronises `stream`; *written receives the bytes used. */
+int nbx_checkpoint_save(nbx_ctx *ctx, const nbx_state *s, void *host, int64_t capacity, int64_t *written,
+                        void *stream);
+/* NBX_ERR_FORMAT on a bad header, size or checksum (nothing is changed then);
+ * NBX_ERR_ARG when the context is too small for it or uses another key order.
+ * Synchronises `stream`. */
+int nbx_checkpoint_restore(nbx_ctx *ctx, nbx_state *s, const void *host, int64_t bytes, void *stream);
 
 /* ---- headless frame ------------------------------------------------------
  * The reference renderer's velocity-coloured dot splat

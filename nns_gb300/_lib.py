@@ -15,7 +15,7 @@ NBX_OK = 0
 STATUS_NAMES = {
     0: "NBX_OK", 1: "NBX_ERR_ARG", 2: "NBX_ERR_CUDA", 3: "NBX_ERR_DEPTH", 4: "NBX_ERR_CAPACITY",
     5: "NBX_ERR_STACK", 6: "NBX_ERR_NONFINITE", 7: "NBX_ERR_CLUSTER", 8: "NBX_ERR_TIMEOUT",
-    9: "NBX_ERR_STATE", 10: "NBX_ERR_NOMEM", 11: "NBX_ERR_SCRATCH",
+    9: "NBX_ERR_STATE", 10: "NBX_ERR_NOMEM", 11: "NBX_ERR_SCRATCH", 12: "NBX_ERR_FORMAT",
 }
 
 
@@ -26,7 +26,7 @@ class nbx_params(C.Structure):
                 ("group", C.c_int), ("stack_depth", C.c_int), ("compensated", C.c_int),
                 ("leaf_size", C.c_int), ("radix_bits", C.c_int), ("walk_warps", C.c_int),
                 ("device", C.c_int), ("block_size", C.c_int), ("grid_size", C.c_int),
-                ("walk_variant", C.c_int), ("key_order", C.c_int)]
+                ("walk_variant", C.c_int), ("key_order", C.c_int), ("node_capacity", C.c_int)]
 
 
 class nbx_state(C.Structure):
@@ -86,6 +86,9 @@ SIGNATURES = {
     "nbx_forces_fp64_lists": (_I, [_P, _P, _I, _P, _P]),
     "nbx_diagnostics_fp64": (_I, [_P, C.POINTER(nbx_state), _I, _P, _P]),
     "nbx_render_params_default": (None, [C.POINTER(nbx_render_params)]),
+    "nbx_checkpoint_bytes": (C.c_int64, [C.c_int64, _I]),
+    "nbx_checkpoint_save": (_I, [_P, C.POINTER(nbx_state), _P, C.c_int64, C.POINTER(C.c_int64), _P]),
+    "nbx_checkpoint_restore": (_I, [_P, C.POINTER(nbx_state), _P, C.c_int64, _P]),
     "nbx_render_frame": (_I, [_P, C.POINTER(nbx_state), _I, C.POINTER(nbx_render_params), _P, _P, _P]),
     "nbx_adjoint_create": (_I, [_P, _I, _I, _I, _I, C.POINTER(_P)]),
     "nbx_adjoint_destroy": (_I, [_P]),

@@ -40,7 +40,7 @@ class Context:
     def __init__(self, max_bodies: int, max_systems: int = 1, theta: float = 0.5,
                  theta_ref: float | None = None, eps: float = 0.05, eps2: float | None = None,
                  dt: float = 1e-3, dampening: float = 1.0, compensated: int = 0,
-                 stack_depth: int = 512, device: int = 0, key_order: int = 0):
+                 stack_depth: int = 512, device: int = 0, key_order: int = 0, node_capacity: int = 0):
         p = L.nbx_params()
         lib().nbx_params_default(C.byref(p))
         p.max_bodies = int(max_bodies)
@@ -53,6 +53,7 @@ class Context:
         p.dampening = dampening
         p.compensated = int(compensated)
         p.stack_depth = stack_depth
+        p.node_capacity = node_capacity
         p.device = device
         p.key_order = int(key_order)
         self.params = p
@@ -200,6 +201,24 @@ class Context:
         check(lib().nbx_potential(self.h, C.byref(s.c), _ptr(phi), _stream_ptr(stream)),
               "nbx_potential", self.h)
         return phi.cpu().numpy()
+
+    def checkpoint(self, s: "State", stream=None) -> np.ndarray:
+        """Raw checkpoint of every system's bodies and the step constants (uint8 array)."""
+        n = int(self.offsets[-1])
+        nbytes = lib().nbx_checkpoint_bytes(n, len(self.offsets) - 1)
+        buf = np.empty(nbytes, np.uint8)
+        written = C.c_int64()
+        check(lib().nbx_checkpoint_save(self.h, C.byref(s.c), buf.ctypes.data_as(C.c_void_p), nbytes,
+                                        C.byref(written), _stream_ptr(stream)), "nbx_checkpoint_save", self.h)
+        return buf[: written.value]
+
+    def restore(self, s: "State", buf, stream=None) -> None:
+        """Restores a checkpoint into this context (systems, constants) and s (bodies)."""
+        b = np.ascontiguousarray(np.frombuffer(buf, np.uint8) if not isinstance(buf, np.ndarray) else buf, np.uint8)
+        check(lib().nbx_checkpoint_restore(self.h, C.byref(s.c), b.ctypes.data_as(C.c_void_p), b.size,
+                                           _stream_ptr(stream)), "nbx_checkpoint_restore", self.h)
+        nsys = int(np.frombuffer(b[12:16].tobytes(), np.int32)[0])
+        self.offsets = [int(v) for v in np.frombuffer(b[56:56 + 8 * (nsys + 1)].tobytes(), np.int64)]
 
     def diagnostics(self, s: "State", n: int | None = None, stream=None):
         out = torch.zeros(8, dtype=torch.float64, device=self.device)

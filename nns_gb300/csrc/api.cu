@@ -159,6 +159,7 @@ const char *nbx_status_string(int s) {
         case NBX_ERR_STATE: return "call out of order or inconsistent tree";
         case NBX_ERR_NOMEM: return "device allocation failed";
         case NBX_ERR_SCRATCH: return "request exceeds the static scratch of a no-allocation entry point";
+        case NBX_ERR_FORMAT: return "checkpoint header, size or checksum mismatch";
         default: return "unknown status";
     }
 }
@@ -196,7 +197,11 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     const int B = p->max_bodies, Ss = p->max_systems;
     ctx->cap_bodies = B;
     ctx->cap_sys = Ss;
-    const int64_t nc = 2ll * B + 65536;
+    if (p->node_capacity != 0 && (p->node_capacity < B + 1 || p->node_capacity > nbx::kMaxNodes)) {
+        delete ctx;
+        return NBX_ERR_ARG;
+    }
+    const int64_t nc = p->node_capacity ? (int64_t)p->node_capacity : 2ll * B + 65536;
     ctx->cap_nodes = (int)(nc < nbx::kMaxNodes ? nc : nbx::kMaxNodes);
     ctx->cap_tiles_body = B / nbx::kTile + Ss + 1;
     ctx->cap_tiles_node = nbx::ceil_div(ctx->cap_nodes, nbx::kTile);
@@ -553,6 +558,10 @@ int nbx_sync_status(nbx_ctx *c, void *stream) {
         ctx->last_error = buf;
         int zero[2] = {0, 0};
         NBX_CUDA(cudaMemcpy(ctx->d_status, zero, sizeof(zero), cudaMemcpyHostToDevice));
+        // the tree of a step that reported an error may be inconsistent: it is
+        // never walked again, the next walk needs a new build
+        ctx->built = false;
+        ctx->ref_m = 0;
     }
     return code;
 }

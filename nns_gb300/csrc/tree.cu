@@ -366,8 +366,9 @@ __global__ void __launch_bounds__(kBlock) k_nodes_b(const unsigned *__restrict__
                                                      int *__restrict__ root_nch, DevStatus *st) {
     const int T = (int)totals[1];
     for (int s = grid_stride_start(); s < nsys; s += grid_stride()) {
-        root_first[s] = fcl[s];
-        root_nch[s] = fcl[s + 1] - fcl[s];
+        const bool ok = st->code == 0;  // a failed build leaves empty roots
+        root_first[s] = ok ? fcl[s] : 0;
+        root_nch[s] = ok ? fcl[s + 1] - fcl[s] : 0;
     }
     for (int b = grid_stride_start(); b < T; b += grid_stride()) {
         int p, l;

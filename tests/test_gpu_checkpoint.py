@@ -1,0 +1,94 @@
+"""Checkpoint / resume (nbx_checkpoint_*) and the node-pool overflow guard.
+
+* A run resumed from a checkpoint continues bit for bit (batched systems,
+  compensated forces).
+* A corrupted or truncated checkpoint is refused with NBX_ERR_FORMAT and
+  changes nothing; a context too small for it is refused with NBX_ERR_ARG.
+* A tree larger than the node pool reports NBX_ERR_CAPACITY; the failed tree is
+  never walked (NBX_ERR_STATE until a new build), and systems that fit the pool
+  still work.
+"""
+import numpy as np
+import pytest
+
+from nns_gb300 import ic
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(ctx, s, k):
+    ctx.step(s, k)
+    ctx.sync()
+    return np.stack([t.cpu().numpy() for t in (s.x, s.y, s.z, s.vx, s.vy, s.vz)])
+
+
+def test_resume_is_bit_exact(cuda):
+    from nns_gb300.barnes_hut import Context, State
+    bodies, off = ic.batched_star_disks(3, seed=ic.SEED0 + 40)
+    n = int(off[-1])
+    ctx = Context(max_bodies=n, max_systems=3, theta=0.5, eps=0.01, dt=1e-3, compensated=1)
+    ctx.set_systems(off)
+    s = State.from_bodies(bodies)
+    _run(ctx, s, 3)
+    buf = ctx.checkpoint(s)
+    want = _run(ctx, s, 4)
+    ctx2 = Context(max_bodies=n + 100, max_systems=4, theta=0.9, eps=0.2, dt=5e-2)
+    s2 = State.empty(n)
+    ctx2.restore(s2, buf)
+    assert ctx2.offsets == [int(v) for v in off]
+    assert ctx2.constants() == ctx.constants()
+    got = _run(ctx2, s2, 4)
+    assert np.array_equal(got, want)
+
+
+def test_bad_checkpoints_are_refused(cuda):
+    from nns_gb300._lib import NbxError
+    from nns_gb300.barnes_hut import Context, State
+    b = ic.star_disk(2000)
+    ctx = Context(max_bodies=2000)
+    ctx.set_systems([0, 2000])
+    s = State.from_bodies(b)
+    buf = ctx.checkpoint(s)
+    x0 = s.x.cpu().numpy().copy()
+    for pos, bit in ((20, 1), (5000, 4), (0, 2)):  # header field, payload, magic
+        bad = buf.copy()
+        bad[pos] ^= bit
+        s.x.fill_(7.0)
+        with pytest.raises(NbxError) as e:
+            ctx.restore(s, bad)
+        assert e.value.code == 12  # NBX_ERR_FORMAT
+        assert float(s.x[0].item()) == 7.0  # nothing was copied
+    with pytest.raises(NbxError) as e:
+        ctx.restore(s, buf[:-8])
+    assert e.value.code == 12
+    small = Context(max_bodies=1000)
+    with pytest.raises(NbxError) as e:
+        small.restore(State.empty(1000), buf)
+    assert e.value.code == 1  # NBX_ERR_ARG
+    ctx.restore(s, buf)
+    assert np.array_equal(s.x.cpu().numpy(), x0)
+
+
+def test_node_pool_overflow_is_reported(cuda):
+    from nns_gb300._lib import NbxError
+    from nns_gb300.barnes_hut import Context, State
+    b = ic.star_disk(1000)
+    ctx = Context(max_bodies=1000, node_capacity=1001)
+    ctx.set_systems([0, 1000])
+    s = State.from_bodies(b)
+    ctx.build(s)
+    ctx.forces(s)
+    with pytest.raises(NbxError) as e:
+        ctx.sync()
+    assert e.value.code == 4  # NBX_ERR_CAPACITY
+    with pytest.raises(NbxError) as e:  # the failed tree is never walked
+        ctx.forces(s)
+    assert e.value.code == 9  # NBX_ERR_STATE
+    small = ic.star_disk(50)
+    s2 = State.from_bodies(small)
+    ctx.set_systems([0, 50])
+    ctx.build(s2)
+    ctx.forces(s2)
+    ctx.sync()
+    a = s2.acc()
+    assert np.isfinite(a).all() and np.abs(a).sum() > 0
