@@ -6,6 +6,16 @@
 #include <vector>
 
 #include "nbx_internal.cuh"
+#include "nvtx3/nvToolsExt.h"
+
+namespace {
+// NVTX range around an entry point: phases show up by name in a profiler's
+// timeline (near-free when no tool is attached)
+struct Range {
+    explicit Range(const char *name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+};
+}  // namespace
 
 namespace nbx {
 int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox, const float *const *bbox_ptrs);
@@ -464,6 +474,7 @@ static int check_state(Ctx *ctx, const nbx_state *s) {
 
 int nbx_build(nbx_ctx *c, const nbx_state *s, void *stream) {
     if (!c) return NBX_ERR_ARG;
+    Range r("nbx_build");
     int rc = check_state(C(c), s);
     if (rc) return rc;
     return nbx::build_tree(C(c), s, S(stream), false, nullptr);
@@ -471,16 +482,19 @@ int nbx_build(nbx_ctx *c, const nbx_state *s, void *stream) {
 
 int nbx_forces(nbx_ctx *c, const nbx_state *s, void *stream) {
     if (!c || !s || !s->ax || !s->ay || !s->az) return NBX_ERR_ARG;
+    Range r("nbx_forces");
     return nbx::walk_forces(C(c), s, S(stream));
 }
 
 int nbx_integrate(nbx_ctx *c, const nbx_state *s, void *stream) {
     if (!c || !s || !s->vx || !s->ax) return NBX_ERR_ARG;
+    Range r("nbx_integrate");
     Ctx *ctx = C(c);
     return nbx::integrate(ctx, s, ctx->p.dt, ctx->p.dampening, (int)ctx->nbodies, S(stream));
 }
 
 static int one_step(Ctx *ctx, const nbx_state *s, cudaStream_t st) {
+    Range r("nbx_step");
     int rc = nbx::build_tree(ctx, s, st, false, nullptr);
     if (rc) return rc;
     rc = nbx::walk_forces(ctx, s, st);
@@ -503,6 +517,7 @@ int nbx_step(nbx_ctx *c, const nbx_state *s, int nsteps, void *stream) {
 
 int nbx_graph_step(nbx_ctx *c, const nbx_state *s, int nsteps, void *stream) {
     if (!c || nsteps < 0) return NBX_ERR_ARG;
+    Range r("nbx_graph_step");
     Ctx *ctx = C(c);
     int rc = check_state(ctx, s);
     if (rc) return rc;
