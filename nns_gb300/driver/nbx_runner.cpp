@@ -10,8 +10,9 @@
 //   -r, --render            write a frame every renderinterval steps to images/StepNNNNN.ppm
 //                           (Renderer::createFrame, Renderer.cpp:37-161, through nbx_render_frame)
 //   -v                      verbosity (repeat)
-//   --model ref-disk|disk|plummer   initial conditions (ref-disk: the recipe of
-//                           BarnesHut::diskModel, BarnesHut.cu:356-415)
+//   --model ref-disk|ref-plummer|disk|plummer   initial conditions (ref-disk and
+//                           ref-plummer: the recipes of BarnesHut::diskModel and
+//                           BarnesHut::plummerModel, BarnesHut.cu:304-415)
 //   --theta-ref X --eps2 X  MAC constant and squared softening (Kernels.cu:17-18 defaults)
 //   --seed N
 #include <sys/stat.h>
@@ -69,6 +70,37 @@ Bodies ref_disk(int n, uint64_t seed) {
     return b;
 }
 
+// BarnesHut::plummerModel (BarnesHut.cu:304-354; present but not called by the
+// reference): unit masses, r = a / sqrt(u^-2/3 - 1) in the x-y plane, z = +-i*1e-3,
+// in-plane speed 100 q sqrt(2) (1 + r^2)^-1/4 with q by rejection on
+// q^2 (1 - q^2)^3.5 (bound 0.1).
+Bodies ref_plummer(int n, uint64_t seed) {
+    Bodies b(n);
+    const double pi = 3.14159265358979323846;
+    for (int i = 0; i < n; i++) {
+        const double phi = 2 * pi * uniform(seed, i, 0);
+        const double u = std::max(uniform(seed, i, 1), 1e-12);
+        const double r = 1.0 / std::sqrt(std::pow(u, -0.666666) - 1.0);
+        b.m[i] = 1.f;
+        b.x[i] = (float)(r * std::cos(phi));
+        b.y[i] = (float)(r * std::sin(phi));
+        b.z[i] = (float)((i % 2 == 0 ? 1e-3 : -1e-3) * i);
+        double q = 0.0;
+        for (int d = 2; d < 4000; d += 2) {
+            const double qq = uniform(seed, i, d), tt = 0.1 * uniform(seed, i, d + 1);
+            if (tt <= qq * qq * std::pow(1 - qq * qq, 3.5)) {
+                q = qq;
+                break;
+            }
+        }
+        const double v = 100 * q * std::sqrt(2.0) * std::pow(1 + r * r, -0.25);
+        const double ph2 = 2 * pi * uniform(seed, i, 4001);
+        b.vx[i] = (float)(v * std::cos(ph2));
+        b.vy[i] = (float)(v * std::sin(ph2));
+    }
+    return b;
+}
+
 // The star + disk workload (mass-1 star, disk bodies of mass 1e-6, r in [0.1, 1]).
 Bodies star_disk(int n, uint64_t seed) {
     Bodies b(n);
@@ -122,7 +154,7 @@ Bodies plummer(int n, uint64_t seed) {
 
 void usage() {
     std::printf("./nbx_runner [-i iterations] [-n particles] [-b blocksize] [-g gridsize] [-R renderinterval]\n"
-                "             [-r] [-v...] [--model ref-disk|disk|plummer] [--theta-ref X] [--eps2 X] [--seed N]\n");
+                "             [-r] [-v...] [--model ref-disk|ref-plummer|disk|plummer] [--theta-ref X] [--eps2 X] [--seed N]\n");
 }
 
 }  // namespace
@@ -168,7 +200,14 @@ int main(int argc, char **argv) {
         usage();
         return 2;
     }
-    Bodies b = model == "disk" ? star_disk(n, seed) : model == "plummer" ? plummer(n, seed) : ref_disk(n, seed);
+    if (model != "ref-disk" && model != "ref-plummer" && model != "disk" && model != "plummer") {
+        std::fprintf(stderr, "unknown model %s\n", model.c_str());
+        return 2;
+    }
+    Bodies b = model == "disk"          ? star_disk(n, seed)
+               : model == "plummer"     ? plummer(n, seed)
+               : model == "ref-plummer" ? ref_plummer(n, seed)
+                                        : ref_disk(n, seed);
     try {
         nbx::BarnesHut bh(p, b.x.data(), b.y.data(), b.z.data(), b.vx.data(), b.vy.data(), b.vz.data(),
                           b.m.data());

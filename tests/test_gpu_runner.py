@@ -36,3 +36,14 @@ def test_runner_rejects_unknown_flag(cuda):
     build.build()
     out = subprocess.run([build.RUNNER, "--no-such-flag"], capture_output=True, text=True, timeout=60)
     assert out.returncode == 2
+
+
+@pytest.mark.parametrize("model", ["ref-plummer", "disk", "plummer"])
+def test_runner_models(cuda, tmp_path, model):
+    from nns_gb300 import build
+    build.build()
+    out = subprocess.run([build.RUNNER, "-n", "2048", "-i", "2", "--model", model], cwd=tmp_path,
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    m = re.search(r"final position of body 1: (\S+) (\S+) (\S+)", out.stdout)
+    assert m and all(abs(float(v)) < 1e6 for v in m.groups())
