@@ -439,25 +439,50 @@ def main():
               "e0": energy0, "how": "K (FP64 sum) + W = 1/2 sum m phi, phi from the Barnes-Hut walk; "
                                     "both forms from the same initial state"}
 
-    # ---- end to end through the public API with host buffers (pinned)
+    # ---- end to end through the public API with host buffers (pinned): every
+    # step copies its inputs in and its results out.  Two device states are
+    # used in turn so that the copies of one step overlap the compute of the
+    # other (copy-in stream, compute stream, copy-out stream, ordered by events).
     host = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
             for a in (b.x, b.y, b.z, b.vx, b.vy, b.vz, b.m)]
-    outs = [torch.empty(n, dtype=torch.float32).pin_memory() for _ in range(6)]
-    dev_in = [s.x, s.y, s.z, s.vx, s.vy, s.vz, s.m]
+    outs = [[torch.empty(n, dtype=torch.float32).pin_memory() for _ in range(6)] for _ in range(2)]
+    states = [s, State.empty(n, device="cuda:%d" % local)]
+    dev_in = [[t.x, t.y, t.z, t.vx, t.vy, t.vz, t.m] for t in states]
     h2d = sum(t.numel() * 4 for t in host)
-    d2h = sum(t.numel() * 4 for t in outs)
+    d2h = sum(t.numel() * 4 for t in outs[0])
+    s_comp, s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
+    ev_in = [torch.cuda.Event() for _ in range(2)]
+    ev_out = [torch.cuda.Event() for _ in range(2)]
+    ev_done = [torch.cuda.Event() for _ in range(2)]
+    cur = torch.cuda.current_stream()
     torch.cuda.synchronize()
+    for e in ev_done:
+        e.record(cur)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        for d, h in zip(dev_in, host):
-            d.copy_(h, non_blocking=True)
-        ctx.step(s, 1)
-        for o, d in zip(outs, dev_in[:6]):
-            o.copy_(d, non_blocking=True)
-    e1.record()
+    e0.record(cur)
+    for st_ in (s_comp, s_in, s_out):
+        st_.wait_event(e0)
+    for k in range(args.steps):
+        i = k % 2
+        with torch.cuda.stream(s_in):
+            s_in.wait_event(ev_done[i])  # the previous results of this state were read out
+            for d, h in zip(dev_in[i], host):
+                d.copy_(h, non_blocking=True)
+            ev_in[i].record(s_in)
+        s_comp.wait_event(ev_in[i])
+        ctx.step(states[i], 1, stream=s_comp)
+        ev_out[i].record(s_comp)
+        with torch.cuda.stream(s_out):
+            s_out.wait_event(ev_out[i])
+            for o, d in zip(outs[i], dev_in[i][:6]):
+                o.copy_(d, non_blocking=True)
+            ev_done[i].record(s_out)
+    for st_ in (s_in, s_comp, s_out):
+        cur.wait_stream(st_)
+    e1.record(cur)
     torch.cuda.synchronize()
+    del states[1], dev_in[1]
     e2e_ms = e0.elapsed_time(e1) / args.steps
     ctx.sync()
     frame = bench_frame(ctx, s, b)
@@ -532,6 +557,7 @@ def main():
         "diagnostics_fp64": {"momentum_drift": float(np.abs(diag1["momentum"] - diag0["momentum"]).max()),
                              "kinetic_rel_change": float((diag1["kinetic"] - diag0["kinetic"]) / diag0["kinetic"])},
         "e2e": {"value": round(1000.0 / e2e_ms, 4), "unit": "steps/s", "h2d_bytes_per_step": h2d,
+                "pipeline": "two device states: the copies of one step overlap the compute of the other",
                 "d2h_bytes_per_step": d2h},
         "batched": batched,
         "adjoint": adjoint,
