@@ -292,6 +292,17 @@ def total_energy(ctx, s) -> float:
     return float(ctx.diagnostics(s)["kinetic"]) + 0.5 * float((m * phi).sum())
 
 
+def hbm_roofline(n: int, integ_ms: float, peaks: dict) -> dict:
+    """The kick-drift kernel (k_update, one launch per step, bracketed alone by
+    the integrate phase events): 36 B read + 24 B written per body against the
+    measured copy bandwidth."""
+    peak = peaks.get("hbm_gbs")
+    achieved = 60.0 * n / (integ_ms * 1e-3) / 1e9
+    return {"bound": "hbm", "kernel": "k_update", "achieved": round(achieved, 1),
+            "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if peak else None,
+            "bytes_per_body": 60, "peak_kind": "measured copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"}
+
+
 def walk_traffic(n: int):
     """DRAM bytes (read + write) of one walk launch at this size, from the committed
     ncu summary of the benchmark workload (profiles/), or None for other sizes."""
@@ -554,6 +565,7 @@ def main():
                      "peak": round(peak, 2), "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
                      "traffic": walk_traffic(n),
                      "peak_kind": "nominal FP32 FMA peak (SMs x 128 x 2 x max SM clock %g MHz)" % max_mhz},
+        "roofline_hbm": hbm_roofline(n, plain["integ_ms"] / args.steps, peaks),
         "diagnostics_fp64": {"momentum_drift": float(np.abs(diag1["momentum"] - diag0["momentum"]).max()),
                              "kinetic_rel_change": float((diag1["kinetic"] - diag0["kinetic"]) / diag0["kinetic"])},
         "e2e": {"value": round(1000.0 / e2e_ms, 4), "unit": "steps/s", "h2d_bytes_per_step": h2d,
