@@ -51,6 +51,10 @@ def parse():
     ap.add_argument("--batched-systems", type=int, default=512)
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--fd-directions", type=int, default=16)
+    ap.add_argument("--adjoint-steps", type=int, default=100)
+    ap.add_argument("--adjoint-checkpoint", type=int, default=10)
+    ap.add_argument("--only", choices=["batched", "adjoint"], default=None,
+                    help="run one extension section alone and print its JSON object")
     return ap.parse_args()
 
 
@@ -229,7 +233,7 @@ def bench_adjoint(args, local):
     from nns_gb300 import ic
     from nns_gb300.adjoint import Adjoint, random_directions
     from nns_gb300.barnes_hut import Context, State
-    n, T, C = 65536, 100, 10
+    n, T, C = 65536, args.adjoint_steps, args.adjoint_checkpoint
     b = ic.plummer(n)
     ctx = Context(max_bodies=n, theta=0.5, eps=0.01, dt=1e-3, device=local)
     ctx.set_systems([0, n])
@@ -354,6 +358,11 @@ def main():
     from nns_gb300.barnes_hut import Context, State
 
     torch.cuda.set_device(local)
+    if args.only:
+        section = bench_batched(args, local) if args.only == "batched" else bench_adjoint(args, local)
+        if rank == 0:
+            print(json.dumps({args.only: section}), flush=True)
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
