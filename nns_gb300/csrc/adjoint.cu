@@ -108,9 +108,11 @@ __global__ void k_adj_prep(double *lam, float *gcot, int n, double dt, double dd
     }
 }
 
-// Force VJP over the recorded lists, one warp per walk group.  Per-lane
-// contributions to each list entry are reduced through shared memory in
-// chunks of 8 entries (row stride 33 avoids bank conflicts) and added to the
+// Force VJP over the recorded lists, one block per walk group: its warps take
+// interleaved chunks of 8 list entries (more warps in flight hide the list and
+// node gathers), and their per-lane target terms are summed in shared memory in
+// a fixed warp order.  Per-lane contributions to each list entry are reduced
+// through shared memory (row stride 33 avoids bank conflicts) and added to the
 // FP64 source gradients with atomics.
 constexpr int kAdjWarps = 4;
 constexpr int kChunk = 8;
@@ -122,8 +124,9 @@ __global__ void __launch_bounds__(kAdjWarps * 32)
                 const int *__restrict__ list_len, int lcap, const float *__restrict__ gcot, int n, float eps2,
                 double *__restrict__ G, int nc_cap, float *__restrict__ tdx) {
     __shared__ float red[kAdjWarps][kChunk * 4][33];
+    __shared__ float part[kAdjWarps][3][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int g = blockIdx.x * kAdjWarps + w; g < ngroups; g += gridDim.x * kAdjWarps) {
+    for (int g = blockIdx.x; g < ngroups; g += gridDim.x) {
         const int p0 = groups[g];
         const int s = body_sys[p0];
         const int end = min(sys_off[s + 1], p0 + 32);
@@ -142,7 +145,7 @@ __global__ void __launch_bounds__(kAdjWarps * 32)
         float ox = 0.f, oy = 0.f, oz = 0.f;
         const int len = list_len[g];
         const int *L = lists + (size_t)g * lcap;
-        for (int base = 0; base < len; base += kChunk) {
+        for (int base = w * kChunk; base < len; base += kAdjWarps * kChunk) {
             const int cnt = min(kChunk, len - base);
             const int cmine = lane < cnt ? L[base + lane] : 0;
 #pragma unroll
@@ -187,11 +190,23 @@ __global__ void __launch_bounds__(kAdjWarps * 32)
             }
             __syncwarp();
         }
-        if (valid) {
-            tdx[ob] = -ox;
-            tdx[n + ob] = -oy;
-            tdx[2 * n + ob] = -oz;
+        part[w][0][lane] = ox;
+        part[w][1][lane] = oy;
+        part[w][2][lane] = oz;
+        __syncthreads();
+        if (w == 0 && valid) {
+            float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+            for (int k = 0; k < kAdjWarps; k++) {
+                sx += part[k][0][lane];
+                sy += part[k][1][lane];
+                sz += part[k][2][lane];
+            }
+            tdx[ob] = -sx;
+            tdx[n + ob] = -sy;
+            tdx[2 * n + ob] = -sz;
         }
+        __syncthreads();  // part is reused by the next group
     }
 }
 
@@ -539,7 +554,7 @@ int adjoint_backward(Ctx *ctx, Adj *a, const nbx_state *s, float *gx, float *gy,
             TapeStep &t = a->tape[j];
             k_adj_prep<<<grid_for(n), kB, 0, st>>>(a->lam, a->gcot, n, dt, ddt);
             NBX_CUDA(cudaMemsetAsync(a->G, 0, sizeof(double) * 4 * (size_t)NC, st));
-            const int blocks = ceil_div(a->ngroups, kAdjWarps);
+            const int blocks = a->ngroups;
             k_adj_force<<<blocks < ctx->nsm * 16 ? blocks : ctx->nsm * 16, kAdjWarps * 32, 0, st>>>(
                 t.node4, t.body4, t.val, t.body_node, ctx->d_groups, a->ngroups, ctx->d_body_sys, ctx->d_sys_off,
                 t.lists, t.list_len, a->lcap, a->gcot, n, ctx->eps2, a->G, NC, a->tdx);
