@@ -114,7 +114,10 @@ __global__ void k_adj_prep(double *lam, float *gcot, int n, double dt, double dd
 // a fixed warp order.  Per-lane contributions to each list entry are reduced
 // through shared memory (row stride 33 avoids bank conflicts) and added to the
 // FP64 source gradients with atomics.
-constexpr int kAdjWarps = 4;
+#ifndef NBX_ADJ_WARPS
+#define NBX_ADJ_WARPS 8
+#endif
+constexpr int kAdjWarps = NBX_ADJ_WARPS;  // warps sharing one group's list
 constexpr int kChunk = 8;
 
 __global__ void __launch_bounds__(kAdjWarps * 32)
