@@ -65,6 +65,19 @@ namespace {
 
 constexpr int kB = 256;
 
+// start/stop events of a timed call, destroyed on every return path
+struct EventPair {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    bool ok = false;
+    EventPair() { ok = cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess; }
+    ~EventPair() {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    }
+    EventPair(const EventPair &) = delete;
+    EventPair &operator=(const EventPair &) = delete;
+};
+
 __global__ void k_copy_state(const float *x, const float *y, const float *z, const float *vx, const float *vy,
                              const float *vz, float *dst, int n) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -503,9 +516,9 @@ int adjoint_forward(Ctx *ctx, Adj *a, const nbx_state *s, const float *tx, const
                     double *loss_host, cudaStream_t st) {
     const int n = a->n;
     if (n != ctx->nbodies) return NBX_ERR_STATE;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    EventPair ev;
+    if (!ev.ok) return NBX_ERR_CUDA;
+    const cudaEvent_t e0 = ev.e0, e1 = ev.e1;
     cudaEventRecord(e0, st);
     NBX_CUDA(cudaMemcpyAsync(a->target, tx, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
     NBX_CUDA(cudaMemcpyAsync(a->target + n, ty, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
@@ -528,8 +541,6 @@ int adjoint_forward(Ctx *ctx, Adj *a, const nbx_state *s, const float *tx, const
     NBX_CUDA(cudaMemcpyAsync(loss_host, a->loss, sizeof(double), cudaMemcpyDeviceToHost, st));
     NBX_CUDA(cudaStreamSynchronize(st));
     cudaEventElapsedTime(&a->fwd_ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     return NBX_OK;
 }
 
@@ -540,9 +551,9 @@ int adjoint_backward(Ctx *ctx, Adj *a, const nbx_state *s, float *gx, float *gy,
     const int NC = ctx->cap_nodes;
     const double dt = ctx->p.dt, ddt = (double)ctx->p.dampening * ctx->p.dt;
     nbx_state w = work_state(a, s);
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    EventPair ev;
+    if (!ev.ok) return NBX_ERR_CUDA;
+    const cudaEvent_t e0 = ev.e0, e1 = ev.e1;
     cudaEventRecord(e0, st);
     for (int seg = a->nseg - 1; seg >= 0; seg--) {
         const int k0 = seg * a->C;
@@ -571,8 +582,6 @@ int adjoint_backward(Ctx *ctx, Adj *a, const nbx_state *s, float *gx, float *gy,
     cudaEventRecord(e1, st);
     NBX_CUDA(cudaStreamSynchronize(st));
     cudaEventElapsedTime(&a->bwd_ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     NBX_CUDA(cudaGetLastError());
     return NBX_OK;
 }

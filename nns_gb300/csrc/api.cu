@@ -94,22 +94,23 @@ struct Timer {
     cudaEvent_t a = nullptr, b = nullptr;
     float *ms;
     cudaStream_t st;
+    bool ok = false;  // events created and the start recorded
     Timer(float *ms_, cudaStream_t st_) : ms(ms_), st(st_) {
         if (ms) {
-            cudaEventCreate(&a);
-            cudaEventCreate(&b);
-            cudaEventRecord(a, st);
+            ok = cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess &&
+                 cudaEventRecord(a, st) == cudaSuccess;
         }
     }
     int finish(int rc) {
         if (ms) {
-            cudaEventRecord(b, st);
-            cudaEventSynchronize(b);
             float t = 0.f;
-            cudaEventElapsedTime(&t, a, b);
+            if (ok && cudaEventRecord(b, st) == cudaSuccess && cudaEventSynchronize(b) == cudaSuccess)
+                cudaEventElapsedTime(&t, a, b);
+            else if (rc == NBX_OK)
+                rc = NBX_ERR_CUDA;
             *ms = t;
-            cudaEventDestroy(a);
-            cudaEventDestroy(b);
+            if (a) cudaEventDestroy(a);
+            if (b) cudaEventDestroy(b);
         }
         return rc;
     }
