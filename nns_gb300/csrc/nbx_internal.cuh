@@ -10,7 +10,10 @@
 
 namespace nbx {
 
-constexpr int kTile = 2048;       // keys per radix tile (one warp: 32 lanes x 64)
+#ifndef NBX_TILE
+#define NBX_TILE 2048
+#endif
+constexpr int kTile = NBX_TILE;   // keys per radix tile (one warp)
 constexpr int kRadixBins = 256;   // 8-bit digits
 constexpr int kMaxLevel = 43;     // 42 key levels + the body level
 constexpr int kBodyFlag = int(0x80000000u);

@@ -74,7 +74,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 // addresses (coalesced, instead of one sector per key).  The tile's count of a
 // digit is the difference of adjacent entries of the scanned histogram (the
 // layout is tile-minor and the scan is continuous; offs[nh] holds the total).
-constexpr int kScatterWarps = 4;
+#ifndef NBX_SCATTER_WARPS
+#define NBX_SCATTER_WARPS 4
+#endif
+constexpr int kScatterWarps = NBX_SCATTER_WARPS;
 
 template <typename K, typename V>
 struct ScatterStage {
