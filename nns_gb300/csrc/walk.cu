@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32)
             __syncwarp();
             top--;
             const int b = e & ((1 << kLevelShift) - 1);
-            const int lvl = e >> kLevelShift;
+            const int lvl = (int)((unsigned)e >> kLevelShift);  // levels 32..42 set the sign bit
             const int mb = meta[b];
             const int first = mb & 0x0fffffff;
             const int nch = ((mb >> 28) & 7) + 1;

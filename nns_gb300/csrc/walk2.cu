@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             if (lane < avail) {
                 const int e = stack[top - 1 - lane];
                 const int b = e & ((1 << kLevelShift) - 1);
-                lvl = e >> kLevelShift;
+                lvl = (int)((unsigned)e >> kLevelShift);  // levels 32..42 set the sign bit
                 const int mb = meta[b];
                 first = mb & 0x0fffffff;
                 nch = ((mb >> 28) & 7) + 1;

@@ -1,6 +1,7 @@
 """Adversarial body sets shared by the oracle and GPU tests: collinear and
 coplanar bodies (degenerate boxes), signed zeros and bodies exactly on the box
-and split planes, and a tight cluster inside a spread population (deep trees)."""
+and split planes, a tight cluster inside a spread population (deep trees), and
+two lattice clusters near the origin whose cells go past level 32."""
 import numpy as np
 
 from nns_gb300 import ic
@@ -46,4 +47,24 @@ def cluster(n=1000, seed=14):
     return _bodies(p[0], p[1], p[2], seed)
 
 
-CASES = {"collinear": collinear, "coplanar": coplanar, "signed_zeros": signed_zeros, "cluster": cluster}
+def deep(n_spread=512, seed=15):
+    """Two 4x4x4 lattices (pitch 2e-12) 5e-10 apart at 1e-7 from the origin, in
+    a population spread over [-1, 1]^3.  Near the origin FP32 resolves 7e-15, so
+    the lattices fill cells down to level ~40, and with a softening of 1e-12
+    the walk decides the MAC on cells past level 32 (their level no longer fits
+    in 5 bits).  Every body pair separates within 42 levels: no key collisions."""
+    rng = np.random.default_rng(seed)
+    spread = rng.uniform(-1, 1, (3, n_spread)).astype(np.float32)
+    g = np.arange(4, dtype=np.float64) * 2e-12
+    lat = np.stack(np.meshgrid(g, g, g, indexing="ij")).reshape(3, -1) + 1e-7
+    lat_b = lat.copy()
+    lat_b[0] += 5e-10
+    p = np.concatenate([spread, lat.astype(np.float32), lat_b.astype(np.float32)], 1)
+    return _bodies(p[0], p[1], p[2], seed)
+
+
+CASES = {"collinear": collinear, "coplanar": coplanar, "signed_zeros": signed_zeros, "cluster": cluster,
+         "deep": deep}
+# softening per case (default 0.01): the deep case needs one far below its
+# cell sizes, else every cell past level ~9 passes the MAC on softening alone
+EPS = {"deep": 1e-12}

@@ -495,15 +495,16 @@ def test_hilbert_order_option(cuda):
     assert np.median(_rel(acc_h, acc_m)) < 1e-3
 
 
-@pytest.mark.parametrize("name", ["collinear", "coplanar", "signed_zeros", "cluster"])
+@pytest.mark.parametrize("name", ["collinear", "coplanar", "signed_zeros", "cluster", "deep"])
 def test_adversarial_geometry(cuda, name):
-    """Degenerate boxes, signed zeros, bodies on split planes and a tight
-    cluster (the oracle is pinned to the reference kernels on the same sets).
+    """Degenerate boxes, signed zeros, bodies on split planes, a tight cluster
+    and MAC decisions on cells past level 32 (the oracle is pinned to the
+    reference kernels on the same sets).
     Tree, keys and every MAC decision are bit-exact; forces within tolerance."""
-    from adversarial import CASES
+    from adversarial import CASES, EPS
     b = CASES[name]()
     n = len(b.x)
-    ctx = _ctx(n, theta=0.5, eps=0.01)
+    ctx = _ctx(n, theta=0.5, eps=EPS.get(name, 0.01))
     ctx.set_systems([0, n])
     s = _state(b)
     ctx.build(s)

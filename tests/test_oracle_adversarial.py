@@ -1,6 +1,6 @@
 """The oracle against the reference's own kernels (compiled for the CPU) on
-adversarial geometry: degenerate boxes, signed zeros, bodies on split planes
-and a tight cluster.  Box, permutation and tree bit-exact."""
+adversarial geometry: degenerate boxes, signed zeros, bodies on split planes,
+a tight cluster and a tree past level 32.  Box, permutation and tree bit-exact."""
 import numpy as np
 import pytest
 
