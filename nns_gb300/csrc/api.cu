@@ -201,7 +201,8 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
         delete ctx;
         return NBX_ERR_ARG;
     }
-    if (cudaSetDevice(p->device) != cudaSuccess) {
+    if (cudaSetDevice(p->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess) {
         delete ctx;
         return NBX_ERR_CUDA;
     }
@@ -214,8 +215,11 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     }
     const int64_t nc = p->node_capacity ? (int64_t)p->node_capacity : 2ll * B + 65536;
     ctx->cap_nodes = (int)(nc < nbx::kMaxNodes ? nc : nbx::kMaxNodes);
-    ctx->cap_tiles_body = B / nbx::kTile + Ss + 1;
-    ctx->cap_tiles_node = nbx::ceil_div(ctx->cap_nodes, nbx::kTile);
+    // a tile below kTile is only chosen while there are fewer than 2 * want tiles
+    const int want_tiles = 2 * ctx->nsm * nbx::kScatterWarps;
+    ctx->cap_tiles_body = (B / nbx::kTile > 2 * want_tiles ? B / nbx::kTile : 2 * want_tiles) + Ss + 1;
+    ctx->tile_node = nbx::tile_for(ctx->cap_nodes, ctx->nsm);
+    ctx->cap_tiles_node = nbx::ceil_div(ctx->cap_nodes, ctx->tile_node);
     const int64_t hist = 256ll * (ctx->cap_tiles_body > ctx->cap_tiles_node ? ctx->cap_tiles_body : ctx->cap_tiles_node);
     int64_t scan_max = hist;
     if (ctx->cap_nodes > scan_max) scan_max = ctx->cap_nodes;
@@ -329,6 +333,7 @@ int nbx_set_systems(nbx_ctx *c, int nsys, const int64_t *offsets) {
         if (offsets[s + 1] <= offsets[s]) return NBX_ERR_ARG;
     if (offsets[nsys] > ctx->cap_bodies) return NBX_ERR_ARG;
     const int n = (int)offsets[nsys];
+    const int tile = nbx::tile_for(n, ctx->nsm);
     std::vector<int> off(nsys + 1);
     std::vector<int4> tiles;
     std::vector<int2> st(nsys);
@@ -336,11 +341,11 @@ int nbx_set_systems(nbx_ctx *c, int nsys, const int64_t *offsets) {
     for (int s = 0; s <= nsys; s++) off[s] = (int)offsets[s];
     for (int s = 0; s < nsys; s++) {
         const int beg = off[s], end = off[s + 1];
-        const int nt = nbx::ceil_div(end - beg, nbx::kTile);
+        const int nt = nbx::ceil_div(end - beg, tile);
         st[s] = make_int2((int)tiles.size(), nt);
         for (int t = 0; t < nt; t++) {
-            const int a = beg + t * nbx::kTile;
-            const int len = (end - a) < nbx::kTile ? (end - a) : nbx::kTile;
+            const int a = beg + t * tile;
+            const int len = (end - a) < tile ? (end - a) : tile;
             tiles.push_back(make_int4(a, len, s, t));
         }
         for (int g = beg; g < end; g += 32) groups.push_back(g);
@@ -358,6 +363,7 @@ int nbx_set_systems(nbx_ctx *c, int nsys, const int64_t *offsets) {
     ctx->nsys = nsys;
     ctx->nbodies = n;
     ctx->ntiles_body = (int)tiles.size();
+    ctx->tile_body = tile;
     ctx->ngroups = (int)groups.size();
     ctx->built = false;
     ctx->ref_m = 0;

@@ -14,6 +14,20 @@ namespace nbx {
 #define NBX_TILE 2048
 #endif
 constexpr int kTile = NBX_TILE;   // keys per radix tile (one warp)
+constexpr int kTileMin = 256;     // smallest radix tile (small systems)
+#ifndef NBX_SCATTER_WARPS
+#define NBX_SCATTER_WARPS 4
+#endif
+constexpr int kScatterWarps = NBX_SCATTER_WARPS;  // tiles (warps) per scatter block
+
+// Radix tile for n keys: the largest power of two <= kTile that still gives
+// about two scatter blocks per SM, but not below kTileMin.
+inline int tile_for(long long n, int nsm) {
+    const long long want = 2ll * nsm * kScatterWarps;
+    int t = kTile;
+    while (t > kTileMin && n < (long long)t * want) t >>= 1;
+    return t;
+}
 constexpr int kRadixBins = 256;   // 8-bit digits
 constexpr int kMaxLevel = 43;     // 42 key levels + the body level
 constexpr int kBodyFlag = int(0x80000000u);
@@ -46,6 +60,7 @@ struct Ctx {
 
     // capacity
     int cap_bodies, cap_sys, cap_nodes, cap_tiles_body, cap_tiles_node;
+    int tile_body = kTile, tile_node = kTile;  // radix tile sizes (tile_for)
     int nsm = 152;         // multiprocessors of the device
     long long launches = 0;  // kernels launched by this context
 

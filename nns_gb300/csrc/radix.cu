@@ -1,6 +1,7 @@
 // radix.cu -- stable LSD radix sort passes (8-bit digits), warp-per-tile.
 //
-// A tile is 2048 consecutive keys owned by one warp.  Per pass:
+// A tile is up to 2048 consecutive keys owned by one warp (smaller for small
+// systems, so that the tiles still fill the GPU).  Per pass:
 //   k_radix_hist    per-tile digit counts, stored [segment][digit][tile]
 //   scan            one exclusive scan over the whole count array: because the
 //                   layout is segment-major, digit-major, tile-minor, the scan
@@ -25,6 +26,7 @@ struct TileMap {
     // uniform mode
     const unsigned *count;  // device-side element count
     int ntiles;             // tiles in the launch
+    int tile;               // keys per tile (<= kTile)
 };
 
 template <bool Seg>
@@ -38,10 +40,10 @@ __device__ __forceinline__ void tile_info(const TileMap &tm, int t, int &start, 
         hbase = (int64_t)s.x * kRadixBins + d.w;
         hstride = s.y;
     } else {
-        int64_t st = (int64_t)t * kTile;
+        int64_t st = (int64_t)t * tm.tile;
         int64_t n = (int64_t)*tm.count;
         start = (int)st;
-        len = (int)(n > st ? (n - st < kTile ? n - st : kTile) : 0);
+        len = (int)(n > st ? (n - st < tm.tile ? n - st : tm.tile) : 0);
         hbase = t;
         hstride = tm.ntiles;
     }
@@ -59,9 +61,17 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     int start, len, hstride;
     int64_t hbase;
     tile_info<Seg>(tm, t, start, len, hbase, hstride);
-    for (int i = lane; i < len; i += 32) {
-        unsigned d = (unsigned)(key[start + i] >> shift) & 0xffu;
-        atomicAdd(&cnt[w][d], 1u);
+    constexpr int kBatch = 8;  // loads in flight together (the atomics would serialise them)
+    for (int i0 = 0; i0 < len; i0 += 32 * kBatch) {
+        unsigned d[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; u++) {
+            const int i = i0 + 32 * u + lane;
+            d[u] = i < len ? (unsigned)(key[start + i] >> shift) & 0xffu : 0x100u;
+        }
+#pragma unroll
+        for (int u = 0; u < kBatch; u++)
+            if (d[u] < 0x100u) atomicAdd(&cnt[w][d[u]], 1u);
     }
     __syncwarp();
     for (int d = lane; d < kRadixBins; d += 32) hist[hbase + (int64_t)d * hstride] = cnt[w][d];
@@ -74,18 +84,26 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 // addresses (coalesced, instead of one sector per key).  The tile's count of a
 // digit is the difference of adjacent entries of the scanned histogram (the
 // layout is tile-minor and the scan is continuous; offs[nh] holds the total).
-#ifndef NBX_SCATTER_WARPS
-#define NBX_SCATTER_WARPS 4
-#endif
-constexpr int kScatterWarps = NBX_SCATTER_WARPS;
+// A warp's stage: gbase (output offset of (digit, tile)), lstart (tile-local
+// start of the digit), cnt (running tile-local position), then the tile's keys
+// and values; sized for the launch's tile.
+template <typename K, typename V>
+__host__ __device__ constexpr size_t stage_bytes(int tile) {
+    return (3 * kRadixBins * sizeof(unsigned) + (size_t)tile * (sizeof(K) + sizeof(V)) + 15) & ~(size_t)15;
+}
 
 template <typename K, typename V>
-struct ScatterStage {
-    K key[kTile];
-    V val[kTile];
-    unsigned gbase[kRadixBins];   // output offset of (digit, tile)
-    unsigned lstart[kRadixBins];  // tile-local start of the digit
-    unsigned cnt[kRadixBins];     // running tile-local position
+struct Stage {
+    unsigned *gbase, *lstart, *cnt;
+    K *key;
+    V *val;
+    __device__ Stage(unsigned char *base, int tile) {
+        gbase = reinterpret_cast<unsigned *>(base);
+        lstart = gbase + kRadixBins;
+        cnt = lstart + kRadixBins;
+        key = reinterpret_cast<K *>(cnt + kRadixBins);
+        val = reinterpret_cast<V *>(key + tile);
+    }
 };
 
 template <typename K, typename V, bool Seg>
@@ -101,7 +119,7 @@ __global__ void __launch_bounds__(kScatterWarps * 32)
     int64_t hbase;
     tile_info<Seg>(tm, t, start, len, hbase, hstride);
     if (len <= 0) return;
-    ScatterStage<K, V> &sg = reinterpret_cast<ScatterStage<K, V> *>(smem_raw)[w];
+    Stage<K, V> sg(smem_raw + (size_t)w * stage_bytes<K, V>(tm.tile), tm.tile);
     // lane owns digits 8*lane .. 8*lane+7: counts, then the tile-local starts
     unsigned c[8], sum = 0;
 #pragma unroll
@@ -170,7 +188,7 @@ __global__ void __launch_bounds__(kScatterWarps * 32)
 template <typename K, typename V, bool Seg>
 int launch_scatter(Ctx *ctx, int nt, const K *kin, K *kout, const V *vin, V *vout, const TileMap &tm, int shift,
                    cudaStream_t st) {
-    const size_t smem = sizeof(ScatterStage<K, V>) * kScatterWarps;
+    const size_t smem = stage_bytes<K, V>(tm.tile) * kScatterWarps;
     k_radix_scatter<K, V, Seg><<<ceil_div(nt, kScatterWarps), kScatterWarps * 32, smem, st>>>(
         kin, kout, vin, vout, tm, shift, ctx->d_hist);
     ++ctx->launches;
@@ -182,7 +200,7 @@ int launch_scatter(Ctx *ctx, int nt, const K *kin, K *kout, const V *vin, V *vou
 // Sorts (d_key, d_val) of every system by the 63-bit key, stably, in place
 // (8 passes, result back in d_key / d_val).
 int radix_sort_bodies(Ctx *ctx, cudaStream_t st) {
-    TileMap tm{ctx->d_tiles, ctx->d_sys_tiles, nullptr, ctx->ntiles_body};
+    TileMap tm{ctx->d_tiles, ctx->d_sys_tiles, nullptr, ctx->ntiles_body, ctx->tile_body};
     const int nt = ctx->ntiles_body;
     if (nt == 0) return NBX_OK;
     const int grid = ceil_div(nt, kWarpsPerBlock);
@@ -209,7 +227,7 @@ int radix_sort_bodies(Ctx *ctx, cudaStream_t st) {
 // level.  Input d_ent, output d_ent_alt; the element count is on the device.
 int radix_sort_entries(Ctx *ctx, cudaStream_t st) {
     const int nt = ctx->cap_tiles_node;
-    TileMap tm{nullptr, nullptr, &ctx->d_totals[1], nt};  // clamped node count (0 on overflow)
+    TileMap tm{nullptr, nullptr, &ctx->d_totals[1], nt, ctx->tile_node};  // clamped node count (0 on overflow)
     const int grid = ceil_div(nt, kWarpsPerBlock);
     const int nh = nt * kRadixBins;
     k_radix_hist<unsigned, false><<<grid, kWarpsPerBlock * 32, 0, st>>>(ctx->d_ent, tm, 24, ctx->d_hist);
@@ -225,9 +243,9 @@ int radix_sort_entries(Ctx *ctx, cudaStream_t st) {
 int radix_init(Ctx *ctx) {
     NBX_CUDA(cudaFuncSetAttribute(k_radix_scatter<unsigned long long, int, true>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(sizeof(ScatterStage<unsigned long long, int>) * kScatterWarps)));
+                                  (int)(stage_bytes<unsigned long long, int>(kTile) * kScatterWarps)));
     NBX_CUDA(cudaFuncSetAttribute(k_radix_scatter<unsigned, int, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(sizeof(ScatterStage<unsigned, int>) * kScatterWarps)));
+                                  (int)(stage_bytes<unsigned, int>(kTile) * kScatterWarps)));
     return NBX_OK;
 }
 

@@ -100,11 +100,48 @@ __global__ void __launch_bounds__(1024) k_scan_down(const T *in, T *out, int n_c
     }
 }
 
+// The whole scan in one block, chunk by chunk with a running carry: for short
+// arrays (the radix histograms of small systems) one launch replaces three.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_scan_single(const T *in, T *out, int n_cap, const unsigned *n_dev,
+                                                      T *total_out) {
+    const int n = scan_count<T>(n_cap, n_dev);
+    __shared__ T tot;
+    T carry = 0;
+    for (int b0 = 0; b0 < n; b0 += kScanItems) {
+        const int base = b0 + 4 * threadIdx.x;
+        T v[4];
+        T s = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            v[k] = base + k < n ? in[base + k] : T(0);
+            s += v[k];
+        }
+        T ex = block_excl_scan<T>(s, &tot) + carry;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (base + k < n) out[base + k] = ex;
+            ex += v[k];
+        }
+        carry += tot;
+        __syncthreads();  // every thread has read tot before the next chunk writes it
+    }
+    if (threadIdx.x == 0 && total_out) *total_out = carry;
+}
+
+constexpr int kScanSingleBlocks = 8;  // up to 32768 elements in one block
+
 template <typename T>
 int scan_impl(Ctx *ctx, const T *in, T *out, int n_cap, const unsigned *n_dev, T *total_out,
               cudaStream_t st) {
     if (n_cap <= 0) return NBX_OK;
     int nblk = ceil_div(n_cap, kScanItems);
+    if (nblk <= kScanSingleBlocks) {
+        k_scan_single<T><<<1, 1024, 0, st>>>(in, out, n_cap, n_dev, total_out);
+        ++ctx->launches;
+        NBX_CUDA(cudaGetLastError());
+        return NBX_OK;
+    }
     if (nblk > ctx->cap_scan_blk) {
         ctx->last_error = "scan: block-sum scratch too small";
         return NBX_ERR_CAPACITY;
