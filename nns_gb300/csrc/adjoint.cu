@@ -27,6 +27,7 @@
 #include <cstring>
 #include <vector>
 
+#include "f32x2.cuh"
 #include "nbx_internal.cuh"
 
 namespace nbx {
@@ -124,14 +125,17 @@ __global__ void k_adj_prep(double *lam, float *gcot, int n, double dt, double dd
 // Force VJP over the recorded lists, one block per walk group: its warps take
 // interleaved chunks of 8 list entries (more warps in flight hide the list and
 // node gathers), and their per-lane target terms are summed in shared memory in
-// a fixed warp order.  Per-lane contributions to each list entry are reduced
-// through shared memory (row stride 33 avoids bank conflicts) and added to the
-// FP64 source gradients with atomics.
+// a fixed warp order.  Each lane evaluates two entries per packed f32x2
+// instruction.  Per-lane contributions to each list entry are reduced through
+// shared memory (lane l sums row l with 16-byte loads; the row stride of 36
+// floats keeps every quarter-warp on distinct banks) and added to the FP64
+// source gradients with atomics.
 #ifndef NBX_ADJ_WARPS
 #define NBX_ADJ_WARPS 8
 #endif
 constexpr int kAdjWarps = NBX_ADJ_WARPS;  // warps sharing one group's list
 constexpr int kChunk = 8;
+constexpr int kRedStride = 36;
 
 __global__ void __launch_bounds__(kAdjWarps * 32)
     k_adj_force(const float4 *__restrict__ node4, const float4 *__restrict__ body4, const int *__restrict__ val,
@@ -139,9 +143,11 @@ __global__ void __launch_bounds__(kAdjWarps * 32)
                 const int *__restrict__ body_sys, const int *__restrict__ sys_off, const int *__restrict__ lists,
                 const int *__restrict__ list_len, int lcap, const float *__restrict__ gcot, int n, float eps2,
                 double *__restrict__ G, int nc_cap, float *__restrict__ tdx) {
-    __shared__ float red[kAdjWarps][kChunk * 4][33];
+    __shared__ __align__(16) float red[kAdjWarps][kChunk * 4][kRedStride];
     __shared__ float part[kAdjWarps][3][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const u64 eps2x2 = pk(eps2, eps2), three2 = pk(3.f, 3.f);
+    constexpr u64 kSign2 = 0x8000000080000000ull;  // flips the sign of both halves
     for (int g = blockIdx.x; g < ngroups; g += gridDim.x) {
         const int p0 = groups[g];
         const int s = body_sys[p0];
@@ -158,57 +164,85 @@ __global__ void __launch_bounds__(kAdjWarps * 32)
             gy = gcot[n + ob];
             gz = gcot[2 * n + ob];
         }
-        float ox = 0.f, oy = 0.f, oz = 0.f;
+        const u64 px = pk(me.x, me.x), py = pk(me.y, me.y), pz = pk(me.z, me.z);
+        const u64 gx2 = pk(gx, gx), gy2 = pk(gy, gy), gz2 = pk(gz, gz);
+        u64 ox = 0ull, oy = 0ull, oz = 0ull;  // packed (+0, +0)
         const int len = list_len[g];
         const int *L = lists + (size_t)g * lcap;
         for (int base = w * kChunk; base < len; base += kAdjWarps * kChunk) {
             const int cnt = min(kChunk, len - base);
             const int cmine = lane < cnt ? L[base + lane] : 0;
 #pragma unroll
-            for (int e = 0; e < kChunk; e++) {
-                float vx = 0.f, vy = 0.f, vz = 0.f, vm = 0.f;
-                if (e < cnt) {
-                    const int c = __shfl_sync(0xffffffffu, cmine, e);
-                    const float4 q = node4[c];
-                    const float dx = q.x - me.x, dy = q.y - me.y, dz = q.z - me.z;
-                    const float s2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-                    const float inv = rsqrtf(s2);
-                    const float inv3 = inv * inv * inv;
-                    const float inv5 = inv3 * inv * inv;
-                    const float dg = fmaf(dz, gz, fmaf(dy, gy, dx * gx));
-                    const float t = 3.f * dg * inv5;
-                    const float jx = fmaf(gx, inv3, -dx * t);
-                    const float jy = fmaf(gy, inv3, -dy * t);
-                    const float jz = fmaf(gz, inv3, -dz * t);
-                    if (c != mynode) {  // a body's own entry has d = 0 and contributes nothing net
-                        vx = q.w * jx;
-                        vy = q.w * jy;
-                        vz = q.w * jz;
-                        vm = dg * inv3;
-                        ox += vx;
-                        oy += vy;
-                        oz += vz;
-                    }
-                }
-                red[w][4 * e + 0][lane] = vx;
-                red[w][4 * e + 1][lane] = vy;
-                red[w][4 * e + 2][lane] = vz;
-                red[w][4 * e + 3][lane] = vm;
+            for (int e = 0; e < kChunk; e += 2) {
+                const int ca = __shfl_sync(0xffffffffu, cmine, e);
+                const int cb = __shfl_sync(0xffffffffu, cmine, e + 1);
+                const float4 qa = node4[ca], qb = node4[cb];
+                const u64 dx = sub2(pk(qa.x, qb.x), px);
+                const u64 dy = sub2(pk(qa.y, qb.y), py);
+                const u64 dz = sub2(pk(qa.z, qb.z), pz);
+                u64 s2 = fma2(dx, dx, eps2x2);
+                s2 = fma2(dy, dy, s2);
+                s2 = fma2(dz, dz, s2);
+                float sa, sb;
+                upk(s2, sa, sb);
+                const u64 inv = pk(rsq(sa), rsq(sb));
+                const u64 inv2 = mul2(inv, inv);
+                const u64 inv3 = mul2(inv2, inv);
+                const u64 inv5 = mul2(inv3, inv2);
+                u64 dg = mul2(dx, gx2);
+                dg = fma2(dy, gy2, dg);
+                dg = fma2(dz, gz2, dg);
+                const u64 mt = mul2(mul2(three2, dg), inv5) ^ kSign2;  // -3 (d.g) s^-5
+                // a body's own entry has d = 0 and contributes nothing net; entries
+                // past the chunk's end contribute nothing
+                const bool la = e < cnt, lb = e + 1 < cnt;
+                const u64 mm = pk(la && ca != mynode ? qa.w : 0.f, lb && cb != mynode ? qb.w : 0.f);
+                const u64 vx = mul2(mm, fma2(dx, mt, mul2(gx2, inv3)));
+                const u64 vy = mul2(mm, fma2(dy, mt, mul2(gy2, inv3)));
+                const u64 vz = mul2(mm, fma2(dz, mt, mul2(gz2, inv3)));
+                ox = add2(ox, vx);
+                oy = add2(oy, vy);
+                oz = add2(oz, vz);
+                float xa, xb, ya, yb, za, zb, ma, mb;
+                upk(vx, xa, xb);
+                upk(vy, ya, yb);
+                upk(vz, za, zb);
+                upk(mul2(dg, inv3), ma, mb);
+                red[w][4 * e + 0][lane] = xa;
+                red[w][4 * e + 1][lane] = ya;
+                red[w][4 * e + 2][lane] = za;
+                red[w][4 * e + 3][lane] = la ? ma : 0.f;
+                red[w][4 * e + 4][lane] = xb;
+                red[w][4 * e + 5][lane] = yb;
+                red[w][4 * e + 6][lane] = zb;
+                red[w][4 * e + 7][lane] = lb ? mb : 0.f;
             }
             __syncwarp();
             // lane l reduces row l: entry l/4, component l%4
             const int crow = __shfl_sync(0xffffffffu, cmine, (lane >> 2) & 7);
             if (lane < 4 * cnt) {
-                float acc = 0.f;
-#pragma unroll 8
-                for (int k = 0; k < 32; k++) acc += red[w][lane][k];
-                if (crow < nc_cap) atomicAdd(&G[(size_t)(lane & 3) * nc_cap + crow], (double)acc);
+                const float4 *row = reinterpret_cast<const float4 *>(&red[w][lane][0]);
+                u64 s01 = 0ull, s23 = 0ull;
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const float4 v = row[k];
+                    s01 = add2(s01, pk(v.x, v.y));
+                    s23 = add2(s23, pk(v.z, v.w));
+                }
+                float a0, a1, a2, a3;
+                upk(s01, a0, a1);
+                upk(s23, a2, a3);
+                if (crow < nc_cap) atomicAdd(&G[(size_t)(lane & 3) * nc_cap + crow], (double)((a0 + a1) + (a2 + a3)));
             }
             __syncwarp();
         }
-        part[w][0][lane] = ox;
-        part[w][1][lane] = oy;
-        part[w][2][lane] = oz;
+        float xa, xb;
+        upk(ox, xa, xb);
+        part[w][0][lane] = xa + xb;
+        upk(oy, xa, xb);
+        part[w][1][lane] = xa + xb;
+        upk(oz, xa, xb);
+        part[w][2][lane] = xa + xb;
         __syncthreads();
         if (w == 0 && valid) {
             float sx = 0.f, sy = 0.f, sz = 0.f;
@@ -226,11 +260,30 @@ __global__ void __launch_bounds__(kAdjWarps * 32)
     }
 }
 
+// Per cell, once: the terms every member body adds, (Gx_c / M_c, Gm_c - Gx_c . X_c / M_c),
+// written over the cell's G entries (FP64 divisions are slow on this part: one
+// per cell instead of one per body and ancestor).  Body entries stay as they are.
+__global__ void k_adj_cells(const float4 *__restrict__ node4, const int *__restrict__ meta,
+                            const unsigned *__restrict__ lvl, double *__restrict__ G, int nc_cap) {
+    const int T = (int)lvl[kMaxLevel + 1];  // node count
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < T; c += gridDim.x * blockDim.x) {
+        if (meta[c] < 0) continue;
+        const float4 q = node4[c];
+        const double M = q.w;
+        const double gxc = G[c], gyc = G[(size_t)nc_cap + c], gzc = G[2 * (size_t)nc_cap + c],
+                     gmc = G[3 * (size_t)nc_cap + c];
+        G[c] = gxc / M;
+        G[(size_t)nc_cap + c] = gyc / M;
+        G[2 * (size_t)nc_cap + c] = gzc / M;
+        G[3 * (size_t)nc_cap + c] = gmc - (gxc * q.x + gyc * q.y + gzc * q.z) / M;
+    }
+}
+
 // Gradients through the centres of mass to every body, and the state update.
-__global__ void k_adj_bodies(const float4 *__restrict__ node4, const float4 *__restrict__ body4,
-                             const int *__restrict__ val, const int *__restrict__ body_node,
-                             const int *__restrict__ parent, const double *__restrict__ G, int nc_cap,
-                             const float *__restrict__ tdx, double *lam, int n) {
+__global__ void k_adj_bodies(const float4 *__restrict__ body4, const int *__restrict__ val,
+                             const int *__restrict__ body_node, const int *__restrict__ parent,
+                             const double *__restrict__ G, int nc_cap, const float *__restrict__ tdx, double *lam,
+                             int n) {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const int i = val[p];
         const int b = body_node[p];
@@ -238,14 +291,10 @@ __global__ void k_adj_bodies(const float4 *__restrict__ node4, const float4 *__r
         double sax = 0.0, say = 0.0, saz = 0.0, sb = 0.0;
         int cur = parent[b];
         for (int guard = 0; guard < 64 && cur >= 0; guard++) {
-            const float4 q = node4[cur];
-            const double M = q.w;
-            const double gxc = G[cur], gyc = G[(size_t)nc_cap + cur], gzc = G[2 * (size_t)nc_cap + cur],
-                         gmc = G[3 * (size_t)nc_cap + cur];
-            sax += gxc / M;
-            say += gyc / M;
-            saz += gzc / M;
-            sb += gmc - (gxc * q.x + gyc * q.y + gzc * q.z) / M;
+            sax += G[cur];
+            say += G[(size_t)nc_cap + cur];
+            saz += G[2 * (size_t)nc_cap + cur];
+            sb += G[3 * (size_t)nc_cap + cur];
             cur = parent[cur];
         }
         const double m = me.w;
@@ -572,9 +621,10 @@ int adjoint_backward(Ctx *ctx, Adj *a, const nbx_state *s, float *gx, float *gy,
             k_adj_force<<<blocks < ctx->nsm * 16 ? blocks : ctx->nsm * 16, kAdjWarps * 32, 0, st>>>(
                 t.node4, t.body4, t.val, t.body_node, ctx->d_groups, a->ngroups, ctx->d_body_sys, ctx->d_sys_off,
                 t.lists, t.list_len, a->lcap, a->gcot, n, ctx->eps2, a->G, NC, a->tdx);
-            k_adj_bodies<<<grid_for(n), kB, 0, st>>>(t.node4, t.body4, t.val, t.body_node, t.parent, a->G, NC,
-                                                      a->tdx, a->lam, n);
-            ctx->launches += 3;
+            k_adj_cells<<<grid_for(NC), kB, 0, st>>>(t.node4, t.meta, t.lvl, a->G, NC);
+            k_adj_bodies<<<grid_for(n), kB, 0, st>>>(t.body4, t.val, t.body_node, t.parent, a->G, NC, a->tdx,
+                                                      a->lam, n);
+            ctx->launches += 4;
         }
     }
     k_lam_out<<<grid_for(n), kB, 0, st>>>(a->lam, n, gx, gy, gz, gvx, gvy, gvz, gm);

@@ -129,7 +129,10 @@ __global__ void __launch_bounds__(1024) k_scan_single(const T *in, T *out, int n
     if (threadIdx.x == 0 && total_out) *total_out = carry;
 }
 
-constexpr int kScanSingleBlocks = 8;  // up to 32768 elements in one block
+#ifndef NBX_SCAN_SINGLE_BLOCKS
+#define NBX_SCAN_SINGLE_BLOCKS 8
+#endif
+constexpr int kScanSingleBlocks = NBX_SCAN_SINGLE_BLOCKS;  // chunks of 4096 scanned in one block
 
 template <typename T>
 int scan_impl(Ctx *ctx, const T *in, T *out, int n_cap, const unsigned *n_dev, T *total_out,

@@ -451,41 +451,61 @@ __global__ void __launch_bounds__(kBlock) k_moments_level(int level, const unsig
     }
 }
 
-// Bottom-up FP64 moments in one launch, one thread per cell in BFS order.  A
-// cell whose children are all bodies is summed at once by its thread.  Every
-// completed cell then arrives at its parent's counter, and the thread that
-// brings the count to the parent's number of cell children sums the parent
-// (children in child order: the same additions as k_moments_level) and climbs
-// on.  Nothing waits: a thread that is not last stops.  The arrival releases
-// the thread's sums, and the last arriver acquires before it reads its
-// children's sums (through L2).  Counters are zeroed by k_nodes_a.
-__device__ __forceinline__ int arrive_release(int *p) {
+// Bottom-up FP64 moments in one launch, one thread per cell in BFS order.
+// Every child arrives once at its cell's counter: the cell's own thread adds
+// the number of its body children in one step, and each child cell arrives
+// when it is complete.  The arrival that brings the count to the cell's number
+// of children sums the cell (children in child order: the same additions as
+// k_moments_level) and climbs on to the parent.  Nothing waits: a thread whose
+// arrival is not the last stops.  A cell's arrival is acquire-release: it
+// publishes the thread's sums and, when last, orders the reads of the
+// siblings' sums (through L2) after their arrivals.  Counters are zeroed by
+// k_nodes_a.
+__device__ __forceinline__ int arrive_acq_rel(int *p) {
     int old;
-    asm volatile("atom.release.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
     return old;
 }
 
+// A cell's sums from its children in child order.  Every child's body record
+// and cell sums are loaded at once and the child's kind picks one (a body's
+// sums entry is never read for its value), so the loads take one round trip.
 __device__ __forceinline__ void sum_cell(int b, int first, int nch, const int *__restrict__ meta, float4 *node4,
                                          double4 *sums, int *count) {
+    int mk[8], ck[8];
+    float4 q[8];
+    double2 v0[8], v1[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        if (j < nch) {
+            const int c = first + j;
+            mk[j] = meta[c];
+            q[j] = node4[c];
+            const double2 *v = reinterpret_cast<const double2 *>(&sums[c]);
+            v0[j] = __ldcg(v);
+            v1[j] = __ldcg(v + 1);
+            ck[j] = __ldcg(&count[c]);
+        }
+    }
     double sm = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
     int cnt = 0;
-    for (int c = first; c < first + nch; c++) {
-        if (meta[c] < 0) {
-            const float4 q = node4[c];
-            const double mb = (double)q.w;
-            sm += mb;
-            sx += mb * (double)q.x;
-            sy += mb * (double)q.y;
-            sz += mb * (double)q.z;
-            cnt += 1;
-        } else {
-            const double2 *v = reinterpret_cast<const double2 *>(&sums[c]);
-            const double2 v0 = __ldcg(v), v1 = __ldcg(v + 1);
-            sm += v0.x;
-            sx += v0.y;
-            sy += v1.x;
-            sz += v1.y;
-            cnt += __ldcg(&count[c]);
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        if (j < nch) {
+            if (mk[j] < 0) {
+                const double mb = (double)q[j].w;
+                sm += mb;
+                sx += mb * (double)q[j].x;
+                sy += mb * (double)q[j].y;
+                sz += mb * (double)q[j].z;
+                cnt += 1;
+            } else {
+                sm += v0[j].x;
+                sx += v0[j].y;
+                sy += v1[j].x;
+                sz += v1[j].y;
+                cnt += ck[j];
+            }
         }
     }
     sums[b] = make_double4(sm, sx, sy, sz);
@@ -505,19 +525,23 @@ __global__ void __launch_bounds__(kBlock) k_moments_up(const unsigned long long 
         int b = cl[nsys + k];
         int pm = meta[b];
         int first = pm & 0x0fffffff, nch = ((pm >> 28) & 7) + 1;
-        bool leaf = true;
-        for (int c = first; c < first + nch; c++) leaf &= meta[c] < 0;
-        if (!leaf) continue;  // summed by the thread of its last child cell
-        sum_cell(b, first, nch, meta, node4, sums, count);
-        for (b = parent[b]; b >= 0; b = parent[b]) {
-            pm = meta[b];
+        int nbody = 0;
+        for (int c = first; c < first + nch; c++) nbody += meta[c] < 0;
+        if (nbody == 0) continue;  // completed by the arrival of its last child cell
+        if (nbody < nch) {  // cell children too: the bodies arrive together (relaxed: nothing to publish)
+            if (atomicAdd(&counter[b], nbody) + nbody != nch) continue;
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        }
+        for (;;) {
+            // the parent and its meta load while the sums do
+            const int up = parent[b];
+            sum_cell(b, first, nch, meta, node4, sums, count);
+            if (up < 0) break;
+            pm = meta[up];
+            if (arrive_acq_rel(&counter[up]) != ((pm >> 28) & 7)) break;  // last of its children?
+            b = up;
             first = pm & 0x0fffffff;
             nch = ((pm >> 28) & 7) + 1;
-            int ncc = 0;
-            for (int c = first; c < first + nch; c++) ncc += meta[c] >= 0;
-            if (arrive_release(&counter[b]) != ncc - 1) break;
-            asm volatile("fence.acq_rel.gpu;" ::: "memory");
-            sum_cell(b, first, nch, meta, node4, sums, count);
         }
     }
 }

@@ -26,6 +26,7 @@
 // Accumulation modes: 0 plain FP32 (two packed partial sums), 1 split
 // compensation (plain FP32 within a round, Kahan across rounds), 2 Kahan on
 // every term.  Optional per-body potential for the energy diagnostics.
+#include "f32x2.cuh"
 #include "nbx_internal.cuh"
 
 namespace nbx {
@@ -67,40 +68,6 @@ constexpr int kReps = NBX_MAC_REPS;
 // (#pragma arguments are not macro-expanded: the unroll factors go through constants)
 constexpr int kBodyUnroll = NBX_BODY_UNROLL;
 constexpr int kCellUnroll = NBX_CELL_UNROLL;
-
-typedef unsigned long long u64;
-
-__device__ __forceinline__ u64 pk(float a, float b) {
-    u64 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void upk(u64 v, float &a, float &b) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-}
-__device__ __forceinline__ u64 sub2(u64 a, u64 b) {
-    u64 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ u64 mul2(u64 a, u64 b) {
-    u64 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ u64 fma2(u64 a, u64 b, u64 c) {
-    u64 r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-
-// Hardware reciprocal square root (MUFU); r >= eps^2 > 0 is never subnormal,
-// so flushing subnormals changes nothing and saves the scaling fix-up.
-__device__ __forceinline__ float rsq(float r) {
-    float y;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(r));
-    return y;
-}
 
 // depth0 * 4^-k exactly (a power-of-two product is exact unless it underflows)
 __device__ __forceinline__ float scale4(float d0, int k) {
