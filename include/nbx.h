@@ -77,6 +77,10 @@ typedef struct nbx_params {
                           are compact but the interaction lists differ from the reference */
     int node_capacity; /* node pool (cells + bodies); 0: 2*max_bodies + 65536.  A tree that
                           needs more nodes reports NBX_ERR_CAPACITY */
+    int moments_mode;  /* centre-of-mass pass: 0 by size (one launch up to 2^21 bodies,
+                          per level above); 1 one launch per tree level; 2 one launch in
+                          which the last child to finish sums its parent.  The sums are
+                          the same FP64 additions in the same order in every mode */
 } nbx_params;
 
 /* SoA device state of all systems; systems are contiguous ranges. */

@@ -26,7 +26,8 @@ class nbx_params(C.Structure):
                 ("group", C.c_int), ("stack_depth", C.c_int), ("compensated", C.c_int),
                 ("leaf_size", C.c_int), ("radix_bits", C.c_int), ("walk_warps", C.c_int),
                 ("device", C.c_int), ("block_size", C.c_int), ("grid_size", C.c_int),
-                ("walk_variant", C.c_int), ("key_order", C.c_int), ("node_capacity", C.c_int)]
+                ("walk_variant", C.c_int), ("key_order", C.c_int), ("node_capacity", C.c_int),
+                ("moments_mode", C.c_int)]
 
 
 class nbx_state(C.Structure):

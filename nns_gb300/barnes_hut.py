@@ -40,7 +40,8 @@ class Context:
     def __init__(self, max_bodies: int, max_systems: int = 1, theta: float = 0.5,
                  theta_ref: float | None = None, eps: float = 0.05, eps2: float | None = None,
                  dt: float = 1e-3, dampening: float = 1.0, compensated: int = 0,
-                 stack_depth: int = 512, device: int = 0, key_order: int = 0, node_capacity: int = 0):
+                 stack_depth: int = 512, device: int = 0, key_order: int = 0, node_capacity: int = 0,
+                 moments_mode: int = 0):
         p = L.nbx_params()
         lib().nbx_params_default(C.byref(p))
         p.max_bodies = int(max_bodies)
@@ -54,6 +55,7 @@ class Context:
         p.compensated = int(compensated)
         p.stack_depth = stack_depth
         p.node_capacity = node_capacity
+        p.moments_mode = moments_mode
         p.device = device
         p.key_order = int(key_order)
         self.params = p

@@ -182,7 +182,8 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     *out = nullptr;
     if (p->max_bodies < 1 || p->max_bodies > (1 << 25) || p->max_systems < 1 ||
         p->max_systems > p->max_bodies || p->group != 32 || p->leaf_size != 1 || p->radix_bits != 8 ||
-        p->stack_depth < 360 || p->stack_depth > 4096 || p->walk_variant < 0 || p->walk_variant > 3)
+        p->stack_depth < 360 || p->stack_depth > 4096 || p->walk_variant < 0 || p->walk_variant > 3 ||
+        p->moments_mode < 0 || p->moments_mode > 2)
         return NBX_ERR_ARG;
     Ctx *ctx = new (std::nothrow) Ctx();
     if (!ctx) return NBX_ERR_NOMEM;

@@ -32,7 +32,7 @@ namespace {
 
 constexpr int kBlock = 256;
 #ifndef NBX_MOMENTS_UP_MAX
-#define NBX_MOMENTS_UP_MAX (1 << 19)
+#define NBX_MOMENTS_UP_MAX (1 << 21)
 #endif
 constexpr int kMomentsUpMaxBodies = NBX_MOMENTS_UP_MAX;  // one-launch moments up to this many bodies
 
@@ -607,10 +607,11 @@ int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox
                                      ctx->d_delta, ctx->d_flags, S, ctx->d_fcl, ctx->d_cl, ctx->d_meta,
                                      ctx->d_parent, ctx->d_root_first, ctx->d_root_nch, ctx->d_status);
     ++ctx->launches;
-    // up to 2^19 bodies the 41 per-level launches cost more than the sums:
-    // one bottom-up launch; above, the per-level launches stream the levels
-    // and are faster (2^24: 6.3 against 11.9 ms per build)
-    if (n <= kMomentsUpMaxBodies) {
+    // up to 2^21 bodies the 41 per-level launches cost more than the sums: one
+    // bottom-up launch (2^16: 0.37 against 0.55 ms per build); above, the
+    // per-level launches stream the levels and are faster
+    const int mode = ctx->p.moments_mode;
+    if (mode == 2 || (mode == 0 && n <= kMomentsUpMaxBodies)) {
         k_moments_up<<<gn, kBlock, 0, st>>>(ctx->d_totals64, ctx->d_cl, S, ctx->d_parent, ctx->d_meta, ctx->d_node4,
                                             ctx->d_sums, ctx->d_count, ctx->d_arrive, ctx->d_status);
         ++ctx->launches;

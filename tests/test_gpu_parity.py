@@ -404,6 +404,25 @@ def test_plummer_2p20_properties(cuda):
     assert np.median(err) < 5e-3 and np.percentile(err, 99) < 5e-2, (np.median(err), np.percentile(err, 99))
 
 
+@pytest.mark.parametrize("mode", [1, 2], ids=["per_level", "one_launch"])
+def test_moments_modes_match_oracle(cuda, mode):
+    """Both centre-of-mass passes (one launch per level; one launch where the
+    last child sums its parent) give the oracle's FP64 sums bit for bit, on a
+    batch of uneven systems."""
+    from nns_gb300.barnes_hut import Context
+    sizes = [5000, 70000, 1, 2, 33000]
+    parts = [ic.plummer(k, seed=ic.SEED0 + 40 + j) for j, k in enumerate(sizes)]
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    b = ic.Bodies(*(np.concatenate([getattr(q, f) for q in parts]) for f in ("x", "y", "z", "vx", "vy", "vz", "m")))
+    ctx = Context(max_bodies=int(off[-1]), max_systems=len(sizes), theta=0.5, eps=0.01, moments_mode=mode)
+    ctx.set_systems(off)
+    s = _state(b)
+    ctx.build(s)
+    ctx.sync()
+    for j, q in enumerate(parts):
+        _check_tree(ctx.export_tree(j), O.build(q.x, q.y, q.z, q.m))
+
+
 def test_autotune_picks_a_valid_config(cuda, tmp_path, monkeypatch):
     from nns_gb300 import autotune
     monkeypatch.setenv("NBX_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
