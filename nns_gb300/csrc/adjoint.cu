@@ -18,8 +18,11 @@
 // Loss L = sum_i |x_i(T) - x*_i|^2, so lx(T) = 2 (x(T) - x*), lv(T) = 0.
 //
 // Memory: checkpoints of (x, v) every C steps; a segment of C steps is
-// recomputed (bit-identical: every kernel is deterministic) with each step's
-// tree and interaction lists recorded on a tape, then reversed.
+// recomputed with each step's tree and interaction lists recorded on a tape,
+// then reversed.  The forward steps with the recording walk's kernel (64-slot
+// buffers, plain FP32) without the recording, so the recompute is bit-identical
+// (every kernel is deterministic).  The forward records the last segment as it
+// goes, so the reverse pass starts without recomputing it.
 //
 // An FP64 replay of the recorded trajectory (same lists and tree structure,
 // centres of mass recomputed from the perturbed state) gives the FP64 loss
@@ -34,6 +37,7 @@ namespace nbx {
 
 int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox, const float *const *bbox_ptrs);
 int walk2_record(Ctx *ctx, const nbx_state *s, int *rec_list, int *rec_len, int rec_cap, cudaStream_t st);
+int walk2_plain64(Ctx *ctx, const nbx_state *s, cudaStream_t st);
 
 struct TapeStep {
     float4 *node4 = nullptr;
@@ -60,6 +64,7 @@ struct Adj {
     float4 *ctx_node4 = nullptr, *ctx_body4 = nullptr;
     int *ctx_meta = nullptr, *ctx_parent = nullptr, *ctx_val = nullptr, *ctx_body_node = nullptr;
     float fwd_ms = 0.f, bwd_ms = 0.f;
+    bool tail_taped = false;  // the forward recorded the last segment into the tape
 };
 
 namespace {
@@ -446,7 +451,10 @@ void swap_in(Ctx *ctx, Adj *a, int j) {
     ctx->d_body4 = t.body4;
 }
 
+// Back to the context's own node arrays.  Its per-build arrays (roots, cell
+// list, status) now describe the tape's tree: a walk needs a new build first.
 void swap_out(Ctx *ctx, Adj *a) {
+    ctx->built = false;
     ctx->d_node4 = a->ctx_node4;
     ctx->d_meta = a->ctx_meta;
     ctx->d_parent = a->ctx_parent;
@@ -572,17 +580,25 @@ int adjoint_forward(Ctx *ctx, Adj *a, const nbx_state *s, const float *tx, const
     NBX_CUDA(cudaMemcpyAsync(a->target, tx, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
     NBX_CUDA(cudaMemcpyAsync(a->target + n, ty, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
     NBX_CUDA(cudaMemcpyAsync(a->target + 2 * n, tz, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+    a->tail_taped = false;
+    const int k_tail = (a->nseg - 1) * a->C;  // first step of the last segment
     for (int k = 0; k < a->T; k++) {
         if (k % a->C == 0) {
             k_copy_state<<<grid_for(n), kB, 0, st>>>(s->x, s->y, s->z, s->vx, s->vy, s->vz,
                                                      a->ckpt + (size_t)(k / a->C) * 6 * n, n);
             ++ctx->launches;
         }
-        int rc = build_tree(ctx, s, st, false, nullptr);
-        if (!rc) rc = walk_forces(ctx, s, st);
-        if (!rc) rc = integrate(ctx, s, ctx->p.dt, ctx->p.dampening, n, st);
+        int rc;
+        if (k >= k_tail) {
+            rc = recorded_step(ctx, a, s, k - k_tail, st);
+        } else {
+            rc = build_tree(ctx, s, st, false, nullptr);
+            if (!rc) rc = walk2_plain64(ctx, s, st);
+            if (!rc) rc = integrate(ctx, s, ctx->p.dt, ctx->p.dampening, n, st);
+        }
         if (rc) return rc;
     }
+    a->tail_taped = true;
     NBX_CUDA(cudaMemsetAsync(a->loss, 0, sizeof(double), st));
     k_loss_init<<<grid_for(n), kB, 0, st>>>(s->x, s->y, s->z, a->target, n, a->lam, a->loss);
     ++ctx->launches;
@@ -607,12 +623,18 @@ int adjoint_backward(Ctx *ctx, Adj *a, const nbx_state *s, float *gx, float *gy,
     for (int seg = a->nseg - 1; seg >= 0; seg--) {
         const int k0 = seg * a->C;
         const int steps = (k0 + a->C <= a->T) ? a->C : a->T - k0;
-        NBX_CUDA(cudaMemcpyAsync(a->work, a->ckpt + (size_t)seg * 6 * n, sizeof(float) * 6 * n,
-                                 cudaMemcpyDeviceToDevice, st));
-        for (int j = 0; j < steps; j++) {
-            int rc = recorded_step(ctx, a, &w, j, st);
-            if (rc) return rc;
+        if (!(seg == a->nseg - 1 && a->tail_taped)) {
+            NBX_CUDA(cudaMemcpyAsync(a->work, a->ckpt + (size_t)seg * 6 * n, sizeof(float) * 6 * n,
+                                     cudaMemcpyDeviceToDevice, st));
+            for (int j = 0; j < steps; j++) {
+                int rc = recorded_step(ctx, a, &w, j, st);
+                if (rc) {
+                    a->tail_taped = false;
+                    return rc;
+                }
+            }
         }
+        a->tail_taped = false;  // the tape now holds this segment
         for (int j = steps - 1; j >= 0; j--) {
             TapeStep &t = a->tape[j];
             k_adj_prep<<<grid_for(n), kB, 0, st>>>(a->lam, a->gcot, n, dt, ddt);
@@ -639,6 +661,7 @@ int adjoint_backward(Ctx *ctx, Adj *a, const nbx_state *s, float *gx, float *gy,
 // Records the whole T-step trajectory from s (needs tape_steps >= T).
 int adjoint_record_all(Ctx *ctx, Adj *a, const nbx_state *s, cudaStream_t st) {
     if (a->tape_steps < a->T) return NBX_ERR_ARG;
+    a->tail_taped = false;
     const int n = a->n;
     nbx_state w = work_state(a, s);
     k_copy_state<<<grid_for(n), kB, 0, st>>>(s->x, s->y, s->z, s->vx, s->vy, s->vz, a->work, n);

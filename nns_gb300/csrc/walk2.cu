@@ -570,6 +570,12 @@ int walk2_record(Ctx *ctx, const nbx_state *s, int *rec_list, int *rec_len, int 
     return launch<64, 0, false, true>(ctx, s, nullptr, ctx->walk_warps, st, rec_list, rec_len, rec_cap);
 }
 
+// The same walk without recording: the recording adds stores only, so both
+// give the same forces bit for bit (the adjoint's forward and recompute).
+int walk2_plain64(Ctx *ctx, const nbx_state *s, cudaStream_t st) {
+    return launch<64, 0, false, false>(ctx, s, nullptr, ctx->walk_warps, st, nullptr, nullptr, 0);
+}
+
 // variant 0: 64-slot candidate buffers; 1: 128-slot buffers (<= 8 warps); 3: 96-slot buffers
 int walk2_forces(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st) {
     if (ctx->walk_variant == 1) return forces_cb<128>(ctx, s, pot, warps > 8 ? 8 : warps, st);

@@ -4,8 +4,9 @@
   accumulation) against FP64 central finite differences of the same
   trajectory replayed in FP64 with the recorded interaction lists (h = 1e-6),
   along random unit directions: error <= 1e-4 of the gradient norm.
-* The checkpoint interval does not change the gradients (the recompute is
-  bit-exact; only the order of FP64 atomic additions may differ).
+* The forward steps with the recording walk, so the recompute is bit-exact;
+  the checkpoint interval does not change the gradients (only the order of
+  FP64 atomic additions may differ).
 * The torch.autograd.Function wrapper returns the same gradients.
 """
 import numpy as np
@@ -64,6 +65,25 @@ def test_adjoint_matches_fp64_finite_differences(cuda):
         ad = float((g * u).sum())
         errs.append(abs(fd - ad) / gnorm)
     assert max(errs) <= 1e-4, errs
+
+
+def test_forward_steps_with_the_recording_walk(cuda):
+    """The adjoint's forward (the 64-slot walk, recording on its last segment)
+    ends bit for bit where T ordinary steps with the 64-slot walk end: recording
+    changes no force, so the reverse pass recomputes exactly the forward."""
+    from nns_gb300.barnes_hut import Context, State
+    n, T = 2048, 12
+    b, ctx, adj, target = _setup(n, T, 5)  # segments of 5, 5, 2 steps
+    s = State.from_bodies(b)
+    adj.forward(s, target)
+    ref = Context(max_bodies=n, theta=0.5, eps=0.01, dt=1e-3)
+    ref.set_systems([0, n])
+    ref.set_walk(8, 0)
+    s2 = State.from_bodies(b)
+    ref.step(s2, T)
+    ref.sync()
+    for got, want in zip(s.host(), s2.host()):
+        assert np.array_equal(got, want)
 
 
 def test_checkpoint_interval_does_not_change_gradients(cuda):
