@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--batched-systems", type=int, default=512)
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-hilbert", action="store_true")
     ap.add_argument("--fd-directions", type=int, default=16)
     ap.add_argument("--adjoint-steps", type=int, default=100)
     ap.add_argument("--adjoint-checkpoint", type=int, default=10)
@@ -285,6 +286,52 @@ def bench_adjoint(args, local):
         del ver
         torch.cuda.empty_cache()
     return out
+
+
+def bench_hilbert(args, local, b, targets, acc64, tune) -> dict:
+    """The same workload with Hilbert-ordered keys (nbx_params.key_order = 1):
+    the same cells with siblings reordered, so the walk groups are more
+    compact.  Not the parity mode: its interaction lists are not the
+    reference's.  Plain FP32 steps from the initial state."""
+    import torch
+    from nns_gb300.barnes_hut import Context, State
+    n = len(b.x)
+    ctx = Context(max_bodies=n, theta=THETA, eps=EPS, dt=DT, device=local, key_order=1)
+    if tune:
+        ctx.set_walk(tune["warps"], tune["variant"])
+    ctx.set_systems([0, n])
+    s = State.from_bodies(b, device="cuda:%d" % local)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    a = s.acc()[targets].astype(np.float64)
+    rel = np.linalg.norm(a - acc64, axis=1) / np.linalg.norm(acc64, axis=1)
+    for _ in range(args.warmup):
+        ctx.step(s)
+    k = max(3, min(args.steps, 5))
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(k)]
+    torch.cuda.synchronize()
+    for e in ev:
+        e[0].record()
+        ctx.build(s)
+        e[1].record()
+        ctx.forces(s)
+        e[2].record()
+        ctx.integrate(s)
+        e[3].record()
+    torch.cuda.synchronize()
+    info = ctx.tree_info()
+    ctx.sync()
+    ms = sum(e[0].elapsed_time(e[3]) for e in ev) / k
+    return {"value": round(1000.0 / ms, 4), "unit": "steps/s", "ms_per_step": round(ms, 3), "steps": k,
+            "phase_ms": {"build": round(sum(e[0].elapsed_time(e[1]) for e in ev) / k, 3),
+                         "walk": round(sum(e[1].elapsed_time(e[2]) for e in ev) / k, 3),
+                         "integrate": round(sum(e[2].elapsed_time(e[3]) for e in ev) / k, 3)},
+            "interactions_per_step": info["interactions"],  # counters restart at every build
+            "force_error_vs_fp64_direct": {"median": float(np.median(rel)),
+                                           "p99": float(np.quantile(rel, 0.99)), "max": float(rel.max())},
+            "note": "key_order=1: same cells and MAC, Hilbert sibling order; the walk groups and so the "
+                    "interaction lists differ from the reference's (not the parity mode)"}
 
 
 def total_energy(ctx, s) -> float:
@@ -527,6 +574,10 @@ def main():
     batched = None
     del ctx, s
     torch.cuda.empty_cache()
+    hilbert = None
+    if not args.no_hilbert:
+        hilbert = bench_hilbert(args, local, b, targets, acc64, tune)
+        torch.cuda.empty_cache()
     if not args.no_batched:
         batched = bench_batched(args, local)
         torch.cuda.empty_cache()
@@ -580,6 +631,7 @@ def main():
         "e2e": {"value": round(1000.0 / e2e_ms, 4), "unit": "steps/s", "h2d_bytes_per_step": h2d,
                 "pipeline": "two device states: the copies of one step overlap the compute of the other",
                 "d2h_bytes_per_step": d2h},
+        "hilbert": hilbert,
         "batched": batched,
         "adjoint": adjoint,
         "autotune": tune,

@@ -137,22 +137,32 @@ __constant__ unsigned char kHilbertState[12][8] = {
     {0, 8, 1, 11, 6, 8, 6, 11}, {10, 0, 9, 1, 10, 7, 9, 7}, {10, 4, 9, 4, 10, 2, 9, 3}, {5, 8, 5, 11, 2, 8, 3, 11},
     {4, 9, 0, 0, 7, 9, 2, 2}, {1, 1, 8, 5, 3, 3, 8, 6}, {11, 5, 0, 0, 11, 6, 2, 2}, {1, 1, 4, 10, 3, 3, 7, 10}};
 
-__device__ __forceinline__ int to_digit(int c, int &state, int order) {
-    if (order == 0) return c;
-    const int b = 7 - c;
-    const int h = kHilbertDigit[state][b];
-    state = kHilbertState[state][b];
-    return h;
+// The lanes of a warp index the tables by their own states, which the constant
+// cache would serialise: each block copies them to shared memory, one byte per
+// (state, child) holding digit | next state << 3.
+__device__ __forceinline__ void load_hilbert(unsigned char *t, int order) {
+    if (order == 0) return;  // uniform over the launch
+    for (int i = threadIdx.x; i < 96; i += blockDim.x)
+        t[i] = (unsigned char)(kHilbertDigit[i >> 3][i & 7] | (kHilbertState[i >> 3][i & 7] << 3));
+    __syncthreads();
 }
 
-__device__ __forceinline__ unsigned long long make_key(float px, float py, float pz, const float *bb, int order) {
+__device__ __forceinline__ int to_digit(int c, int &state, int order, const unsigned char *t) {
+    if (order == 0) return c;
+    const int e = t[(state << 3) + 7 - c];
+    state = e >> 3;
+    return e & 7;
+}
+
+__device__ __forceinline__ unsigned long long make_key(float px, float py, float pz, const float *bb, int order,
+                                                       const unsigned char *t) {
     float mnx = bb[0], mxx = bb[1], mny = bb[2], mxy = bb[3], mnz = bb[4], mxz = bb[5];
     unsigned long long key = 0ull;
     int state = 0;
 #pragma unroll 3
     for (int l = 1; l <= 21; l++) {
         int c = split_axis(px, mnx, mxx) + 2 * split_axis(py, mny, mxy) + 4 * split_axis(pz, mnz, mxz);
-        key = (key << 3) | (unsigned long long)to_digit(c, state, order);
+        key = (key << 3) | (unsigned long long)to_digit(c, state, order, t);
     }
     return key;
 }
@@ -165,6 +175,8 @@ __global__ void __launch_bounds__(kBlock) k_keys(const float *__restrict__ x, co
                                                   const float *__restrict__ bbox, int n,
                                                   unsigned long long *__restrict__ key, int *__restrict__ val,
                                                   float4 *__restrict__ pos4, DevStatus *st, int order) {
+    __shared__ unsigned char ht[96];
+    load_hilbert(ht, order);
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         const float px = x[i], py = y[i], pz = z[i];
         pos4[i] = make_float4(px, py, pz, m[i]);
@@ -173,7 +185,7 @@ __global__ void __launch_bounds__(kBlock) k_keys(const float *__restrict__ x, co
         float bb[6];
 #pragma unroll
         for (int k = 0; k < 6; k++) bb[k] = bbox[6 * s + k];
-        key[i] = make_key(px, py, pz, bb, order);
+        key[i] = make_key(px, py, pz, bb, order, ht);
         val[i] = i;
     }
 }
@@ -185,6 +197,8 @@ __global__ void k_refine(const float *__restrict__ x, const float *__restrict__ 
                          const unsigned long long *__restrict__ key,
                          unsigned long long *__restrict__ key_lo, int *__restrict__ val,
                          DevStatus *st, int order) {
+    __shared__ unsigned char ht[96];
+    load_hilbert(ht, order);
     for (int p = grid_stride_start(); p < n; p += grid_stride()) {
         const int s = body_sys[p];
         const int beg = sys_off[s], end = sys_off[s + 1];
@@ -208,7 +222,7 @@ __global__ void k_refine(const float *__restrict__ x, const float *__restrict__ 
             int state = 0;
             for (int l = 1; l <= 42; l++) {
                 int c = split_axis(px, mnx, mxx) + 2 * split_axis(py, mny, mxy) + 4 * split_axis(pz, mnz, mxz);
-                const int d = to_digit(c, state, order);
+                const int d = to_digit(c, state, order, ht);
                 if (l > 21) lo = (lo << 3) | (unsigned long long)d;
             }
             key_lo[q] = lo;
