@@ -45,3 +45,19 @@ def test_create_rejects_bad_params_without_gpu():
     p.group = 16  # the walk group is a warp
     h = ctypes.c_void_p()
     assert L.nbx_create(ctypes.byref(p), ctypes.byref(h)) == 1
+
+
+def test_params_layout_and_option_ranges_without_gpu():
+    """The library's defaults for the option fields at the end of nbx_params, and
+    out-of-range options rejected before any CUDA call."""
+    from nns_gb300 import _lib
+    L = _lib.lib()
+    p = _lib.nbx_params()
+    L.nbx_params_default(ctypes.byref(p))
+    assert p.moments_mode == 0 and p.key_order == 0 and p.node_capacity == 0
+    for field, bad in (("moments_mode", 3), ("moments_mode", -1), ("key_order", 2), ("walk_variant", 4)):
+        q = _lib.nbx_params()
+        L.nbx_params_default(ctypes.byref(q))
+        setattr(q, field, bad)
+        h = ctypes.c_void_p()
+        assert L.nbx_create(ctypes.byref(q), ctypes.byref(h)) == 1, field
