@@ -423,6 +423,28 @@ def test_moments_modes_match_oracle(cuda, mode):
         _check_tree(ctx.export_tree(j), O.build(q.x, q.y, q.z, q.m))
 
 
+def test_sort_with_full_size_tiles(cuda):
+    """2^22 bodies: the radix sort runs with 2048-key tiles (smaller systems use
+    256..1024) for the bodies and the node entries.  The permutation equals the
+    oracle's 42-level key order and the tree's moments sum to the total mass."""
+    n = 1 << 22
+    b = ic.binary_disk(n, seed=ic.SEED0 + 51)
+    ctx = _ctx(n, theta=0.5, eps=0.005)
+    ctx.set_systems([0, n])
+    s = _state(b)
+    ctx.build(s)
+    ctx.sync()
+    keys, perm = ctx.export_keys()
+    bb = O.bbox(b.x, b.y, b.z)
+    hi, lo = O.keys(b.x, b.y, b.z, bb, 42)
+    assert np.array_equal(perm, np.lexsort((lo, hi)))
+    assert np.array_equal(keys, hi[perm])
+    gt = ctx.export_tree(0)
+    roots = gt["root_child"][gt["root_child"] >= n] - n
+    total = gt["cell_m"][roots].astype(np.float64).sum() + b.m[gt["root_child"][(gt["root_child"] >= 0) & (gt["root_child"] < n)]].sum()
+    assert abs(total - b.m.astype(np.float64).sum()) < 1e-5
+
+
 def test_autotune_picks_a_valid_config(cuda, tmp_path, monkeypatch):
     from nns_gb300 import autotune
     monkeypatch.setenv("NBX_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
