@@ -65,6 +65,16 @@ struct Adj {
     int *ctx_meta = nullptr, *ctx_parent = nullptr, *ctx_val = nullptr, *ctx_body_node = nullptr;
     float fwd_ms = 0.f, bwd_ms = 0.f;
     bool tail_taped = false;  // the forward recorded the last segment into the tape
+    float *mass = nullptr;    // [n] the caller's masses, copied by the forward
+    // The steps run as CUDA graphs, captured on first use and replayed: one plain
+    // forward step, one recorded step and one reverse step per tape slot.  They
+    // read only the adjoint's own buffers, so they stay valid from call to call
+    // until the context's systems, constants or walk change (graph_gen).
+    cudaStream_t gs = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    cudaGraphExec_t g_plain = nullptr;
+    std::vector<cudaGraphExec_t> g_rec, g_rev;
+    unsigned gen = 0;
 };
 
 namespace {
@@ -490,7 +500,7 @@ int recorded_step(Ctx *ctx, Adj *a, const nbx_state *s, int j, cudaStream_t st) 
     return rc;
 }
 
-nbx_state work_state(Adj *a, const nbx_state *s) {
+nbx_state work_state(Adj *a) {
     const int n = a->n;
     nbx_state w{};
     w.x = a->work;
@@ -502,8 +512,80 @@ nbx_state work_state(Adj *a, const nbx_state *s) {
     w.ax = a->work + 6 * n;
     w.ay = a->work + 7 * n;
     w.az = a->work + 8 * n;
-    w.m = s->m;
+    w.m = a->mass;
     return w;
+}
+
+void destroy_graphs(Adj *a) {
+    if (a->g_plain) cudaGraphExecDestroy(a->g_plain);
+    a->g_plain = nullptr;
+    for (auto *v : {&a->g_rec, &a->g_rev})
+        for (cudaGraphExec_t &g : *v) {
+            if (g) cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
+
+// Replays *g on st, capturing body() into it first if it is empty.
+template <typename F>
+int replay(Ctx *ctx, cudaStream_t st, cudaGraphExec_t *g, F &&body) {
+    if (!*g) {
+        cudaGraph_t graph = nullptr;
+        NBX_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const int rc = body();
+        const cudaError_t e = cudaStreamEndCapture(st, &graph);
+        if (rc || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            if (rc) return rc;
+            ctx->last_error = std::string("adjoint graph capture: ") + cudaGetErrorString(e);
+            return NBX_ERR_CUDA;
+        }
+        const cudaError_t ei = cudaGraphInstantiate(g, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) {
+            *g = nullptr;
+            ctx->last_error = std::string("adjoint graph instantiate: ") + cudaGetErrorString(ei);
+            return NBX_ERR_CUDA;
+        }
+    }
+    NBX_CUDA(cudaGraphLaunch(*g, st));
+    return NBX_OK;
+}
+
+// The caller's stream and the adjoint's stream, ordered both ways by events.
+int enter(Ctx *ctx, Adj *a, cudaStream_t user) {
+    if (a->gen != ctx->graph_gen) {
+        destroy_graphs(a);
+        a->gen = ctx->graph_gen;
+    }
+    NBX_CUDA(cudaEventRecord(a->ev_in, user));
+    NBX_CUDA(cudaStreamWaitEvent(a->gs, a->ev_in, 0));
+    return NBX_OK;
+}
+
+int leave(Ctx *ctx, Adj *a, cudaStream_t user) {
+    ctx->built = false;  // the context's per-build arrays describe a tape's tree
+    NBX_CUDA(cudaEventRecord(a->ev_out, a->gs));
+    NBX_CUDA(cudaStreamWaitEvent(user, a->ev_out, 0));
+    return NBX_OK;
+}
+
+// One reverse step through tape slot j.
+int reverse_step(Ctx *ctx, Adj *a, int j, cudaStream_t st) {
+    const int n = a->n, NC = ctx->cap_nodes;
+    const double dt = ctx->p.dt, ddt = (double)ctx->p.dampening * ctx->p.dt;
+    TapeStep &t = a->tape[j];
+    k_adj_prep<<<grid_for(n), kB, 0, st>>>(a->lam, a->gcot, n, dt, ddt);
+    NBX_CUDA(cudaMemsetAsync(a->G, 0, sizeof(double) * 4 * (size_t)NC, st));
+    const int blocks = a->ngroups;
+    k_adj_force<<<blocks < ctx->nsm * 16 ? blocks : ctx->nsm * 16, kAdjWarps * 32, 0, st>>>(
+        t.node4, t.body4, t.val, t.body_node, ctx->d_groups, a->ngroups, ctx->d_body_sys, ctx->d_sys_off, t.lists,
+        t.list_len, a->lcap, a->gcot, n, ctx->eps2, a->G, NC, a->tdx);
+    k_adj_cells<<<grid_for(NC), kB, 0, st>>>(t.node4, t.meta, t.lvl, a->G, NC);
+    k_adj_bodies<<<grid_for(n), kB, 0, st>>>(t.body4, t.val, t.body_node, t.parent, a->G, NC, a->tdx, a->lam, n);
+    ctx->launches += 4;
+    NBX_CUDA(cudaGetLastError());
+    return NBX_OK;
 }
 
 }  // namespace
@@ -530,6 +612,16 @@ int adjoint_create(Ctx *ctx, int T, int C, int lcap, int tape_steps, Adj **out) 
     rc |= amalloc(ctx, a, &a->G, (size_t)4 * NC);
     rc |= amalloc(ctx, a, &a->loss, 2);
     rc |= amalloc(ctx, a, &a->r64, (size_t)10 * n + (size_t)4 * NC);
+    rc |= amalloc(ctx, a, &a->mass, (size_t)n);
+    if (cudaStreamCreateWithFlags(&a->gs, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&a->ev_in, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&a->ev_out, cudaEventDisableTiming) != cudaSuccess) {
+        ctx->last_error = "adjoint: stream or event creation failed";
+        rc |= NBX_ERR_CUDA;
+    }
+    a->g_rec.assign(tape_steps, nullptr);
+    a->g_rev.assign(tape_steps, nullptr);
+    a->gen = ctx->graph_gen;
     a->tape.resize(tape_steps);
     for (int j = 0; j < tape_steps && rc == 0; j++) {
         TapeStep &t = a->tape[j];
@@ -555,7 +647,11 @@ int adjoint_create(Ctx *ctx, int T, int C, int lcap, int tape_steps, Adj **out) 
 
 void adjoint_destroy(Adj *a) {
     if (!a) return;
-    void *p[] = {a->ckpt, a->work, a->target, a->lam, a->gcot, a->tdx, a->G, a->loss, a->r64};
+    destroy_graphs(a);
+    if (a->ev_in) cudaEventDestroy(a->ev_in);
+    if (a->ev_out) cudaEventDestroy(a->ev_out);
+    if (a->gs) cudaStreamDestroy(a->gs);
+    void *p[] = {a->ckpt, a->work, a->target, a->lam, a->gcot, a->tdx, a->G, a->loss, a->r64, a->mass};
     for (void *q : p)
         if (q) cudaFree(q);
     for (TapeStep &t : a->tape) {
@@ -568,94 +664,100 @@ void adjoint_destroy(Adj *a) {
 
 size_t adjoint_bytes(const Adj *a) { return a->bytes; }
 
-// Forward T steps from s (x, v, m), checkpoints every C steps; s ends at x(T), v(T).
+// Forward T steps from s (x, v, m), checkpoints every C steps; s ends at x(T), v(T)
+// (and its accelerations are those of the last step).  The steps run on the
+// adjoint's own copy of the state.
 int adjoint_forward(Ctx *ctx, Adj *a, const nbx_state *s, const float *tx, const float *ty, const float *tz,
-                    double *loss_host, cudaStream_t st) {
+                    double *loss_host, cudaStream_t user) {
     const int n = a->n;
     if (n != ctx->nbodies) return NBX_ERR_STATE;
+    int rc = enter(ctx, a, user);
+    if (rc) return rc;
+    const cudaStream_t st = a->gs;
     EventPair ev;
     if (!ev.ok) return NBX_ERR_CUDA;
-    const cudaEvent_t e0 = ev.e0, e1 = ev.e1;
-    cudaEventRecord(e0, st);
-    NBX_CUDA(cudaMemcpyAsync(a->target, tx, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
-    NBX_CUDA(cudaMemcpyAsync(a->target + n, ty, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
-    NBX_CUDA(cudaMemcpyAsync(a->target + 2 * n, tz, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+    NBX_CUDA(cudaEventRecord(ev.e0, st));
+    const float *tgt[3] = {tx, ty, tz};
+    for (int k = 0; k < 3; k++)
+        NBX_CUDA(cudaMemcpyAsync(a->target + (size_t)k * n, tgt[k], sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+    float *const caller[9] = {s->x, s->y, s->z, s->vx, s->vy, s->vz, s->ax, s->ay, s->az};
+    for (int k = 0; k < 6; k++)
+        NBX_CUDA(cudaMemcpyAsync(a->work + (size_t)k * n, caller[k], sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+    NBX_CUDA(cudaMemcpyAsync(a->mass, s->m, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+    const nbx_state w = work_state(a);
     a->tail_taped = false;
     const int k_tail = (a->nseg - 1) * a->C;  // first step of the last segment
-    for (int k = 0; k < a->T; k++) {
+    for (int k = 0; k < a->T && !rc; k++) {
         if (k % a->C == 0) {
-            k_copy_state<<<grid_for(n), kB, 0, st>>>(s->x, s->y, s->z, s->vx, s->vy, s->vz,
+            k_copy_state<<<grid_for(n), kB, 0, st>>>(w.x, w.y, w.z, w.vx, w.vy, w.vz,
                                                      a->ckpt + (size_t)(k / a->C) * 6 * n, n);
             ++ctx->launches;
         }
-        int rc;
         if (k >= k_tail) {
-            rc = recorded_step(ctx, a, s, k - k_tail, st);
+            const int j = k - k_tail;
+            rc = replay(ctx, st, &a->g_rec[j], [&] { return recorded_step(ctx, a, &w, j, st); });
         } else {
-            rc = build_tree(ctx, s, st, false, nullptr);
-            if (!rc) rc = walk2_plain64(ctx, s, st);
-            if (!rc) rc = integrate(ctx, s, ctx->p.dt, ctx->p.dampening, n, st);
+            rc = replay(ctx, st, &a->g_plain, [&] {
+                int r = build_tree(ctx, &w, st, false, nullptr);
+                if (!r) r = walk2_plain64(ctx, &w, st);
+                if (!r) r = integrate(ctx, &w, ctx->p.dt, ctx->p.dampening, n, st);
+                return r;
+            });
         }
-        if (rc) return rc;
+    }
+    if (rc) {
+        leave(ctx, a, user);
+        return rc;
     }
     a->tail_taped = true;
+    for (int k = 0; k < 9; k++)
+        NBX_CUDA(cudaMemcpyAsync(caller[k], a->work + (size_t)k * n, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
     NBX_CUDA(cudaMemsetAsync(a->loss, 0, sizeof(double), st));
-    k_loss_init<<<grid_for(n), kB, 0, st>>>(s->x, s->y, s->z, a->target, n, a->lam, a->loss);
+    k_loss_init<<<grid_for(n), kB, 0, st>>>(w.x, w.y, w.z, a->target, n, a->lam, a->loss);
     ++ctx->launches;
-    cudaEventRecord(e1, st);
+    NBX_CUDA(cudaEventRecord(ev.e1, st));
     NBX_CUDA(cudaMemcpyAsync(loss_host, a->loss, sizeof(double), cudaMemcpyDeviceToHost, st));
     NBX_CUDA(cudaStreamSynchronize(st));
-    cudaEventElapsedTime(&a->fwd_ms, e0, e1);
-    return NBX_OK;
+    cudaEventElapsedTime(&a->fwd_ms, ev.e0, ev.e1);
+    return leave(ctx, a, user);
 }
 
 // Reverse through all segments; writes dL/dx0, dL/dv0, dL/dm (original order).
 int adjoint_backward(Ctx *ctx, Adj *a, const nbx_state *s, float *gx, float *gy, float *gz, float *gvx, float *gvy,
-                     float *gvz, float *gm, cudaStream_t st) {
+                     float *gvz, float *gm, cudaStream_t user) {
+    (void)s;  // the reverse pass works on the forward's copy of the state
     const int n = a->n;
-    const int NC = ctx->cap_nodes;
-    const double dt = ctx->p.dt, ddt = (double)ctx->p.dampening * ctx->p.dt;
-    nbx_state w = work_state(a, s);
+    int rc = enter(ctx, a, user);
+    if (rc) return rc;
+    const cudaStream_t st = a->gs;
+    const nbx_state w = work_state(a);
     EventPair ev;
     if (!ev.ok) return NBX_ERR_CUDA;
-    const cudaEvent_t e0 = ev.e0, e1 = ev.e1;
-    cudaEventRecord(e0, st);
-    for (int seg = a->nseg - 1; seg >= 0; seg--) {
+    NBX_CUDA(cudaEventRecord(ev.e0, st));
+    for (int seg = a->nseg - 1; seg >= 0 && !rc; seg--) {
         const int k0 = seg * a->C;
         const int steps = (k0 + a->C <= a->T) ? a->C : a->T - k0;
         if (!(seg == a->nseg - 1 && a->tail_taped)) {
             NBX_CUDA(cudaMemcpyAsync(a->work, a->ckpt + (size_t)seg * 6 * n, sizeof(float) * 6 * n,
                                      cudaMemcpyDeviceToDevice, st));
-            for (int j = 0; j < steps; j++) {
-                int rc = recorded_step(ctx, a, &w, j, st);
-                if (rc) {
-                    a->tail_taped = false;
-                    return rc;
-                }
-            }
+            for (int j = 0; j < steps && !rc; j++)
+                rc = replay(ctx, st, &a->g_rec[j], [&] { return recorded_step(ctx, a, &w, j, st); });
         }
         a->tail_taped = false;  // the tape now holds this segment
-        for (int j = steps - 1; j >= 0; j--) {
-            TapeStep &t = a->tape[j];
-            k_adj_prep<<<grid_for(n), kB, 0, st>>>(a->lam, a->gcot, n, dt, ddt);
-            NBX_CUDA(cudaMemsetAsync(a->G, 0, sizeof(double) * 4 * (size_t)NC, st));
-            const int blocks = a->ngroups;
-            k_adj_force<<<blocks < ctx->nsm * 16 ? blocks : ctx->nsm * 16, kAdjWarps * 32, 0, st>>>(
-                t.node4, t.body4, t.val, t.body_node, ctx->d_groups, a->ngroups, ctx->d_body_sys, ctx->d_sys_off,
-                t.lists, t.list_len, a->lcap, a->gcot, n, ctx->eps2, a->G, NC, a->tdx);
-            k_adj_cells<<<grid_for(NC), kB, 0, st>>>(t.node4, t.meta, t.lvl, a->G, NC);
-            k_adj_bodies<<<grid_for(n), kB, 0, st>>>(t.body4, t.val, t.body_node, t.parent, a->G, NC, a->tdx,
-                                                      a->lam, n);
-            ctx->launches += 4;
-        }
+        for (int j = steps - 1; j >= 0 && !rc; j--)
+            rc = replay(ctx, st, &a->g_rev[j], [&] { return reverse_step(ctx, a, j, st); });
+    }
+    if (rc) {
+        leave(ctx, a, user);
+        return rc;
     }
     k_lam_out<<<grid_for(n), kB, 0, st>>>(a->lam, n, gx, gy, gz, gvx, gvy, gvz, gm);
     ++ctx->launches;
-    cudaEventRecord(e1, st);
+    NBX_CUDA(cudaEventRecord(ev.e1, st));
     NBX_CUDA(cudaStreamSynchronize(st));
-    cudaEventElapsedTime(&a->bwd_ms, e0, e1);
+    cudaEventElapsedTime(&a->bwd_ms, ev.e0, ev.e1);
     NBX_CUDA(cudaGetLastError());
-    return NBX_OK;
+    return leave(ctx, a, user);
 }
 
 // Records the whole T-step trajectory from s (needs tape_steps >= T).
@@ -663,13 +765,15 @@ int adjoint_record_all(Ctx *ctx, Adj *a, const nbx_state *s, cudaStream_t st) {
     if (a->tape_steps < a->T) return NBX_ERR_ARG;
     a->tail_taped = false;
     const int n = a->n;
-    nbx_state w = work_state(a, s);
+    const nbx_state w = work_state(a);
     k_copy_state<<<grid_for(n), kB, 0, st>>>(s->x, s->y, s->z, s->vx, s->vy, s->vz, a->work, n);
     ++ctx->launches;
+    NBX_CUDA(cudaMemcpyAsync(a->mass, s->m, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
     for (int k = 0; k < a->T; k++) {
         int rc = recorded_step(ctx, a, &w, k, st);
         if (rc) return rc;
     }
+    ctx->built = false;
     NBX_CUDA(cudaStreamSynchronize(st));
     return NBX_OK;
 }

@@ -299,11 +299,12 @@ int nbx_get_constants(nbx_ctx *c, float *theta_ref, float *eps2) {
 
 int nbx_set_constants(nbx_ctx *c, float theta_ref, float eps2, int compensated) {
     if (!c || !(theta_ref > 0.f) || !(eps2 >= 0.f)) return NBX_ERR_ARG;
+    if (compensated < 0 || compensated > 2) return NBX_ERR_ARG;
     Ctx *ctx = C(c);
     ctx->theta_ref = theta_ref;
     ctx->eps2 = eps2;
-    if (compensated < 0 || compensated > 2) return NBX_ERR_ARG;
     ctx->compensated = compensated;
+    ++ctx->graph_gen;
     if (ctx->graph_exec) {
         cudaGraphExecDestroy(ctx->graph_exec);
         ctx->graph_exec = nullptr;
@@ -318,6 +319,7 @@ int nbx_set_walk_config(nbx_ctx *c, int warps_per_block, int variant) {
     Ctx *ctx = C(c);
     ctx->walk_warps = warps_per_block;
     ctx->walk_variant = variant;
+    ++ctx->graph_gen;
     if (ctx->graph_exec) {
         cudaGraphExecDestroy(ctx->graph_exec);
         ctx->graph_exec = nullptr;
@@ -368,6 +370,7 @@ int nbx_set_systems(nbx_ctx *c, int nsys, const int64_t *offsets) {
     ctx->ngroups = (int)groups.size();
     ctx->built = false;
     ctx->ref_m = 0;
+    ++ctx->graph_gen;
     if (ctx->graph_exec) {
         cudaGraphExecDestroy(ctx->graph_exec);
         ctx->graph_exec = nullptr;

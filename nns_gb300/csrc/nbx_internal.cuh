@@ -122,6 +122,7 @@ struct Ctx {
 
     // graph
     cudaGraphExec_t graph_exec = nullptr;
+    unsigned graph_gen = 0;  // bumped whenever captured launches go stale (systems, constants, walk)
     nbx_state graph_state{};
     int graph_nsys = -1;
     cudaStream_t graph_stream = nullptr;
