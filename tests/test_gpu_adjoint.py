@@ -86,6 +86,29 @@ def test_forward_steps_with_the_recording_walk(cuda):
         assert np.array_equal(got, want)
 
 
+def test_step_graphs_follow_context_changes(cuda):
+    """The adjoint replays captured step graphs; after the context's constants
+    change it recaptures them, so its forward ends where a fresh adjoint's does
+    (the forward's end state is deterministic: compared bit for bit)."""
+    from nns_gb300.adjoint import Adjoint
+    from nns_gb300.barnes_hut import State
+    b, ctx, adj, target = _setup(1024, 6, 3)
+
+    def end_state(a):
+        s = State.from_bodies(b)
+        a.forward(s, target)
+        return s.host()
+
+    p1 = end_state(adj)
+    assert all(np.array_equal(u, v) for u, v in zip(end_state(adj), p1))  # replayed graphs
+    t, e2 = ctx.constants()
+    ctx.set_constants(t, 4 * e2, 0)
+    p2 = end_state(adj)
+    assert not np.array_equal(p2[3], p1[3])
+    p3 = end_state(Adjoint(ctx, 6, 3, 8192, 3))
+    assert all(np.array_equal(u, v) for u, v in zip(p2, p3))
+
+
 def test_checkpoint_interval_does_not_change_gradients(cuda):
     b, ctx, adj5, target = _setup(1024, 12, 4)
     _, g4 = _grads(b, adj5, target)
