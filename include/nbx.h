@@ -48,7 +48,7 @@ extern "C" {
 typedef struct nbx_ctx nbx_ctx;
 
 typedef struct nbx_params {
-    int max_bodies;    /* capacity: total bodies over all systems (<= 2^25) */
+    int max_bodies;    /* capacity: total bodies over all systems (<= 2^26) */
     int max_systems;   /* capacity: independent systems */
     float theta;       /* opening angle: a cell of x-side s at squared distance r
                           (softened) is accepted when s^2 / theta^2 <= r, i.e. the

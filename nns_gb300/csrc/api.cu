@@ -81,7 +81,7 @@ void free_all(Ctx *ctx) {
                     ctx->d_root_nch, ctx->d_key, ctx->d_key_alt, ctx->d_key_lo, ctx->d_val, ctx->d_val_alt,
                     ctx->d_body4, ctx->d_delta, ctx->d_ecount, ctx->d_body_node, ctx->d_nlist, ctx->d_nopen,
                     ctx->d_ent, ctx->d_ent_alt, ctx->d_flags, ctx->d_node4, ctx->d_meta, ctx->d_parent,
-                    ctx->d_sums, ctx->d_count, ctx->d_arrive, ctx->d_fcl, ctx->d_cl, ctx->d_hist,
+                    ctx->d_sums, ctx->d_count, ctx->d_arrive, ctx->d_lvl8, ctx->d_fcl, ctx->d_cl, ctx->d_hist,
                     ctx->d_scan_blk, ctx->d_totals, ctx->d_totals64, ctx->d_status};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -180,7 +180,7 @@ const char *nbx_last_error(nbx_ctx *c) { return c ? C(c)->last_error.c_str() : "
 int nbx_create(const nbx_params *p, nbx_ctx **out) {
     if (!p || !out) return NBX_ERR_ARG;
     *out = nullptr;
-    if (p->max_bodies < 1 || p->max_bodies > (1 << 25) || p->max_systems < 1 ||
+    if (p->max_bodies < 1 || p->max_bodies > (1 << 26) || p->max_systems < 1 ||
         p->max_systems > p->max_bodies || p->group != 32 || p->leaf_size != 1 || p->radix_bits != 8 ||
         p->stack_depth < 360 || p->stack_depth > 4096 || p->walk_variant < 0 || p->walk_variant > 3 ||
         p->moments_mode < 0 || p->moments_mode > 2)
@@ -260,6 +260,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     rc |= nbx::dmalloc(ctx, &ctx->d_sums, NC);
     rc |= nbx::dmalloc(ctx, &ctx->d_count, NC);
     rc |= nbx::dmalloc(ctx, &ctx->d_arrive, NC);
+    rc |= nbx::dmalloc(ctx, &ctx->d_lvl8, NC);
     rc |= nbx::dmalloc(ctx, &ctx->d_fcl, (size_t)NC + Ss + 2);
     rc |= nbx::dmalloc(ctx, &ctx->d_cl, (size_t)NC + Ss + 2);
     rc |= nbx::dmalloc(ctx, &ctx->d_hist, hist + 1);  // + the scanned total

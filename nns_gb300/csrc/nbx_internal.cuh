@@ -31,8 +31,8 @@ inline int tile_for(long long n, int nsm) {
 constexpr int kRadixBins = 256;   // 8-bit digits
 constexpr int kMaxLevel = 43;     // 42 key levels + the body level
 constexpr int kBodyFlag = int(0x80000000u);
-constexpr int kLevelShift = 26;   // walk stack entry = node | level << 26
-constexpr int kMaxNodes = 1 << 26;
+constexpr int kLevelShift = 26;   // build node entry = level << 26 | sorted position
+constexpr int kMaxNodes = 1 << 28; // cells + bodies: meta's first-child field has 28 bits
 constexpr int kScanItems = 4096;  // elements per scan block (1024 threads x 4)
 constexpr int kMaxRun = 4096;     // longest run of equal 21-level keys refined
 
@@ -103,6 +103,7 @@ struct Ctx {
     double4 *d_sums = nullptr;                        // [NC] m, m*x, m*y, m*z (FP64)
     int *d_count = nullptr;                           // [NC]
     int *d_arrive = nullptr;                          // [NC]
+    unsigned char *d_lvl8 = nullptr;                  // [NC] tree level of each node (root children: 1)
     int *d_fcl = nullptr;                             // [NC+S+1] first-child list
     int *d_cl = nullptr;                              // [NC+S] cell list (BFS index)
 

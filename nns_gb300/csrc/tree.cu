@@ -347,7 +347,8 @@ __global__ void __launch_bounds__(kBlock) k_nodes_a(const unsigned *__restrict__
                                                      int *__restrict__ fcl, int *__restrict__ cl,
                                                      float4 *__restrict__ node4, int *__restrict__ meta,
                                                      int *__restrict__ body_node, int *__restrict__ count,
-                                                     int *__restrict__ arrive, DevStatus *st) {
+                                                     int *__restrict__ arrive, unsigned char *__restrict__ lvl8,
+                                                     DevStatus *st) {
     const int T = (int)totals[1];
     if (grid_stride_start() == 0) {
         const unsigned long long tot = totals64[0];
@@ -362,6 +363,7 @@ __global__ void __launch_bounds__(kBlock) k_nodes_a(const unsigned *__restrict__
         const unsigned long long ex = flags_ex[b];
         if (f) fcl[(int)(ex & 0xffffffffull)] = b;
         arrive[b] = 0;
+        lvl8[b] = (unsigned char)l;
         if (c) {
             cl[nsys + (int)(ex >> 32)] = b;
         } else {
@@ -615,7 +617,7 @@ int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox
     k_nodes_a<<<gn, kBlock, 0, st>>>(ctx->d_ent_alt, ctx->d_totals, ctx->d_totals64, ctx->d_body_sys,
                                      ctx->d_sys_off, ctx->d_delta, ctx->d_flags, ctx->d_body4, S, ctx->d_fcl,
                                      ctx->d_cl, ctx->d_node4, ctx->d_meta, ctx->d_body_node, ctx->d_count,
-                                     ctx->d_arrive, ctx->d_status);
+                                     ctx->d_arrive, ctx->d_lvl8, ctx->d_status);
     ++ctx->launches;
     k_nodes_b<<<gn, kBlock, 0, st>>>(ctx->d_ent_alt, ctx->d_totals, ctx->d_body_sys, ctx->d_sys_off,
                                      ctx->d_delta, ctx->d_flags, S, ctx->d_fcl, ctx->d_cl, ctx->d_meta,

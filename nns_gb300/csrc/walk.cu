@@ -87,7 +87,8 @@ __device__ __forceinline__ void interact(A &acc, float cx, float cy, float cz, f
 
 template <int Mode>
 __global__ void __launch_bounds__(kWalkWarps * 32)
-    k_walk(const float4 *__restrict__ node4, const int *__restrict__ meta, const float4 *__restrict__ body4,
+    k_walk(const float4 *__restrict__ node4, const int *__restrict__ meta, const unsigned char *__restrict__ lvl8,
+           const float4 *__restrict__ body4,
            const int *__restrict__ val, const int *__restrict__ groups, int ngroups,
            const int *__restrict__ body_sys, const int *__restrict__ sys_off, const float *__restrict__ depth0,
            const int *__restrict__ root_first, const int *__restrict__ root_nch, float eps2, int stack_cap,
@@ -131,7 +132,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32)
                     interact<Mode>(acc, cx, cy, cz, cw, dx, dy, dz, r, me, eps2);
                     len++;
                 } else {
-                    if (lane == 0) stack[top] = (first + j) | (1 << kLevelShift);
+                    if (lane == 0) stack[top] = first + j;
                     top++;
                     opened++;
                 }
@@ -140,11 +141,10 @@ __global__ void __launch_bounds__(kWalkWarps * 32)
         }
 
         while (top > 0) {
-            const int e = stack[top - 1];
+            const int b = stack[top - 1];  // stack entries are node indices
             __syncwarp();
             top--;
-            const int b = e & ((1 << kLevelShift) - 1);
-            const int lvl = (int)((unsigned)e >> kLevelShift);  // levels 32..42 set the sign bit
+            const int lvl = lvl8[b];
             const int mb = meta[b];
             const int first = mb & 0x0fffffff;
             const int nch = ((mb >> 28) & 7) + 1;
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32)
                         overflow = true;
                         break;
                     }
-                    if (lane == 0) stack[top] = (first + j) | ((lvl + 1) << kLevelShift);
+                    if (lane == 0) stack[top] = first + j;
                     top++;
                     opened++;
                 }
@@ -238,13 +238,13 @@ int walk_forces(Ctx *ctx, const nbx_state *s, cudaStream_t st) {
     if (grid <= 0) return NBX_OK;
     if (ctx->compensated) {
         k_walk<1><<<grid, kWalkWarps * 32, smem, st>>>(
-            ctx->d_node4, ctx->d_meta, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
+            ctx->d_node4, ctx->d_meta, ctx->d_lvl8, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
             ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay,
             s->az, ctx->d_nlist, ctx->d_nopen, ctx->d_status, nullptr, 0);
         ++ctx->launches;
     } else {
         k_walk<0><<<grid, kWalkWarps * 32, smem, st>>>(
-            ctx->d_node4, ctx->d_meta, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
+            ctx->d_node4, ctx->d_meta, ctx->d_lvl8, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
             ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay,
             s->az, ctx->d_nlist, ctx->d_nopen, ctx->d_status, nullptr, 0);
         ++ctx->launches;
@@ -264,7 +264,7 @@ int walk_fp64_lists(Ctx *ctx, const int *group_starts, int ngroups, double *a64,
     const int blocks_needed = ceil_div(ngroups, kWalkWarps);
     const int grid = blocks_needed < ctx->nsm * 8 ? blocks_needed : ctx->nsm * 8;
     k_walk<2><<<grid, kWalkWarps * 32, smem, st>>>(
-        ctx->d_node4, ctx->d_meta, ctx->d_body4, ctx->d_val, group_starts, ngroups, ctx->d_body_sys, ctx->d_sys_off,
+        ctx->d_node4, ctx->d_meta, ctx->d_lvl8, ctx->d_body4, ctx->d_val, group_starts, ngroups, ctx->d_body_sys, ctx->d_sys_off,
         ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, nullptr, nullptr, nullptr, nullptr,
         nullptr, ctx->d_status, a64, (int)ctx->nbodies);
     ++ctx->launches;

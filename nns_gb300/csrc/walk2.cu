@@ -85,7 +85,7 @@ struct WarpBuf {
     ulonglong2 ca[kPairs];  // cells:  (x0,x1) (y0,y1)
     ulonglong2 cb[kPairs];  //         (z0,z1) (m0,m1)
     u64 cd[kPairs];         //         (dp0,dp1)
-    int cid[CB];            //         node | level << 26
+    int cid[CB];            //         node index
     int bid[CB];            // body node ids (interaction-list recording only)
     float4 cls[3];          // group box lo, hi, centre
     ulonglong2 rxy[8];      // representative bodies, in pairs: (x0,x1) (y0,y1)
@@ -139,7 +139,8 @@ struct WalkBounds {
 
 template <int CB, int Mode, bool Pot, bool Rec>
 __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMinBlocks)
-    k_walk2(const float4 *__restrict__ node4, const int *__restrict__ meta, const float4 *__restrict__ body4,
+    k_walk2(const float4 *__restrict__ node4, const int *__restrict__ meta, const unsigned char *__restrict__ lvl8,
+            const float4 *__restrict__ body4,
             const int *__restrict__ val, const int *__restrict__ groups, int ngroups,
             const int *__restrict__ body_sys, const int *__restrict__ sys_off, const float *__restrict__ depth0,
             const int *__restrict__ root_first, const int *__restrict__ root_nch, float eps2, int stack_cap,
@@ -241,7 +242,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 put4(buf.ba, buf.bb, __popc(bodies & lt), q);
                 if (Rec) buf.bid[__popc(bodies & lt)] = rf + lane;
             }
-            if (lane < rn && cm >= 0) stack[__popc(cells & lt)] = (rf + lane) | (1 << kLevelShift);
+            if (lane < rn && cm >= 0) stack[__popc(cells & lt)] = rf + lane;
             nb = __popc(bodies);
             top = __popc(cells);
             opened += top;
@@ -256,9 +257,8 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             const int avail = min(top, 32);
             int first = 0, nch = 0, lvl = 0;
             if (lane < avail) {
-                const int e = stack[top - 1 - lane];
-                const int b = e & ((1 << kLevelShift) - 1);
-                lvl = (int)((unsigned)e >> kLevelShift);  // levels 32..42 set the sign bit
+                const int b = stack[top - 1 - lane];  // stack entries are node indices
+                lvl = lvl8[b];
                 const int mb = meta[b];
                 first = mb & 0x0fffffff;
                 nch = ((mb >> 28) & 7) + 1;
@@ -356,9 +356,9 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                     const int slot = ncell + __popc(cmk & lt);
                     put4(buf.ca, buf.cb, slot, q);
                     reinterpret_cast<float *>(&buf.cd[slot >> 1])[slot & 1] = dpc;
-                    buf.cid[slot] = c | ((lj + 1) << kLevelShift);  // children are at level lj+1
+                    buf.cid[slot] = c;
                 }
-                if (tos) stack[top + nsrej + __popc(smk & lt)] = c | ((lj + 1) << kLevelShift);
+                if (tos) stack[top + nsrej + __popc(smk & lt)] = c;
                 nbody += __popc(bm);
                 ncell += __popc(cmk);
                 nsrej += __popc(smk);
@@ -432,14 +432,14 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                     if (lane == 0) stack[top + nrej] = buf.cid[2 * q];
                     nrej++;
                 } else if (Rec && 2 * q < ncell) {
-                    if (lane == 0 && nrec < rec_cap) rec[nrec] = buf.cid[2 * q] & ((1 << kLevelShift) - 1);
+                    if (lane == 0 && nrec < rec_cap) rec[nrec] = buf.cid[2 * q];
                     nrec++;
                 }
                 if (!okb) {
                     if (lane == 0) stack[top + nrej] = buf.cid[2 * q + 1];
                     nrej++;
                 } else if (Rec && 2 * q + 1 < ncell) {
-                    if (lane == 0 && nrec < rec_cap) rec[nrec] = buf.cid[2 * q + 1] & ((1 << kLevelShift) - 1);
+                    if (lane == 0 && nrec < rec_cap) rec[nrec] = buf.cid[2 * q + 1];
                     nrec++;
                 }
             }
@@ -524,7 +524,7 @@ int launch(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st,
     if (grid <= 0) return NBX_OK;
     NBX_CUDA(cudaMemsetAsync(&ctx->d_status->walk_next, 0, sizeof(unsigned), st));
     k_walk2<CB, Mode, Pot, Rec><<<grid, warps * 32, smem, st>>>(
-        ctx->d_node4, ctx->d_meta, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
+        ctx->d_node4, ctx->d_meta, ctx->d_lvl8, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
         ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay, s->az,
         pot, ctx->d_nlist, ctx->d_nopen, ctx->d_status, rec_list, rec_len, rec_cap);
     ++ctx->launches;

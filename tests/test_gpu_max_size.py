@@ -1,5 +1,5 @@
-"""The largest context: 2^25 bodies (nbx_params.max_bodies' limit), where node
-indices fill the 26 bits of the walk's stack entries.  One full step runs
+"""The largest context: 2^26 bodies (nbx_params.max_bodies' limit), about 10^8
+nodes, so node indices need more than 26 bits.  One full step runs
 without a device error; the forces equal an FP64 evaluation of the same
 interaction lists within the walk tolerance and the Barnes-Hut error against
 an FP64 direct sum is the usual one."""
@@ -13,8 +13,9 @@ pytestmark = pytest.mark.gpu
 
 def test_max_size_step(cuda):
     from nns_gb300.barnes_hut import Context, State
-    n = 1 << 25
-    b = ic.binary_disk(n)
+    n = 1 << 26
+    # the benchmark's system (2^24 disk bodies of 1e-8): the same total disk mass
+    b = ic.binary_disk(n, disk_mass=1e-8 * (1 << 24) / n)
     ctx = Context(max_bodies=n, theta=0.5, eps=0.005, dt=5e-4)
     ctx.set_systems([0, n])
     s = State.from_bodies(b)
