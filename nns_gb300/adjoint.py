@@ -41,7 +41,12 @@ class Adjoint:
             pass
 
     def forward(self, s: State, target: torch.Tensor, stream=None) -> float:
-        """T steps from s (advanced in place); loss against target (3, n) on the device."""
+        """T steps from s (advanced in place); loss against target (3, n) on the device.
+
+        The steps run on the adjoint's own copy of the state, as replayed CUDA
+        graphs on the adjoint's stream (ordered after ``stream``); the call
+        returns when the loss is known.  The context needs a new build before
+        its next walk."""
         t = target.contiguous()
         loss = C.c_double()
         check(lib().nbx_adjoint_forward(self.ctx.h, self.h, C.byref(s.c), t[0].data_ptr(),
@@ -51,7 +56,7 @@ class Adjoint:
         return loss.value
 
     def backward(self, s: State, stream=None):
-        """(dL/dx0 (3,n), dL/dv0 (3,n), dL/dm (n,)) as device tensors."""
+        """(dL/dx0 (3,n), dL/dv0 (3,n), dL/dm (n,)) of the last forward, as device tensors."""
         n = s.x.numel()
         g = torch.empty(7, n, dtype=torch.float32, device=s.x.device)
         check(lib().nbx_adjoint_backward(self.ctx.h, self.h, C.byref(s.c),

@@ -35,7 +35,11 @@ def _stream_ptr(stream) -> int | None:
 
 
 class Context:
-    """One libnbx context: tree scratch for up to ``max_bodies`` bodies."""
+    """One libnbx context: tree scratch for up to ``max_bodies`` bodies (<= 2^26).
+
+    ``key_order`` 1 orders bodies along the Hilbert curve (faster walk; lists
+    differ from the reference's); ``moments_mode`` picks the centre-of-mass pass
+    (0 by size, 1 per tree level, 2 one launch), all with the same sums."""
 
     def __init__(self, max_bodies: int, max_systems: int = 1, theta: float = 0.5,
                  theta_ref: float | None = None, eps: float = 0.05, eps2: float | None = None,
