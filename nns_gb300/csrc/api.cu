@@ -183,7 +183,8 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     if (p->max_bodies < 1 || p->max_bodies > (1 << 26) || p->max_systems < 1 ||
         p->max_systems > p->max_bodies || p->group != 32 || p->leaf_size != 1 || p->radix_bits != 8 ||
         p->stack_depth < 360 || p->stack_depth > 4096 || p->walk_variant < 0 || p->walk_variant > 3 ||
-        p->moments_mode < 0 || p->moments_mode > 2)
+        p->moments_mode < 0 || p->moments_mode > 2 ||
+        (p->node_capacity != 0 && (p->node_capacity < p->max_bodies + 1 || p->node_capacity > nbx::kMaxNodes)))
         return NBX_ERR_ARG;
     Ctx *ctx = new (std::nothrow) Ctx();
     if (!ctx) return NBX_ERR_NOMEM;
@@ -210,10 +211,6 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     const int B = p->max_bodies, Ss = p->max_systems;
     ctx->cap_bodies = B;
     ctx->cap_sys = Ss;
-    if (p->node_capacity != 0 && (p->node_capacity < B + 1 || p->node_capacity > nbx::kMaxNodes)) {
-        delete ctx;
-        return NBX_ERR_ARG;
-    }
     const int64_t nc = p->node_capacity ? (int64_t)p->node_capacity : 2ll * B + 65536;
     ctx->cap_nodes = (int)(nc < nbx::kMaxNodes ? nc : nbx::kMaxNodes);
     // a tile below kTile is only chosen while there are fewer than 2 * want tiles

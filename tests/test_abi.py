@@ -61,3 +61,16 @@ def test_params_layout_and_option_ranges_without_gpu():
         setattr(q, field, bad)
         h = ctypes.c_void_p()
         assert L.nbx_create(ctypes.byref(q), ctypes.byref(h)) == 1, field
+
+
+def test_capacity_bounds_without_gpu():
+    """max_bodies above 2^26 and node pools above 2^28 are rejected before any CUDA call."""
+    from nns_gb300 import _lib
+    L = _lib.lib()
+    for field, bad in (("max_bodies", (1 << 26) + 1), ("node_capacity", (1 << 28) + 1)):
+        q = _lib.nbx_params()
+        L.nbx_params_default(ctypes.byref(q))
+        q.max_bodies = 1 << 20
+        setattr(q, field, bad)
+        h = ctypes.c_void_p()
+        assert L.nbx_create(ctypes.byref(q), ctypes.byref(h)) == 1, field

@@ -210,6 +210,36 @@ def test_batched_equals_unbatched(cuda):
             assert np.array_equal(t1[k], tb[k]), (i, k)
 
 
+def test_batched_equals_unbatched_hilbert(cuda):
+    """Hilbert keys (key_order 1): each system of a batch equals its own
+    single-system run bit for bit (keys, tree and forces)."""
+    from nns_gb300.barnes_hut import Context
+    sizes = [3000, 41, 5000, 700]
+    parts = [ic.plummer(k, seed=ic.SEED0 + 60 + i) for i, k in enumerate(sizes)]
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    cat = lambda k: np.concatenate([getattr(p, k) for p in parts])  # noqa: E731
+    B = ic.Bodies(cat("x"), cat("y"), cat("z"), cat("vx"), cat("vy"), cat("vz"), cat("m"))
+    ctx = Context(max_bodies=int(off[-1]), max_systems=len(sizes), theta=0.5, eps=0.01, key_order=1)
+    ctx.set_systems(off)
+    s = _state(B)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    accb = s.acc()
+    keys_b, _ = ctx.export_keys()
+    for i, p in enumerate(parts):
+        n = len(p.x)
+        c1 = Context(max_bodies=n, theta=0.5, eps=0.01, key_order=1)
+        c1.set_systems([0, n])
+        s1 = _state(p)
+        c1.build(s1)
+        c1.forces(s1)
+        c1.sync()
+        assert np.array_equal(accb[off[i]:off[i + 1]], s1.acc()), i
+        k1, _ = c1.export_keys()
+        assert np.array_equal(keys_b[off[i]:off[i + 1]], k1), i
+
+
 def test_graph_step_equals_eager(cuda):
     b = ic.star_disk(4096)
     n = len(b.x)
