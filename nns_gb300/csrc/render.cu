@@ -167,6 +167,7 @@ extern "C" int nbx_render_frame(nbx_ctx *c, const nbx_state *s, int n, const nbx
         return NBX_ERR_ARG;
     if (p->width < 1 || p->height < 1 || p->dot_size < 0 || p->dot_size > nbx::kMaxDot ||
         !(p->system_size > 0.0) || !(p->render_scale > 0.0) || !(p->max_velocity_color > 0.0) ||
+        !(p->particle_brightness >= 0.0) ||
         (long long)p->width * p->height > (1ll << 28))
         return NBX_ERR_ARG;
     Ctx *ctx = reinterpret_cast<Ctx *>(c);
