@@ -276,7 +276,7 @@ typedef struct nbx_render_params {
     double render_scale;        /* RENDER_SCALE */
     double max_velocity_color;  /* MAX_VEL_COLOR */
     double min_velocity_color;  /* MIN_VEL_COLOR */
-    double particle_brightness; /* PARTICLE_BRIGHTNESS */
+    double particle_brightness; /* PARTICLE_BRIGHTNESS (>= 0) */
     double particle_sharpness;  /* PARTICLE_SHARPNESS */
     int dot_size;               /* DOT_SIZE (<= 16) */
     double system_size;         /* > 0; main.cu:95 passes 2 * BarnesHut::getSystemSize() */
