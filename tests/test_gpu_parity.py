@@ -566,8 +566,9 @@ def test_hilbert_order_option(cuda):
     assert np.median(_rel(acc_h, acc_m)) < 1e-3
 
 
+@pytest.mark.parametrize("variant", [3, 2], ids=["walk96", "walk1"])
 @pytest.mark.parametrize("name", ["collinear", "coplanar", "signed_zeros", "cluster", "deep"])
-def test_adversarial_geometry(cuda, name):
+def test_adversarial_geometry(cuda, name, variant):
     """Degenerate boxes, signed zeros, bodies on split planes, a tight cluster
     and MAC decisions on cells past level 32 (the oracle is pinned to the
     reference kernels on the same sets).
@@ -576,6 +577,7 @@ def test_adversarial_geometry(cuda, name):
     b = CASES[name]()
     n = len(b.x)
     ctx = _ctx(n, theta=0.5, eps=EPS.get(name, 0.01))
+    ctx.set_walk(8, variant)
     ctx.set_systems([0, n])
     s = _state(b)
     ctx.build(s)
