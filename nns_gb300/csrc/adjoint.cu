@@ -149,6 +149,16 @@ __global__ void k_adj_prep(double *lam, float *gcot, int n, double dt, double dd
 #define NBX_ADJ_WARPS 8
 #endif
 constexpr int kAdjWarps = NBX_ADJ_WARPS;  // warps sharing one group's list
+
+// Asynchronous 16-byte global-to-shared copies (cp.async, sm_80+): the copy
+// proceeds while the warp computes; wait_group orders it before the reads.
+__device__ __forceinline__ void cp_async16(float4 *dst, const float4 *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 constexpr int kChunk = 8;
 constexpr int kRedStride = 36;
 
@@ -159,6 +169,7 @@ __global__ void __launch_bounds__(kAdjWarps * 32)
                 const int *__restrict__ list_len, int lcap, const float *__restrict__ gcot, int n, float eps2,
                 double *__restrict__ G, int nc_cap, float *__restrict__ tdx) {
     __shared__ __align__(16) float red[kAdjWarps][kChunk * 4][kRedStride];
+    __shared__ __align__(16) float4 stage[kAdjWarps][2][kChunk];  // node records of two chunks
     __shared__ float part[kAdjWarps][3][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const u64 eps2x2 = pk(eps2, eps2), three2 = pk(3.f, 3.f);
@@ -184,14 +195,30 @@ __global__ void __launch_bounds__(kAdjWarps * 32)
         u64 ox = 0ull, oy = 0ull, oz = 0ull;  // packed (+0, +0)
         const int len = list_len[g];
         const int *L = lists + (size_t)g * lcap;
-        for (int base = w * kChunk; base < len; base += kAdjWarps * kChunk) {
+        // A three-stage pipeline per warp: the records of the next chunk are in
+        // flight (cp.async into this warp's staging slot) and the list entries of
+        // the chunk after it are loading while this chunk computes.  Lanes past a
+        // chunk's end fetch node 0, so every staged record is a valid float4.
+        constexpr int kStride = kAdjWarps * kChunk;
+        const int base0 = w * kChunk;
+        int cmine = (lane < kChunk && base0 + lane < len) ? L[base0 + lane] : 0;
+        if (lane < kChunk) cp_async16(&stage[w][0][lane], &node4[cmine]);
+        cp_async_commit();
+        int cnext = (lane < kChunk && base0 + kStride + lane < len) ? L[base0 + kStride + lane] : 0;
+        int sb = 0;
+        for (int base = base0; base < len; base += kStride) {
             const int cnt = min(kChunk, len - base);
-            const int cmine = lane < cnt ? L[base + lane] : 0;
+            if (lane < kChunk) cp_async16(&stage[w][sb ^ 1][lane], &node4[cnext]);
+            cp_async_commit();
+            const int c2 = base + 2 * kStride + lane;
+            const int cafter = (lane < kChunk && c2 < len) ? L[c2] : 0;
+            cp_async_wait_one();  // this chunk's records have landed
+            __syncwarp();
 #pragma unroll
             for (int e = 0; e < kChunk; e += 2) {
                 const int ca = __shfl_sync(0xffffffffu, cmine, e);
                 const int cb = __shfl_sync(0xffffffffu, cmine, e + 1);
-                const float4 qa = node4[ca], qb = node4[cb];
+                const float4 qa = stage[w][sb][e], qb = stage[w][sb][e + 1];
                 const u64 dx = sub2(pk(qa.x, qb.x), px);
                 const u64 dy = sub2(pk(qa.y, qb.y), py);
                 const u64 dz = sub2(pk(qa.z, qb.z), pz);
@@ -249,8 +276,13 @@ __global__ void __launch_bounds__(kAdjWarps * 32)
                 upk(s23, a2, a3);
                 if (crow < nc_cap) atomicAdd(&G[(size_t)(lane & 3) * nc_cap + crow], (double)((a0 + a1) + (a2 + a3)));
             }
-            __syncwarp();
+            __syncwarp();  // the staging slot and the reduction rows are free again
+            cmine = cnext;
+            cnext = cafter;
+            sb ^= 1;
         }
+        cp_async_wait_all();  // nothing of this group stays in flight
+        __syncwarp();
         float xa, xb;
         upk(ox, xa, xb);
         part[w][0][lane] = xa + xb;
