@@ -213,12 +213,29 @@ def bench_batched(args, local):
     e1.record()
     torch.cuda.synchronize()
     t_single = e0.elapsed_time(e1) / single_steps
+    # the same, each system replayed from its own captured graph (on a side
+    # stream, so no call synchronises): the strongest single-system usage
+    gs = torch.cuda.Stream()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(gs):
+        for c1, s1 in zip(ctxs, states):
+            c1.graph_step(s1, 1, stream=gs)  # capture, then one step
+        gs.synchronize()
+        g0.record(gs)
+        for _ in range(single_steps):
+            for c1, s1 in zip(ctxs, states):
+                c1.graph_step(s1, 1, stream=gs)
+        g1.record(gs)
+    torch.cuda.synchronize()
+    t_single_graph = g0.elapsed_time(g1) / single_steps
     return {"systems": nsys, "bodies": ntot, "steps": steps,
             "ms_per_step": round(t_batch, 3),
             "systems_steps_per_s": round(nsys * 1000.0 / t_batch, 2),
             "one_at_a_time_ms_per_step": round(t_single, 3),
             "one_at_a_time_systems_steps_per_s": round(nsys * 1000.0 / t_single, 2),
             "speedup_vs_one_at_a_time": round(t_single / t_batch, 3),
+            "one_at_a_time_graphs_ms_per_step": round(t_single_graph, 3),
+            "speedup_vs_one_at_a_time_graphs": round(t_single_graph / t_batch, 3),
             "interactions_per_step": inter,
             "per_system_forces_bitwise_equal_unbatched": checks,
             "walk_config": {"warps": tune["warps"], "variant": tune["variant"]}}
