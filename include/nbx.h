@@ -176,9 +176,13 @@ int nbx_build(nbx_ctx *ctx, const nbx_state *s, void *stream);
 int nbx_forces(nbx_ctx *ctx, const nbx_state *s, void *stream);
 /* kick-drift with the context's dt and dampening */
 int nbx_integrate(nbx_ctx *ctx, const nbx_state *s, void *stream);
-/* nsteps x (build, forces, integrate), launched kernel by kernel */
+/* nsteps x (build, forces, integrate).  One step is launched kernel by kernel;
+   several replay nbx_graph_step's captured step (not while `stream` is being
+   captured: then every step is launched kernel by kernel). */
 int nbx_step(nbx_ctx *ctx, const nbx_state *s, int nsteps, void *stream);
-/* the same steps replayed from a CUDA graph captured once per state */
+/* the same steps replayed from a CUDA graph captured once per state, on the
+   context's own stream, ordered after and before `stream` by events
+   (asynchronous; NBX_ERR_ARG while `stream` is being captured) */
 int nbx_graph_step(nbx_ctx *ctx, const nbx_state *s, int nsteps, void *stream);
 /* synchronises `stream` and returns (and clears) the sticky device status */
 int nbx_sync_status(nbx_ctx *ctx, void *stream);

@@ -88,6 +88,8 @@ void free_all(Ctx *ctx) {
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->graph_stream) cudaStreamDestroy(ctx->graph_stream);
+    if (ctx->graph_ev_in) cudaEventDestroy(ctx->graph_ev_in);
+    if (ctx->graph_ev_out) cudaEventDestroy(ctx->graph_ev_out);
 }
 
 struct Timer {
@@ -511,40 +513,27 @@ static int one_step(Ctx *ctx, const nbx_state *s, cudaStream_t st) {
     return nbx::integrate(ctx, s, ctx->p.dt, ctx->p.dampening, (int)ctx->nbodies, st);
 }
 
-int nbx_step(nbx_ctx *c, const nbx_state *s, int nsteps, void *stream) {
-    if (!c || nsteps < 0) return NBX_ERR_ARG;
-    Ctx *ctx = C(c);
-    int rc = check_state(ctx, s);
-    if (rc) return rc;
-    if (!s->vx || !s->ax) return NBX_ERR_ARG;
-    for (int k = 0; k < nsteps; k++) {
-        rc = one_step(ctx, s, S(stream));
-        if (rc) return rc;
-    }
-    return NBX_OK;
-}
+namespace {
 
-int nbx_graph_step(nbx_ctx *c, const nbx_state *s, int nsteps, void *stream) {
-    if (!c || nsteps < 0) return NBX_ERR_ARG;
-    Range r("nbx_graph_step");
-    Ctx *ctx = C(c);
-    int rc = check_state(ctx, s);
-    if (rc) return rc;
-    if (!s->vx || !s->ax) return NBX_ERR_ARG;
-    cudaStream_t st = S(stream);
-    if (st == nullptr) {
-        if (!ctx->graph_stream) NBX_CUDA(cudaStreamCreateWithFlags(&ctx->graph_stream, cudaStreamNonBlocking));
-        st = ctx->graph_stream;
-        NBX_CUDA(cudaDeviceSynchronize());
-    }
+// One step captured as a CUDA graph (captured again when the state arrays or
+// the systems change; the setters of constants, walk and systems drop it) and
+// replayed nsteps times on the context's own stream, ordered after and before
+// the caller's stream by events, so the call stays asynchronous.
+int replay_steps(Ctx *ctx, const nbx_state *s, int nsteps, cudaStream_t user) {
+    if (!ctx->graph_stream) NBX_CUDA(cudaStreamCreateWithFlags(&ctx->graph_stream, cudaStreamNonBlocking));
+    if (!ctx->graph_ev_in) NBX_CUDA(cudaEventCreateWithFlags(&ctx->graph_ev_in, cudaEventDisableTiming));
+    if (!ctx->graph_ev_out) NBX_CUDA(cudaEventCreateWithFlags(&ctx->graph_ev_out, cudaEventDisableTiming));
+    const cudaStream_t st = ctx->graph_stream;
     if (ctx->graph_exec && (std::memcmp(&ctx->graph_state, s, sizeof(nbx_state)) != 0 || ctx->graph_nsys != ctx->nsys)) {
         cudaGraphExecDestroy(ctx->graph_exec);
         ctx->graph_exec = nullptr;
     }
+    NBX_CUDA(cudaEventRecord(ctx->graph_ev_in, user));
+    NBX_CUDA(cudaStreamWaitEvent(st, ctx->graph_ev_in, 0));
     if (!ctx->graph_exec) {
         cudaGraph_t g = nullptr;
         NBX_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        rc = one_step(ctx, s, st);
+        const int rc = one_step(ctx, s, st);
         cudaError_t e = cudaStreamEndCapture(st, &g);
         if (rc) {
             if (g) cudaGraphDestroy(g);
@@ -565,8 +554,43 @@ int nbx_graph_step(nbx_ctx *c, const nbx_state *s, int nsteps, void *stream) {
         ctx->graph_nsys = ctx->nsys;
     }
     for (int k = 0; k < nsteps; k++) NBX_CUDA(cudaGraphLaunch(ctx->graph_exec, st));
-    if (S(stream) == nullptr) NBX_CUDA(cudaStreamSynchronize(st));
+    NBX_CUDA(cudaEventRecord(ctx->graph_ev_out, st));
+    NBX_CUDA(cudaStreamWaitEvent(user, ctx->graph_ev_out, 0));
     return NBX_OK;
+}
+
+bool capturing(cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+}
+
+}  // namespace
+
+// Several steps replay one captured step; a single step (or a call made while
+// the caller's stream is being captured) launches its kernels directly.
+int nbx_step(nbx_ctx *c, const nbx_state *s, int nsteps, void *stream) {
+    if (!c || nsteps < 0) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    int rc = check_state(ctx, s);
+    if (rc) return rc;
+    if (!s->vx || !s->ax) return NBX_ERR_ARG;
+    if (nsteps >= 2 && !capturing(S(stream))) return replay_steps(ctx, s, nsteps, S(stream));
+    for (int k = 0; k < nsteps; k++) {
+        rc = one_step(ctx, s, S(stream));
+        if (rc) return rc;
+    }
+    return NBX_OK;
+}
+
+int nbx_graph_step(nbx_ctx *c, const nbx_state *s, int nsteps, void *stream) {
+    if (!c || nsteps < 0) return NBX_ERR_ARG;
+    Range r("nbx_graph_step");
+    Ctx *ctx = C(c);
+    int rc = check_state(ctx, s);
+    if (rc) return rc;
+    if (!s->vx || !s->ax) return NBX_ERR_ARG;
+    if (capturing(S(stream))) return NBX_ERR_ARG;  // a captured step cannot be nested in a capture
+    return replay_steps(ctx, s, nsteps, S(stream));
 }
 
 int nbx_sync_status(nbx_ctx *c, void *stream) {

@@ -127,6 +127,7 @@ struct Ctx {
     nbx_state graph_state{};
     int graph_nsys = -1;
     cudaStream_t graph_stream = nullptr;
+    cudaEvent_t graph_ev_in = nullptr, graph_ev_out = nullptr;  // order graph_stream against the caller's
 };
 
 // ---- host helpers ----

@@ -241,21 +241,31 @@ def test_batched_equals_unbatched_hilbert(cuda):
 
 
 def test_graph_step_equals_eager(cuda):
+    """Five steps launched kernel by kernel, five replays of the captured step
+    (graph_step), and one five-step call (which replays the graph) agree bit
+    for bit; so does a second graph_step call that reuses the captured graph."""
+    import torch
     b = ic.star_disk(4096)
     n = len(b.x)
     outs = []
-    for graph in (False, True):
+    for how in ("eager", "graph", "steps"):
         ctx = _ctx(n, theta=0.5, eps=0.01, dt=1e-3)
         ctx.set_systems([0, n])
         s = _state(b)
-        if graph:
-            ctx.graph_step(s, 5)
+        if how == "eager":
+            for _ in range(5):
+                ctx.step(s, 1)
+        elif how == "graph":
+            ctx.graph_step(s, 2)
+            ctx.graph_step(s, 3, stream=torch.cuda.Stream())
         else:
             ctx.step(s, 5)
         ctx.sync()
+        torch.cuda.synchronize()
         outs.append(s.host())
-    for a, c in zip(*outs):
-        assert np.array_equal(a, c)
+    for other in outs[1:]:
+        for a, c in zip(outs[0], other):
+            assert np.array_equal(a, c)
 
 
 def test_trajectory_matches_oracle(cuda):
