@@ -19,7 +19,7 @@
 //
 // Memory: checkpoints of (x, v) every C steps; a segment of C steps is
 // recomputed with each step's tree and interaction lists recorded on a tape,
-// then reversed.  The forward steps with the recording walk's kernel (64-slot
+// then reversed.  The forward steps with the recording walk's kernel (96-slot
 // buffers, plain FP32) without the recording, so the recompute is bit-identical
 // (every kernel is deterministic).  The forward records the last segment as it
 // goes, so the reverse pass starts without recomputing it.
@@ -37,7 +37,7 @@ namespace nbx {
 
 int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox, const float *const *bbox_ptrs);
 int walk2_record(Ctx *ctx, const nbx_state *s, int *rec_list, int *rec_len, int rec_cap, cudaStream_t st);
-int walk2_plain64(Ctx *ctx, const nbx_state *s, cudaStream_t st);
+int walk2_unrecorded(Ctx *ctx, const nbx_state *s, cudaStream_t st);
 
 struct TapeStep {
     float4 *node4 = nullptr;
@@ -731,7 +731,7 @@ int adjoint_forward(Ctx *ctx, Adj *a, const nbx_state *s, const float *tx, const
         } else {
             rc = replay(ctx, st, &a->g_plain, [&] {
                 int r = build_tree(ctx, &w, st, false, nullptr);
-                if (!r) r = walk2_plain64(ctx, &w, st);
+                if (!r) r = walk2_unrecorded(ctx, &w, st);
                 if (!r) r = integrate(ctx, &w, ctx->p.dt, ctx->p.dampening, n, st);
                 return r;
             });

@@ -566,20 +566,20 @@ int walk2_init(Ctx *ctx) {
     rc |= set_attr<96, 1, false>(ctx, smem_optin);
     rc |= set_attr<96, 2, false>(ctx, smem_optin);
     rc |= set_attr<96, 0, true>(ctx, smem_optin);
-    rc |= set_attr<64, 0, false, true>(ctx, smem_optin);
+    rc |= set_attr<96, 0, false, true>(ctx, smem_optin);
     return rc;
 }
 
 // Plain walk that also records every group's interaction list (node ids, in
 // evaluation order) into rec_list[g * rec_cap ...], its length into rec_len[g].
 int walk2_record(Ctx *ctx, const nbx_state *s, int *rec_list, int *rec_len, int rec_cap, cudaStream_t st) {
-    return launch<64, 0, false, true>(ctx, s, nullptr, ctx->walk_warps, st, rec_list, rec_len, rec_cap);
+    return launch<96, 0, false, true>(ctx, s, nullptr, ctx->walk_warps, st, rec_list, rec_len, rec_cap);
 }
 
 // The same walk without recording: the recording adds stores only, so both
 // give the same forces bit for bit (the adjoint's forward and recompute).
-int walk2_plain64(Ctx *ctx, const nbx_state *s, cudaStream_t st) {
-    return launch<64, 0, false, false>(ctx, s, nullptr, ctx->walk_warps, st, nullptr, nullptr, 0);
+int walk2_unrecorded(Ctx *ctx, const nbx_state *s, cudaStream_t st) {
+    return launch<96, 0, false, false>(ctx, s, nullptr, ctx->walk_warps, st, nullptr, nullptr, 0);
 }
 
 // variant 0: 64-slot candidate buffers; 1: 128-slot buffers (<= 8 warps); 3: 96-slot buffers

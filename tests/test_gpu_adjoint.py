@@ -68,8 +68,8 @@ def test_adjoint_matches_fp64_finite_differences(cuda):
 
 
 def test_forward_steps_with_the_recording_walk(cuda):
-    """The adjoint's forward (the 64-slot walk, recording on its last segment)
-    ends bit for bit where T ordinary steps with the 64-slot walk end: recording
+    """The adjoint's forward (the 96-slot walk, recording on its last segment)
+    ends bit for bit where T ordinary steps with the 96-slot walk end: recording
     changes no force, so the reverse pass recomputes exactly the forward."""
     from nns_gb300.barnes_hut import Context, State
     n, T = 2048, 12
@@ -78,7 +78,7 @@ def test_forward_steps_with_the_recording_walk(cuda):
     adj.forward(s, target)
     ref = Context(max_bodies=n, theta=0.5, eps=0.01, dt=1e-3)
     ref.set_systems([0, n])
-    ref.set_walk(8, 0)
+    ref.set_walk(8, 3)
     s2 = State.from_bodies(b)
     ref.step(s2, T)
     ref.sync()
