@@ -372,12 +372,12 @@ def total_energy(ctx, s) -> float:
 
 
 def hbm_roofline(n: int, integ_ms: float, peaks: dict) -> dict:
-    """The kick-drift kernel (k_update, one launch per step, bracketed alone by
-    the integrate phase events): 36 B read + 24 B written per body against the
-    measured copy bandwidth."""
+    """The kick-drift kernel (k_update4, 16-byte accesses, one launch per step
+    for a multiple of 4 bodies, bracketed alone by the integrate phase events):
+    36 B read + 24 B written per body against the measured copy bandwidth."""
     peak = peaks.get("hbm_gbs")
     achieved = 60.0 * n / (integ_ms * 1e-3) / 1e9
-    return {"bound": "hbm", "kernel": "k_update", "achieved": round(achieved, 1),
+    return {"bound": "hbm", "kernel": "k_update4", "achieved": round(achieved, 1),
             "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if peak else None,
             "bytes_per_body": 60, "peak_kind": "measured copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"}
 
