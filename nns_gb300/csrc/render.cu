@@ -10,11 +10,12 @@
 // every dot lands where the reference puts it.  The colour ramp, the offsets
 // a_i, b_j (from the FP64 fraction px - floor(px)) and the weights are FP32:
 // an 8-bit output needs far less, and FP64 runs at a small fraction of the
-// FP32 rate on this part.  The power is exp2(0.75 log2(.)).  Bodies are visited in the tree's sorted order when the
-// context holds a tree for them, so a block's 256 consecutive bodies cover a
-// small pixel window: that window is accumulated with shared-memory integer
-// atomics in fixed point and flushed once as FP32; a block whose window is too
-// large adds to global memory directly.  A final pass converts to bytes as int(255 clamp(v)).
+// FP32 rate on this part.  The power is exp2(0.75 log2(.)).
+// Bodies are visited in the tree's sorted order when the context holds a tree
+// for them, so a block's 256 consecutive bodies cover a small pixel window:
+// that window is accumulated with shared-memory integer atomics in fixed point
+// and flushed once as FP32; a block whose window is too large adds to global
+// memory directly.  A final pass converts to bytes as int(255 clamp(v)).
 #include "nbx_internal.cuh"
 
 namespace nbx {

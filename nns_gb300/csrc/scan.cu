@@ -1,4 +1,5 @@
-// scan.cu -- device-wide exclusive prefix sum (reduce / scan block sums / downsweep).
+// scan.cu -- device-wide exclusive prefix sum (reduce / scan block sums / downsweep;
+// arrays of up to 8 x 4096 elements in one block and one launch).
 //
 // The element count may live on the device (n_dev), so a scan can be launched
 // with a capacity-sized grid inside a captured graph: blocks past the count

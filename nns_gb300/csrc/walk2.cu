@@ -6,8 +6,8 @@
 //   expand   the P top-of-stack cells whose children fit the buffers are popped
 //            at once, one per lane; their child blocks (contiguous in the BFS
 //            node array) are spread over the lanes, one child per lane.  Each
-//            lane classifies its child cell against the group's box and a few
-//            representative bodies (exactly, see below): surely accepted cells
+//            lane classifies its child cell against the group's box and the
+//            representative pair of the child's octant (exactly, see below): surely accepted cells
 //            join the bodies in the body buffer, surely rejected cells are
 //            pushed at once, the rest go to the cell buffer with their
 //            threshold dp = depth0 * 0.25^(L-1) and id;
