@@ -358,7 +358,8 @@ def _section(fn, *a):
     try:
         return fn(*a)
     except Exception as e:  # noqa: BLE001 -- reported in the line
-        torch.cuda.synchronize()
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
         return {"unavailable": "%s: %s" % (type(e).__name__, str(e)[:200])}
 
 
