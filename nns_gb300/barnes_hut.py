@@ -115,10 +115,14 @@ class Context:
               self.h)
 
     def step(self, s: "State", nsteps: int = 1, stream=None):
+        """nsteps x (build, forces, integrate), asynchronous on ``stream``.  One step
+        launches its kernels; several replay the captured step of graph_step."""
         check(lib().nbx_step(self.h, C.byref(s.c), nsteps, _stream_ptr(stream)), "nbx_step",
               self.h)
 
     def graph_step(self, s: "State", nsteps: int = 1, stream=None):
+        """The same steps replayed from a CUDA graph captured once per state, on the
+        context's own stream, ordered after and before ``stream`` by events."""
         check(lib().nbx_graph_step(self.h, C.byref(s.c), nsteps, _stream_ptr(stream)),
               "nbx_graph_step", self.h)
 
