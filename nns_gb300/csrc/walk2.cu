@@ -255,13 +255,14 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             // else one cell per round (depth-first), which cannot outgrow it
             // P = the most top-of-stack cells whose children fit the buffers
             const int avail = min(top, 32);
-            int first = 0, nch = 0, lvl = 0;
+            int first = 0, nch = 0;
+            float dpp = 0.f;  // the children's opening threshold, depth0 * 4^-level(popped cell)
             if (lane < avail) {
                 const int b = stack[top - 1 - lane];  // stack entries are node indices
-                lvl = lvl8[b];
                 const int mb = meta[b];
                 first = mb & 0x0fffffff;
                 nch = ((mb >> 28) & 7) + 1;
+                dpp = scale4(d0, lvl8[b]);
             }
             int incl = nch;
 #pragma unroll
@@ -270,6 +271,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 if (lane >= o) incl += u;
             }
             const int excl = incl - nch;
+            const int cbase = first - excl;  // child t of this lane's cell is node cbase + t
             int P = __popc(__ballot_sync(0xffffffffu, lane < avail && incl <= kCB - nb));
             int T = __shfl_sync(0xffffffffu, incl, (P + 31) & 31);
             // the stack grows by at most T - P: wide rounds only while that keeps
@@ -312,15 +314,13 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 const unsigned le = lane == 31 ? 0xffffffffu : (2u << lane) - 1u;
                 const int j = jbase + __popc(seg[k] & le);
                 jbase += __popc(seg[k]);
-                const int fj = __shfl_sync(0xffffffffu, first, j);
-                const int lj = __shfl_sync(0xffffffffu, lvl, j);
-                const int ej = __shfl_sync(0xffffffffu, excl, j);
+                const int bj = __shfl_sync(0xffffffffu, cbase, j);
+                const float dpc = __shfl_sync(0xffffffffu, dpp, j);
                 const bool ok = t < T;
-                const int c = fj + (t - ej);
+                const int c = bj + t;
                 const int cm = ok ? meta[c] : 0;
                 const float4 q = ok ? node4[c] : make_float4(0.f, 0.f, 0.f, 0.f);
                 const bool isc = ok && cm >= 0;
-                const float dpc = scale4(d0, lj);
                 bool sacc = false, srej = false;
                 {  // on every lane, without a branch; the results are masked by isc below
                     const float4 lo = buf.cls[0], hi = buf.cls[1];
