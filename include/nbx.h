@@ -64,7 +64,7 @@ typedef struct nbx_params {
     int compensated;   /* 0 plain FP32; 1 split compensation (FP32 partial sums per
                           walk round, Kahan across rounds); 2 Kahan on every term */
     int leaf_size;     /* bodies per leaf: 1 */
-    int radix_bits;    /* radix digit width of the key sort: 8 */
+    int radix_bits;    /* radix digit width of the key sort: 8 (8 passes) or 9 (7 passes) */
     int walk_warps;    /* warps per block of the walk kernel (0 = autotuned default) */
     int device;        /* CUDA device ordinal */
     int block_size;    /* reference launch-shape hints (main.cu:30-31); informational */
@@ -118,6 +118,11 @@ int nbx_set_constants(nbx_ctx *ctx, float theta_ref, float eps2, int compensated
 /* Launch shape of the walk: warps per block (4, 8 or 16) and variant; used by
  * the autotuner (nns_gb300/autotune.py). */
 int nbx_set_walk_config(nbx_ctx *ctx, int warps_per_block, int variant);
+/* Sort digit width (8: 8 passes, 9: 7 passes over the 63-bit keys; both give the
+ * same stable order) and walk stack entries per warp (360..4096; a launch whose
+ * stacks and buffers exceed the device's shared memory per block fails with
+ * NBX_ERR_ARG).  A built tree stays valid.  Used by the autotuner. */
+int nbx_set_tuning(nbx_ctx *ctx, int radix_bits, int stack_depth);
 
 /* ---- reference-compatible phase entry points (KernelsWrapper.cu) ---- */
 /* KernelsWrapper::resetArrays (KernelsWrapper.cu:28; Kernels.cu:21-64) */

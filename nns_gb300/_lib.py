@@ -71,6 +71,7 @@ SIGNATURES = {
     "nbx_compute_forces": (_I, [_P] + [_P] * 14 + [_I, _F, _P, _PF]),
     "nbx_update": (_I, [_P] + [_P] * 9 + [_I, _F, _F, _P, _PF]),
     "nbx_set_walk_config": (_I, [_P, _I, _I]),
+    "nbx_set_tuning": (_I, [_P, _I, _I]),
     "nbx_set_systems": (_I, [_P, _I, C.POINTER(C.c_int64)]),
     "nbx_build": (_I, [_P, C.POINTER(nbx_state), _P]),
     "nbx_forces": (_I, [_P, C.POINTER(nbx_state), _P]),

@@ -1,13 +1,18 @@
-"""Autotuner for the launch parameters of the force walk.
+"""Autotuner for the launch parameters of the force walk and the key sort.
 
 The interaction lists are fixed by the reference's semantics (group of 32,
-leaf bucket of one body, 8-bit radix digits are what the parity tests pin), so
-the tunable knobs are the ones that change only speed:
+leaf bucket of one body), so the tunable knobs are the ones that change only
+speed:
   * warps per block of the walk (4, 8, 16) -- occupancy vs. shared memory,
-  * candidate buffer size of the walk (64, 96 or 128 slots per warp).
+  * candidate buffer size of the walk (64, 96 or 128 slots per warp),
+  * walk stack entries per warp (a deeper stack keeps more rounds wide, a
+    shallower one leaves shared memory for more blocks),
+  * sort digit width (8 bits in 8 passes or 9 bits in 7 passes; a stable LSD
+    sort gives the same order for any width).
 Candidates are timed with CUDA events on the caller's workload after one
-build; the winner is applied to the context and cached per (device, n, systems)
-in ``~/.cache/nbx_autotune.json`` (override with NBX_AUTOTUNE_CACHE).
+build, in that order, each stage with the winners of the stages before it;
+the winner is applied to the context and cached per (device, n, systems) in
+``~/.cache/nbx_autotune.json`` (override with NBX_AUTOTUNE_CACHE).
 """
 from __future__ import annotations
 
@@ -16,7 +21,11 @@ import os
 
 import torch
 
+from ._lib import NbxError
+
 CANDIDATES = ((8, 3), (16, 3), (4, 3), (8, 0), (16, 0), (8, 1), (4, 1))
+STACK_DEPTHS = (512, 384, 768)
+RADIX_BITS = (8, 9)
 
 
 def _cache_path():
@@ -30,8 +39,22 @@ def _key(ctx, n):
     return "%s|n=%d|sys=%d|comp=%d" % (name, n, nsys, int(ctx.params.compensated))
 
 
-def tune_walk(ctx, state, reps: int = 2, candidates=CANDIDATES, use_cache: bool = True) -> dict:
-    """Times each candidate walk configuration and applies the fastest."""
+def _time(fn, reps):
+    """Mean CUDA-event milliseconds of fn() after one untimed call."""
+    fn()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(reps):
+        fn()
+    ev1.record()
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / reps
+
+
+def tune_walk(ctx, state, reps: int = 2, candidates=CANDIDATES, use_cache: bool = True,
+              stack_depths=STACK_DEPTHS, radix_bits=RADIX_BITS) -> dict:
+    """Times the candidate configurations and applies the fastest."""
     n = int(ctx.offsets[-1])
     key = _key(ctx, n)
     path = _cache_path()
@@ -41,29 +64,46 @@ def tune_walk(ctx, state, reps: int = 2, candidates=CANDIDATES, use_cache: bool 
             cache = json.load(open(path))
         except (OSError, ValueError):
             cache = {}
-    if use_cache and key in cache:
+    if use_cache and key in cache and "stack_depth" in cache[key]:
         best = cache[key]
         ctx.set_walk(best["warps"], best["variant"])
+        ctx.set_tuning(best["radix_bits"], best["stack_depth"])
         return dict(best, cached=True)
+    bits0 = int(ctx.params.radix_bits)
+    depth0 = int(ctx.params.stack_depth)
     ctx.build(state)
     ctx.sync()
+    # 1. walk launch shape
     times = {}
     for warps, variant in candidates:
         ctx.set_walk(warps, variant)
-        ctx.forces(state)  # warm-up
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        ev0.record()
-        for _ in range(reps):
-            ctx.forces(state)
-        ev1.record()
-        torch.cuda.synchronize()
-        times["%d/%d" % (warps, variant)] = ev0.elapsed_time(ev1) / reps
+        times["%d/%d" % (warps, variant)] = _time(lambda: ctx.forces(state), reps)
     ctx.sync()
     wbest = min(times, key=times.get)
     warps, variant = (int(v) for v in wbest.split("/"))
     ctx.set_walk(warps, variant)
-    best = {"warps": warps, "variant": variant, "ms": times}
+    # 2. stack depth with that shape (a depth whose stacks do not fit the
+    #    shape's shared memory is skipped)
+    stimes = {}
+    for depth in stack_depths:
+        ctx.set_tuning(bits0, depth)
+        try:
+            stimes[str(depth)] = _time(lambda: ctx.forces(state), reps)
+        except NbxError:
+            continue
+    ctx.sync()
+    depth = int(min(stimes, key=stimes.get)) if stimes else depth0
+    # 3. sort digit width, timed over whole builds
+    btimes = {}
+    for bits in radix_bits:
+        ctx.set_tuning(bits, depth)
+        btimes[str(bits)] = _time(lambda: ctx.build(state), reps)
+    ctx.sync()
+    bits = int(min(btimes, key=btimes.get))
+    ctx.set_tuning(bits, depth)
+    ctx.build(state)
+    best = {"warps": warps, "variant": variant, "stack_depth": depth, "radix_bits": bits,
+            "ms": times, "ms_stack": stimes, "ms_build": btimes}
     if use_cache:
         cache[key] = best
         try:

@@ -39,13 +39,14 @@ class Context:
 
     ``key_order`` 1 orders bodies along the Hilbert curve (faster walk; lists
     differ from the reference's); ``moments_mode`` picks the centre-of-mass pass
-    (0 by size, 1 per tree level, 2 one launch), all with the same sums."""
+    (0 by size, 1 per tree level, 2 one launch), all with the same sums;
+    ``radix_bits`` 8 or 9 sorts the keys in 8 or 7 passes, to the same order."""
 
     def __init__(self, max_bodies: int, max_systems: int = 1, theta: float = 0.5,
                  theta_ref: float | None = None, eps: float = 0.05, eps2: float | None = None,
                  dt: float = 1e-3, dampening: float = 1.0, compensated: int = 0,
                  stack_depth: int = 512, device: int = 0, key_order: int = 0, node_capacity: int = 0,
-                 moments_mode: int = 0):
+                 moments_mode: int = 0, radix_bits: int = 8):
         p = L.nbx_params()
         lib().nbx_params_default(C.byref(p))
         p.max_bodies = int(max_bodies)
@@ -58,6 +59,7 @@ class Context:
         p.dampening = dampening
         p.compensated = int(compensated)
         p.stack_depth = stack_depth
+        p.radix_bits = int(radix_bits)
         p.node_capacity = node_capacity
         p.moments_mode = moments_mode
         p.device = device
@@ -95,6 +97,13 @@ class Context:
         """Walk launch shape (4/8/16 warps per block) and variant (0 production, 2 simple)."""
         check(lib().nbx_set_walk_config(self.h, warps_per_block, variant), "nbx_set_walk_config",
               self.h)
+
+    def set_tuning(self, radix_bits: int = 8, stack_depth: int = 512):
+        """Sort digit width (8 or 9 bits: 8 or 7 passes, same order) and walk stack
+        entries per warp (360..4096).  A built tree stays valid."""
+        check(lib().nbx_set_tuning(self.h, int(radix_bits), int(stack_depth)), "nbx_set_tuning", self.h)
+        self.params.radix_bits = int(radix_bits)
+        self.params.stack_depth = int(stack_depth)
 
     def set_systems(self, offsets):
         off = np.ascontiguousarray(offsets, dtype=np.int64)

@@ -183,7 +183,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     if (!p || !out) return NBX_ERR_ARG;
     *out = nullptr;
     if (p->max_bodies < 1 || p->max_bodies > (1 << 26) || p->max_systems < 1 ||
-        p->max_systems > p->max_bodies || p->group != 32 || p->leaf_size != 1 || p->radix_bits != 8 ||
+        p->max_systems > p->max_bodies || p->group != 32 || p->leaf_size != 1 || (p->radix_bits != 8 && p->radix_bits != 9) ||
         p->stack_depth < 360 || p->stack_depth > 4096 || p->walk_variant < 0 || p->walk_variant > 3 ||
         p->moments_mode < 0 || p->moments_mode > 2 ||
         (p->node_capacity != 0 && (p->node_capacity < p->max_bodies + 1 || p->node_capacity > nbx::kMaxNodes)))
@@ -196,6 +196,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     ctx->compensated = p->compensated;
     ctx->walk_variant = p->walk_variant;
     ctx->key_order = p->key_order;
+    ctx->radix_bits = p->radix_bits;
     if (p->key_order < 0 || p->key_order > 1) {
         delete ctx;
         return NBX_ERR_ARG;
@@ -220,7 +221,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     ctx->cap_tiles_body = (B / nbx::kTile > 2 * want_tiles ? B / nbx::kTile : 2 * want_tiles) + Ss + 1;
     ctx->tile_node = nbx::tile_for(ctx->cap_nodes, ctx->nsm);
     ctx->cap_tiles_node = nbx::ceil_div(ctx->cap_nodes, ctx->tile_node);
-    const int64_t hist = 256ll * (ctx->cap_tiles_body > ctx->cap_tiles_node ? ctx->cap_tiles_body : ctx->cap_tiles_node);
+    const int64_t hist = (1ll << nbx::kMaxRadixBits) * (ctx->cap_tiles_body > ctx->cap_tiles_node ? ctx->cap_tiles_body : ctx->cap_tiles_node);
     int64_t scan_max = hist;
     if (ctx->cap_nodes > scan_max) scan_max = ctx->cap_nodes;
     if (B > scan_max) scan_max = B;
@@ -319,6 +320,20 @@ int nbx_set_walk_config(nbx_ctx *c, int warps_per_block, int variant) {
     Ctx *ctx = C(c);
     ctx->walk_warps = warps_per_block;
     ctx->walk_variant = variant;
+    ++ctx->graph_gen;
+    if (ctx->graph_exec) {
+        cudaGraphExecDestroy(ctx->graph_exec);
+        ctx->graph_exec = nullptr;
+    }
+    return NBX_OK;
+}
+
+int nbx_set_tuning(nbx_ctx *c, int radix_bits, int stack_depth) {
+    if (!c || (radix_bits != 8 && radix_bits != 9) || stack_depth < 360 || stack_depth > 4096) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    ctx->radix_bits = radix_bits;
+    ctx->p.radix_bits = radix_bits;
+    ctx->p.stack_depth = stack_depth;  // the built tree stays valid: neither changes it
     ++ctx->graph_gen;
     if (ctx->graph_exec) {
         cudaGraphExecDestroy(ctx->graph_exec);

@@ -28,7 +28,9 @@ inline int tile_for(long long n, int nsm) {
     while (t > kTileMin && n < (long long)t * want) t >>= 1;
     return t;
 }
-constexpr int kRadixBins = 256;   // 8-bit digits
+constexpr int kMaxRadixBits = 9;  // body-key digits: 8 or 9 bits (histograms sized for 9)
+// LSD passes over the 63-bit body keys for a digit width
+constexpr int radix_passes(int bits) { return (63 + bits - 1) / bits; }
 constexpr int kMaxLevel = 43;     // 42 key levels + the body level
 constexpr int kBodyFlag = int(0x80000000u);
 constexpr int kLevelShift = 26;   // build node entry = level << 26 | sorted position
@@ -56,12 +58,14 @@ struct Ctx {
     int walk_variant = 0;  // 0 production walk (walk2.cu), 2 one-cell-at-a-time walk (walk.cu)
     int walk_warps = 8;    // warps per block of the production walk
     int key_order = 0;     // 0 the reference's (Lebesgue) order, 1 Hilbert
+    int radix_bits = 8;    // digit width of the body-key sort (8: 8 passes, 9: 7 passes)
     std::string last_error;
 
     // capacity
     int cap_bodies, cap_sys, cap_nodes, cap_tiles_body, cap_tiles_node;
     int tile_body = kTile, tile_node = kTile;  // radix tile sizes (tile_for)
     int nsm = 152;         // multiprocessors of the device
+    int smem_optin = 0;    // shared memory per block (opt-in maximum)
     long long launches = 0;  // kernels launched by this context
 
     // systems
@@ -108,7 +112,7 @@ struct Ctx {
     int *d_cl = nullptr;                              // [NC+S] cell list (BFS index)
 
     // radix + scan scratch
-    unsigned *d_hist = nullptr;        // [256 * max(tiles)]
+    unsigned *d_hist = nullptr;        // [2^kMaxRadixBits * max(tiles)]
     unsigned long long *d_scan_blk = nullptr;  // block sums
     unsigned *d_totals = nullptr;      // [8] device-side totals: 0 entries, 1 cells+first..., etc
     unsigned long long *d_totals64 = nullptr;

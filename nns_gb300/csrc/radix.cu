@@ -1,4 +1,8 @@
-// radix.cu -- stable LSD radix sort passes (8-bit digits), warp-per-tile.
+// radix.cu -- stable LSD radix sort passes, warp-per-tile.
+//
+// The body keys (63 bits) are sorted in 8 passes of 8-bit digits or 7 passes of
+// 9-bit digits (nbx_params.radix_bits).  Any digit width gives the same stable
+// order, so the width only trades passes against histogram size.
 //
 // A tile is up to 2048 consecutive keys owned by one warp (smaller for small
 // systems, so that the tiles still fill the GPU).  Per pass:
@@ -29,7 +33,7 @@ struct TileMap {
     int tile;               // keys per tile (<= kTile)
 };
 
-template <bool Seg>
+template <bool Seg, int Bins>
 __device__ __forceinline__ void tile_info(const TileMap &tm, int t, int &start, int &len,
                                           int64_t &hbase, int &hstride) {
     if (Seg) {
@@ -37,7 +41,7 @@ __device__ __forceinline__ void tile_info(const TileMap &tm, int t, int &start, 
         int2 s = tm.seg_tiles[d.z];
         start = d.x;
         len = d.y;
-        hbase = (int64_t)s.x * kRadixBins + d.w;
+        hbase = (int64_t)s.x * Bins + d.w;
         hstride = s.y;
     } else {
         int64_t st = (int64_t)t * tm.tile;
@@ -49,32 +53,34 @@ __device__ __forceinline__ void tile_info(const TileMap &tm, int t, int &start, 
     }
 }
 
-template <typename K, bool Seg>
+template <typename K, bool Seg, int Bits>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     k_radix_hist(const K *__restrict__ key, TileMap tm, int shift, unsigned *__restrict__ hist) {
-    __shared__ unsigned cnt[kWarpsPerBlock][kRadixBins];
+    constexpr int kBins = 1 << Bits;
+    constexpr unsigned kMask = kBins - 1;
+    __shared__ unsigned cnt[kWarpsPerBlock][kBins];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int t = blockIdx.x * kWarpsPerBlock + w;
     if (t >= tm.ntiles) return;
-    for (int d = lane; d < kRadixBins; d += 32) cnt[w][d] = 0;
+    for (int d = lane; d < kBins; d += 32) cnt[w][d] = 0;
     __syncwarp();
     int start, len, hstride;
     int64_t hbase;
-    tile_info<Seg>(tm, t, start, len, hbase, hstride);
+    tile_info<Seg, kBins>(tm, t, start, len, hbase, hstride);
     constexpr int kBatch = 8;  // loads in flight together (the atomics would serialise them)
     for (int i0 = 0; i0 < len; i0 += 32 * kBatch) {
         unsigned d[kBatch];
 #pragma unroll
         for (int u = 0; u < kBatch; u++) {
             const int i = i0 + 32 * u + lane;
-            d[u] = i < len ? (unsigned)(key[start + i] >> shift) & 0xffu : 0x100u;
+            d[u] = i < len ? (unsigned)(key[start + i] >> shift) & kMask : (unsigned)kBins;
         }
 #pragma unroll
         for (int u = 0; u < kBatch; u++)
-            if (d[u] < 0x100u) atomicAdd(&cnt[w][d[u]], 1u);
+            if (d[u] < (unsigned)kBins) atomicAdd(&cnt[w][d[u]], 1u);
     }
     __syncwarp();
-    for (int d = lane; d < kRadixBins; d += 32) hist[hbase + (int64_t)d * hstride] = cnt[w][d];
+    for (int d = lane; d < kBins; d += 32) hist[hbase + (int64_t)d * hstride] = cnt[w][d];
 }
 
 // Scatter with the tile staged in shared memory in output order: every lane
@@ -87,44 +93,47 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 // A warp's stage: gbase (output offset of (digit, tile)), lstart (tile-local
 // start of the digit), cnt (running tile-local position), then the tile's keys
 // and values; sized for the launch's tile.
-template <typename K, typename V>
+template <typename K, typename V, int Bits>
 __host__ __device__ constexpr size_t stage_bytes(int tile) {
-    return (3 * kRadixBins * sizeof(unsigned) + (size_t)tile * (sizeof(K) + sizeof(V)) + 15) & ~(size_t)15;
+    return (3 * (size_t(1) << Bits) * sizeof(unsigned) + (size_t)tile * (sizeof(K) + sizeof(V)) + 15) & ~(size_t)15;
 }
 
-template <typename K, typename V>
+template <typename K, typename V, int Bits>
 struct Stage {
     unsigned *gbase, *lstart, *cnt;
     K *key;
     V *val;
     __device__ Stage(unsigned char *base, int tile) {
         gbase = reinterpret_cast<unsigned *>(base);
-        lstart = gbase + kRadixBins;
-        cnt = lstart + kRadixBins;
-        key = reinterpret_cast<K *>(cnt + kRadixBins);
+        lstart = gbase + (1 << Bits);
+        cnt = lstart + (1 << Bits);
+        key = reinterpret_cast<K *>(cnt + (1 << Bits));
         val = reinterpret_cast<V *>(key + tile);
     }
 };
 
-template <typename K, typename V, bool Seg>
+template <typename K, typename V, bool Seg, int Bits>
 __global__ void __launch_bounds__(kScatterWarps * 32)
     k_radix_scatter(const K *__restrict__ key_in, K *__restrict__ key_out,
                     const V *__restrict__ val_in, V *__restrict__ val_out, TileMap tm, int shift,
                     const unsigned *__restrict__ offs) {
+    constexpr int kBins = 1 << Bits;
+    constexpr unsigned kMask = kBins - 1;
+    constexpr int kPer = kBins / 32;  // digits owned by one lane
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int t = blockIdx.x * kScatterWarps + w;
     if (t >= tm.ntiles) return;
     int start, len, hstride;
     int64_t hbase;
-    tile_info<Seg>(tm, t, start, len, hbase, hstride);
+    tile_info<Seg, kBins>(tm, t, start, len, hbase, hstride);
     if (len <= 0) return;
-    Stage<K, V> sg(smem_raw + (size_t)w * stage_bytes<K, V>(tm.tile), tm.tile);
-    // lane owns digits 8*lane .. 8*lane+7: counts, then the tile-local starts
-    unsigned c[8], sum = 0;
+    Stage<K, V, Bits> sg(smem_raw + (size_t)w * stage_bytes<K, V, Bits>(tm.tile), tm.tile);
+    // lane owns digits kPer*lane .. kPer*lane+kPer-1: counts, then the tile-local starts
+    unsigned c[kPer], sum = 0;
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-        const int d = 8 * lane + k;
+    for (int k = 0; k < kPer; k++) {
+        const int d = kPer * lane + k;
         const int64_t idx = hbase + (int64_t)d * hstride;
         const unsigned g = offs[idx];
         c[k] = offs[idx + 1] - g;
@@ -139,9 +148,9 @@ __global__ void __launch_bounds__(kScatterWarps * 32)
     }
     unsigned run = incl - sum;
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-        sg.lstart[8 * lane + k] = run;
-        sg.cnt[8 * lane + k] = run;
+    for (int k = 0; k < kPer; k++) {
+        sg.lstart[kPer * lane + k] = run;
+        sg.cnt[kPer * lane + k] = run;
         run += c[k];
     }
     __syncwarp();
@@ -162,7 +171,7 @@ __global__ void __launch_bounds__(kScatterWarps * 32)
             if (j >= len) break;
             const bool valid = j + lane < len;
             const K k = kk[u];
-            const unsigned d = valid ? ((unsigned)(k >> shift) & 0xffu) : (0x100u + lane);
+            const unsigned d = valid ? ((unsigned)(k >> shift) & kMask) : ((unsigned)kBins + lane);
             const unsigned peers = __match_any_sync(0xffffffffu, d);
             const unsigned rank = __popc(peers & lt);
             const unsigned base = valid ? sg.cnt[d] : 0u;
@@ -178,48 +187,61 @@ __global__ void __launch_bounds__(kScatterWarps * 32)
     __syncwarp();
     for (int j = lane; j < len; j += 32) {
         const K k = sg.key[j];
-        const unsigned d = (unsigned)(k >> shift) & 0xffu;
+        const unsigned d = (unsigned)(k >> shift) & kMask;
         const unsigned dst = sg.gbase[d] + ((unsigned)j - sg.lstart[d]);
         key_out[dst] = k;
         if (val_in) val_out[dst] = sg.val[j];
     }
 }
 
-template <typename K, typename V, bool Seg>
+template <typename K, typename V, bool Seg, int Bits>
 int launch_scatter(Ctx *ctx, int nt, const K *kin, K *kout, const V *vin, V *vout, const TileMap &tm, int shift,
                    cudaStream_t st) {
-    const size_t smem = stage_bytes<K, V>(tm.tile) * kScatterWarps;
-    k_radix_scatter<K, V, Seg><<<ceil_div(nt, kScatterWarps), kScatterWarps * 32, smem, st>>>(
+    const size_t smem = stage_bytes<K, V, Bits>(tm.tile) * kScatterWarps;
+    k_radix_scatter<K, V, Seg, Bits><<<ceil_div(nt, kScatterWarps), kScatterWarps * 32, smem, st>>>(
         kin, kout, vin, vout, tm, shift, ctx->d_hist);
     ++ctx->launches;
     return NBX_OK;
 }
 
-}  // namespace
-
-// Sorts (d_key, d_val) of every system by the 63-bit key, stably, in place
-// (8 passes, result back in d_key / d_val).
-int radix_sort_bodies(Ctx *ctx, cudaStream_t st) {
+template <int Bits>
+int sort_bodies(Ctx *ctx, cudaStream_t st) {
     TileMap tm{ctx->d_tiles, ctx->d_sys_tiles, nullptr, ctx->ntiles_body, ctx->tile_body};
     const int nt = ctx->ntiles_body;
     if (nt == 0) return NBX_OK;
     const int grid = ceil_div(nt, kWarpsPerBlock);
-    const int nh = nt * kRadixBins;
+    const int nh = nt * (1 << Bits);
+    const int passes = radix_passes(Bits);
+    // an odd pass count starts from the alternate buffers (where k_keys wrote)
     unsigned long long *k0 = ctx->d_key, *k1 = ctx->d_key_alt;
     int *v0 = ctx->d_val, *v1 = ctx->d_val_alt;
-    for (int pass = 0; pass < 8; pass++) {
-        const int shift = 8 * pass;
-        k_radix_hist<unsigned long long, true>
+    if (passes & 1) {
+        std::swap(k0, k1);
+        std::swap(v0, v1);
+    }
+    for (int pass = 0; pass < passes; pass++) {
+        const int shift = Bits * pass;
+        k_radix_hist<unsigned long long, true, Bits>
             <<<grid, kWarpsPerBlock * 32, 0, st>>>(k0, tm, shift, ctx->d_hist);
         ++ctx->launches;
         int rc = scan_exclusive_u32(ctx, ctx->d_hist, ctx->d_hist, nh, nullptr, ctx->d_hist + nh, st);
         if (rc) return rc;
-        launch_scatter<unsigned long long, int, true>(ctx, nt, k0, k1, v0, v1, tm, shift, st);
+        launch_scatter<unsigned long long, int, true, Bits>(ctx, nt, k0, k1, v0, v1, tm, shift, st);
         std::swap(k0, k1);
         std::swap(v0, v1);
     }
     NBX_CUDA(cudaGetLastError());
     return NBX_OK;
+}
+
+}  // namespace
+
+// Sorts the 63-bit keys of every system stably, with the sort permutation,
+// into d_key / d_val.  The keys and identity values are expected in d_key /
+// d_val for an even pass count and in d_key_alt / d_val_alt for an odd one
+// (keys_in_alt), so that the last pass always writes d_key / d_val.
+int radix_sort_bodies(Ctx *ctx, cudaStream_t st) {
+    return ctx->radix_bits == 9 ? sort_bodies<9>(ctx, st) : sort_bodies<8>(ctx, st);
 }
 
 // Stable sort of the node entries (level << 26 | position) by level: one pass
@@ -229,23 +251,26 @@ int radix_sort_entries(Ctx *ctx, cudaStream_t st) {
     const int nt = ctx->cap_tiles_node;
     TileMap tm{nullptr, nullptr, &ctx->d_totals[1], nt, ctx->tile_node};  // clamped node count (0 on overflow)
     const int grid = ceil_div(nt, kWarpsPerBlock);
-    const int nh = nt * kRadixBins;
-    k_radix_hist<unsigned, false><<<grid, kWarpsPerBlock * 32, 0, st>>>(ctx->d_ent, tm, 24, ctx->d_hist);
+    const int nh = nt * 256;
+    k_radix_hist<unsigned, false, 8><<<grid, kWarpsPerBlock * 32, 0, st>>>(ctx->d_ent, tm, 24, ctx->d_hist);
     ++ctx->launches;
     int rc = scan_exclusive_u32(ctx, ctx->d_hist, ctx->d_hist, nh, nullptr, ctx->d_hist + nh, st);
     if (rc) return rc;
-    launch_scatter<unsigned, int, false>(ctx, nt, ctx->d_ent, ctx->d_ent_alt, (const int *)nullptr, (int *)nullptr,
+    launch_scatter<unsigned, int, false, 8>(ctx, nt, ctx->d_ent, ctx->d_ent_alt, (const int *)nullptr, (int *)nullptr,
                                          tm, 24, st);
     NBX_CUDA(cudaGetLastError());
     return NBX_OK;
 }
 
 int radix_init(Ctx *ctx) {
-    NBX_CUDA(cudaFuncSetAttribute(k_radix_scatter<unsigned long long, int, true>,
+    NBX_CUDA(cudaFuncSetAttribute(k_radix_scatter<unsigned long long, int, true, 8>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(stage_bytes<unsigned long long, int>(kTile) * kScatterWarps)));
-    NBX_CUDA(cudaFuncSetAttribute(k_radix_scatter<unsigned, int, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(stage_bytes<unsigned, int>(kTile) * kScatterWarps)));
+                                  (int)(stage_bytes<unsigned long long, int, 8>(kTile) * kScatterWarps)));
+    NBX_CUDA(cudaFuncSetAttribute(k_radix_scatter<unsigned long long, int, true, 9>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(stage_bytes<unsigned long long, int, 9>(kTile) * kScatterWarps)));
+    NBX_CUDA(cudaFuncSetAttribute(k_radix_scatter<unsigned, int, false, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(stage_bytes<unsigned, int, 8>(kTile) * kScatterWarps)));
     return NBX_OK;
 }
 

@@ -588,8 +588,11 @@ int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox
     }
     // the node array is free until the nodes are written: it holds the packed bodies
     float4 *pos4 = ctx->d_node4;
-    k_keys<<<gb, kBlock, 0, st>>>(s->x, s->y, s->z, s->m, ctx->d_body_sys, ctx->d_bbox, n, ctx->d_key,
-                                  ctx->d_val, pos4, ctx->d_status, ctx->key_order);
+    // the sort's last pass writes d_key / d_val: an odd pass count starts from the alternates
+    const bool alt = radix_passes(ctx->radix_bits) & 1;
+    k_keys<<<gb, kBlock, 0, st>>>(s->x, s->y, s->z, s->m, ctx->d_body_sys, ctx->d_bbox, n,
+                                  alt ? ctx->d_key_alt : ctx->d_key, alt ? ctx->d_val_alt : ctx->d_val, pos4,
+                                  ctx->d_status, ctx->key_order);
     ++ctx->launches;
     int rc = radix_sort_bodies(ctx, st);
     if (rc) return rc;

@@ -215,11 +215,13 @@ int walk2_init(Ctx *ctx);
 int walk2_forces(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st);
 
 int walk_init(Ctx *ctx) {
-    const int smem = kWalkWarps * ctx->p.stack_depth * (int)sizeof(int);
+    // the attribute is per kernel, not per context: allow the device maximum
+    // (8 warps x 4096 entries x 4 bytes = 128 KB at most)
     NBX_CUDA(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->p.device));
-    NBX_CUDA(cudaFuncSetAttribute(k_walk<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    NBX_CUDA(cudaFuncSetAttribute(k_walk<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    NBX_CUDA(cudaFuncSetAttribute(k_walk<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    NBX_CUDA(cudaDeviceGetAttribute(&ctx->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->p.device));
+    NBX_CUDA(cudaFuncSetAttribute(k_walk<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin));
+    NBX_CUDA(cudaFuncSetAttribute(k_walk<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin));
+    NBX_CUDA(cudaFuncSetAttribute(k_walk<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_optin));
     return walk2_init(ctx);
 }
 

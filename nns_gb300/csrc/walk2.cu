@@ -516,6 +516,10 @@ int launch(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st,
            int *rec_len = nullptr, int rec_cap = 0) {
     const int cap = ctx->p.stack_depth;
     const size_t smem = (size_t)warps * (sizeof(WarpBuf<CB>) + (size_t)cap * sizeof(int));
+    if (smem > (size_t)ctx->smem_optin) {
+        ctx->last_error = "walk: stack_depth too large for the launch shape's shared memory";
+        return NBX_ERR_ARG;
+    }
     const int blocks_needed = ceil_div(ctx->ngroups, warps);
     int per_sm = 1;
     NBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk2<CB, Mode, Pot, Rec>, warps * 32, smem));
@@ -551,8 +555,7 @@ int forces_cb(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t 
 }  // namespace
 
 int walk2_init(Ctx *ctx) {
-    int smem_optin = 0;
-    NBX_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->p.device));
+    const int smem_optin = ctx->smem_optin;
     int rc = 0;
     rc |= set_attr<64, 0, false>(ctx, smem_optin);
     rc |= set_attr<64, 1, false>(ctx, smem_optin);

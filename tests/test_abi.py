@@ -55,7 +55,9 @@ def test_params_layout_and_option_ranges_without_gpu():
     p = _lib.nbx_params()
     L.nbx_params_default(ctypes.byref(p))
     assert p.moments_mode == 0 and p.key_order == 0 and p.node_capacity == 0
-    for field, bad in (("moments_mode", 3), ("moments_mode", -1), ("key_order", 2), ("walk_variant", 4)):
+    assert p.radix_bits == 8 and p.stack_depth == 512
+    for field, bad in (("moments_mode", 3), ("moments_mode", -1), ("key_order", 2), ("walk_variant", 4),
+                       ("radix_bits", 7), ("radix_bits", 10), ("stack_depth", 359), ("stack_depth", 4097)):
         q = _lib.nbx_params()
         L.nbx_params_default(ctypes.byref(q))
         setattr(q, field, bad)
@@ -74,3 +76,11 @@ def test_capacity_bounds_without_gpu():
         setattr(q, field, bad)
         h = ctypes.c_void_p()
         assert L.nbx_create(ctypes.byref(q), ctypes.byref(h)) == 1, field
+
+
+def test_set_tuning_validates_without_gpu():
+    """nbx_set_tuning rejects a null context and out-of-range values before any CUDA call."""
+    from nns_gb300 import _lib
+    L = _lib.lib()
+    assert L.nbx_set_tuning(None, 8, 512) == 1
+    assert L.nbx_set_tuning(None, 9, 4096) == 1

@@ -119,6 +119,25 @@ def test_checkpoint_interval_does_not_change_gradients(cuda):
     assert np.allclose(g4, g12, rtol=1e-5, atol=1e-7 * np.abs(g4).max())
 
 
+def test_radix_width_does_not_change_the_adjoint(cuda):
+    """With 9-bit sort digits (7 passes) the adjoint's builds write the sort
+    permutation into its taped arrays as with 8-bit digits: the forward ends at
+    the same state bit for bit and the gradients agree (up to the order of the
+    FP64 atomic additions)."""
+    from nns_gb300.barnes_hut import State
+    b, ctx, adj, target = _setup(1024, 8, 4)
+    s8 = State.from_bodies(b)
+    adj.forward(s8, target)
+    _, g8 = _grads(b, adj, target)
+    ctx.set_tuning(9, 512)
+    s9 = State.from_bodies(b)
+    adj.forward(s9, target)
+    for u, v in zip(s8.host(), s9.host()):
+        assert np.array_equal(u, v)
+    _, g9 = _grads(b, adj, target)
+    assert np.allclose(g8, g9, rtol=1e-5, atol=1e-7 * np.abs(g8).max())
+
+
 def test_autograd_function(cuda):
     import torch
     from nns_gb300.adjoint import TrajectoryLoss

@@ -210,6 +210,65 @@ def test_batched_equals_unbatched(cuda):
             assert np.array_equal(t1[k], tb[k]), (i, k)
 
 
+def test_radix_width_gives_the_same_trees(cuda):
+    """9-bit digits (7 passes, the keys generated into the alternate buffers)
+    against 8-bit digits (8 passes): single systems of odd and ragged sizes and a
+    batch of uneven systems give the oracle's trees and bit-identical forces;
+    switching the width on a live context (nbx_set_tuning) and replaying the
+    step graph gives the same state as eager steps."""
+    for n in (1, 33, 4099, 16384):
+        b = ic.star_disk(n) if n > 1 else ic.plummer(1)
+        acc = {}
+        for bits in (8, 9):
+            ctx = _ctx(n, theta=0.5, eps=0.01, radix_bits=bits)
+            ctx.set_systems([0, n])
+            s = _state(b)
+            ctx.build(s)
+            ctx.forces(s)
+            ctx.sync()
+            _check_tree(ctx.export_tree(0), O.build(b.x, b.y, b.z, b.m))
+            acc[bits] = s.acc()
+        assert np.array_equal(acc[8], acc[9]), n
+    sizes = [1024, 37, 3000, 5, 2048, 777]
+    parts = [ic.star_disk(k, seed=ic.SEED0 + 1 + i) for i, k in enumerate(sizes)]
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    cat = lambda k: np.concatenate([getattr(p, k) for p in parts])  # noqa: E731
+    B = ic.Bodies(cat("x"), cat("y"), cat("z"), cat("vx"), cat("vy"), cat("vz"), cat("m"))
+    res = {}
+    for bits in (8, 9):
+        ctx = _ctx(int(off[-1]), nsys=len(sizes), theta=0.5, eps=0.01, radix_bits=bits)
+        ctx.set_systems(off)
+        s = _state(B)
+        ctx.build(s)
+        ctx.forces(s)
+        ctx.sync()
+        for i, p in enumerate(parts):
+            _check_tree(ctx.export_tree(i), O.build(p.x, p.y, p.z, p.m))
+        res[bits] = s.acc()
+    assert np.array_equal(res[8], res[9])
+    # live switch, graph replay against eager steps
+    n = int(off[-1])
+    ends = []
+    for graphs in (False, True):
+        ctx = _ctx(n, nsys=len(sizes), theta=0.5, eps=0.01, dt=1e-3)
+        ctx.set_systems(off)
+        s = _state(B)
+        if graphs:
+            ctx.graph_step(s, 2)
+            ctx.set_tuning(9, 512)
+            ctx.graph_step(s, 2)
+        else:
+            ctx.step(s)
+            ctx.step(s)
+            ctx.set_tuning(9, 512)
+            ctx.step(s)
+            ctx.step(s)
+        ctx.sync()
+        ends.append(s.host())
+    for a, b2 in zip(*ends):
+        assert np.array_equal(a, b2)
+
+
 def test_batched_equals_unbatched_hilbert(cuda):
     """Hilbert keys (key_order 1): each system of a batch equals its own
     single-system run bit for bit (keys, tree and forces)."""
@@ -463,13 +522,15 @@ def test_moments_modes_match_oracle(cuda, mode):
         _check_tree(ctx.export_tree(j), O.build(q.x, q.y, q.z, q.m))
 
 
-def test_sort_with_full_size_tiles(cuda):
+@pytest.mark.parametrize("radix_bits", [8, 9])
+def test_sort_with_full_size_tiles(cuda, radix_bits):
     """2^22 bodies: the radix sort runs with 2048-key tiles (smaller systems use
-    256..1024) for the bodies and the node entries.  The permutation equals the
-    oracle's 42-level key order and the tree's moments sum to the total mass."""
+    256..1024) for the bodies and the node entries, with 8-bit digits (8 passes)
+    or 9-bit digits (7 passes).  The permutation equals the oracle's 42-level
+    key order and the tree's moments sum to the total mass."""
     n = 1 << 22
     b = ic.binary_disk(n, seed=ic.SEED0 + 51)
-    ctx = _ctx(n, theta=0.5, eps=0.005)
+    ctx = _ctx(n, theta=0.5, eps=0.005, radix_bits=radix_bits)
     ctx.set_systems([0, n])
     s = _state(b)
     ctx.build(s)
@@ -495,8 +556,10 @@ def test_autotune_picks_a_valid_config(cuda, tmp_path, monkeypatch):
     s = _state(b)
     r = autotune.tune_walk(ctx, s, reps=1)
     assert (r["warps"], r["variant"]) in autotune.CANDIDATES and not r["cached"]
+    assert r["stack_depth"] in autotune.STACK_DEPTHS and r["radix_bits"] in autotune.RADIX_BITS
+    assert ctx.params.stack_depth == r["stack_depth"] and ctx.params.radix_bits == r["radix_bits"]
     r2 = autotune.tune_walk(ctx, s, reps=1)
-    assert r2["cached"] and r2["warps"] == r["warps"]
+    assert r2["cached"] and r2["warps"] == r["warps"] and r2["radix_bits"] == r["radix_bits"]
     ctx.build(s)
     ctx.forces(s)
     ctx.sync()
