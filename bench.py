@@ -238,7 +238,7 @@ def bench_batched(args, local):
             "speedup_vs_one_at_a_time_graphs": round(t_single_graph / t_batch, 3),
             "interactions_per_step": inter,
             "per_system_forces_bitwise_equal_unbatched": checks,
-            "walk_config": {"warps": tune["warps"], "variant": tune["variant"]}}
+            "walk_config": {k: tune[k] for k in ("warps", "variant", "stack_depth", "radix_bits")}}
 
 
 def bench_adjoint(args, local):
