@@ -28,6 +28,7 @@ sys.path.insert(0, ROOT)
 METRIC = "16M-body BH steps/s, plain vs compensated FP32 @1e-4 err; adjoint/fwd cost"
 N_DEFAULT = 1 << 24
 THETA, EPS, DT = 0.5, 0.005, 5e-4
+RUN_STEPS = 20  # the precision form's run length: energy drift is reported over it
 FLOP_PER_INTERACTION = 20
 
 
@@ -521,6 +522,8 @@ def main():
     with Clocks(local) as clk:
         plain = timed(args.steps)
     clocks = clk.summary()
+    extra = max(0, RUN_STEPS - args.warmup - args.steps)  # untimed, to the end of the run
+    timed(extra)
     energy1 = total_energy(ctx, s)
     diag1 = ctx.diagnostics(s)
     # ---- compensated FP32, the same steps from the same initial state
@@ -530,9 +533,10 @@ def main():
     ctx.set_constants(t_ref, e2, True)
     timed(args.warmup)
     comp = timed(args.steps)
+    timed(extra)
     ctx.set_constants(t_ref, e2, False)
     energy2 = total_energy(ctx, s)
-    nst = args.warmup + args.steps
+    nst = args.warmup + args.steps + extra
     energy = {"plain": {"steps": nst, "rel_drift": (energy1 - energy0) / abs(energy0)},
               "compensated": {"steps": nst, "rel_drift": (energy2 - energy0) / abs(energy0)},
               "e0": energy0, "how": "K (FP64 sum) + W = 1/2 sum m phi, phi from the Barnes-Hut walk; "
