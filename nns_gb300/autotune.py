@@ -53,8 +53,10 @@ def _time(fn, reps):
 
 
 def tune_walk(ctx, state, reps: int = 2, candidates=CANDIDATES, use_cache: bool = True,
-              stack_depths=STACK_DEPTHS, radix_bits=RADIX_BITS) -> dict:
-    """Times the candidate configurations and applies the fastest."""
+              stack_depths=STACK_DEPTHS, radix_bits=RADIX_BITS, timer=None) -> dict:
+    """Times the candidate configurations and applies the fastest.  ``timer(fn,
+    reps)`` returns milliseconds per call (CUDA events by default)."""
+    timer = timer or _time
     n = int(ctx.offsets[-1])
     key = _key(ctx, n)
     path = _cache_path()
@@ -77,7 +79,7 @@ def tune_walk(ctx, state, reps: int = 2, candidates=CANDIDATES, use_cache: bool 
     times = {}
     for warps, variant in candidates:
         ctx.set_walk(warps, variant)
-        times["%d/%d" % (warps, variant)] = _time(lambda: ctx.forces(state), reps)
+        times["%d/%d" % (warps, variant)] = timer(lambda: ctx.forces(state), reps)
     ctx.sync()
     wbest = min(times, key=times.get)
     warps, variant = (int(v) for v in wbest.split("/"))
@@ -88,7 +90,7 @@ def tune_walk(ctx, state, reps: int = 2, candidates=CANDIDATES, use_cache: bool 
     for depth in stack_depths:
         ctx.set_tuning(bits0, depth)
         try:
-            stimes[str(depth)] = _time(lambda: ctx.forces(state), reps)
+            stimes[str(depth)] = timer(lambda: ctx.forces(state), reps)
         except NbxError:
             continue
     ctx.sync()
@@ -97,7 +99,7 @@ def tune_walk(ctx, state, reps: int = 2, candidates=CANDIDATES, use_cache: bool 
     btimes = {}
     for bits in radix_bits:
         ctx.set_tuning(bits, depth)
-        btimes[str(bits)] = _time(lambda: ctx.build(state), reps)
+        btimes[str(bits)] = timer(lambda: ctx.build(state), reps)
     ctx.sync()
     bits = int(min(btimes, key=btimes.get))
     ctx.set_tuning(bits, depth)
