@@ -445,6 +445,32 @@ def test_errors_are_reported(cuda):
     ctx.sync()
 
 
+def test_stack_beyond_shared_memory_is_an_argument_error(cuda):
+    """4096 stack entries per warp with 16-warp blocks need about 326 KB of shared
+    memory per block (more than the device gives): the walk is not launched and
+    the call reports NBX_ERR_ARG; with 4-warp blocks (83 KB) the same context
+    walks and matches the oracle's lists."""
+    from nns_gb300._lib import NbxError
+    b = ic.star_disk(4096)
+    n = len(b.x)
+    ctx = _ctx(n, theta=0.5, eps=0.01, stack_depth=4096)
+    ctx.set_walk(16, 3)
+    ctx.set_systems([0, n])
+    s = _state(b)
+    ctx.build(s)
+    with pytest.raises(NbxError) as e:
+        ctx.forces(s)
+    assert e.value.code == 1  # NBX_ERR_ARG
+    ctx.set_walk(4, 3)
+    ctx.forces(s)
+    ctx.sync()
+    ot = O.build(b.x, b.y, b.z, b.m)
+    t, e2 = ctx.constants()
+    f = O.forces(b.x, b.y, b.z, b.m, ot, t, e2)
+    nl, _ = ctx.walk_stats()
+    assert np.array_equal(nl, f.nlist)
+
+
 def test_kernels_wrapper_sequence(cuda):
     """The reference's BarnesHut::update sequence through the phase entry points."""
     from nns_gb300.barnes_hut import BarnesHut
