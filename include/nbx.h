@@ -60,7 +60,8 @@ typedef struct nbx_params {
     float dampening;   /* velocity factor of the drift (main.cu:54) */
     float gravity;     /* accepted for interface parity; the force uses G = 1 (Kernels.cu:462) */
     int group;         /* bodies sharing one walk (warp-coherent MAC vote): 32 */
-    int stack_depth;   /* walk stack entries per warp */
+    int stack_depth;   /* walk stack entries per warp, 360..4096 (512); the stacks and buffers of
+                          one walk block must fit its shared memory (NBX_ERR_ARG otherwise) */
     int compensated;   /* 0 plain FP32; 1 split compensation (FP32 partial sums per
                           walk round, Kahan across rounds); 2 Kahan on every term */
     int leaf_size;     /* bodies per leaf: 1 */
