@@ -5,6 +5,9 @@ Bit-exact: bounding box, keys order, sort permutation, canonical topology
 FP32, per-group interaction-list lengths and the update.
 Forces: the same interaction lists evaluated in FP32 (rsqrt and summation
 order differ) -- tolerance 1e-5 median / 1e-4 max relative error.
+Both sort digit widths (8 bits in 8 passes, 9 bits in 7) give the same trees,
+and out-of-range launch settings are argument errors that leave the context
+usable.
 """
 import numpy as np
 import pytest
