@@ -31,12 +31,6 @@ def test_runner_report_and_frames(cuda, tmp_path):
     assert any(data[len(head):])  # something was drawn
 
 
-def test_runner_rejects_unknown_flag(cuda):
-    from nns_gb300 import build
-    build.build()
-    out = subprocess.run([build.RUNNER, "--no-such-flag"], capture_output=True, text=True, timeout=60)
-    assert out.returncode == 2
-
 
 @pytest.mark.parametrize("model", ["ref-plummer", "disk", "plummer"])
 def test_runner_models(cuda, tmp_path, model):
