@@ -144,8 +144,10 @@ int nbx_compute_bounding_box(nbx_ctx *ctx, int *mutex, float *x, float *y, float
  * bits.  Its scratch is a static per-device array of 4096 block partials
  * (128 KiB + 256 B) held by every GPU that loads the library: grid_size above
  * 4096 returns NBX_ERR_SCRATCH.  All calls on a device share that array, so
- * calls that overlap on the GPU race.  The first call on a device resolves the
- * array's address (cudaGetSymbolAddress): make it before any stream capture.
+ * calls that overlap on the GPU race.  Every call resolves the array's address
+ * in the current context (cudaGetSymbolAddress); the first call on a device,
+ * and the first after a device reset (which invalidates the old address), may
+ * load the module: make those calls before any stream capture.
  * `mutex` is accepted for the reference signature and unused. */
 int nbx_compute_bounding_box_noalloc(int *mutex, const float *x, const float *y, const float *z,
                                      float *minX, float *maxX, float *minY, float *maxY, float *minZ,
@@ -260,12 +262,15 @@ int nbx_diagnostics_fp64(nbx_ctx *ctx, const nbx_state *s, int n, double *out, v
 /* ---- checkpoint / resume -------------------------------------------------
  * The reference has none (it only writes frames).  A checkpoint is a raw dump
  * of every system's bodies (x, y, z, vx, vy, vz, m: the state a kick-drift step
- * needs) plus the system offsets and the step's constants (MAC constant,
- * softening, dt, dampening, compensation, key order), into a caller-owned host
- * buffer: a versioned header, the offsets, the seven float arrays, and 64-bit
- * checksums of header and payload.  Restoring it into a context (capacity
- * permitting) sets the systems and constants and copies the bodies into the
- * caller's device state, so that the run continues bit for bit. */
+ * needs) plus the system offsets, the step's constants (MAC constant,
+ * softening, dt, dampening, compensation, key order) and the walk's launch
+ * shape and buffer variant (which fix the order of the force sums), into a
+ * caller-owned host buffer: a versioned header (64 bytes), the offsets, the
+ * seven float arrays, and 64-bit checksums of header and payload.  Restoring
+ * it into a context (capacity permitting) sets the systems, constants and walk
+ * configuration and copies the bodies into the caller's device state, so that
+ * the run continues bit for bit.  The sort's digit width and the stack depth
+ * change no result and are not recorded. */
 int64_t nbx_checkpoint_bytes(int64_t nbodies, int nsystems);
 /* Synchronises `stream`; *written receives the bytes used. */
 int nbx_checkpoint_save(nbx_ctx *ctx, const nbx_state *s, void *host, int64_t capacity, int64_t *written,

@@ -36,7 +36,8 @@ def _cache_path():
 def _key(ctx, n):
     name = torch.cuda.get_device_name(ctx.device)
     nsys = 1 if ctx.offsets is None else len(ctx.offsets) - 1
-    return "%s|n=%d|sys=%d|comp=%d" % (name, n, nsys, int(ctx.params.compensated))
+    return "%s|n=%d|sys=%d|comp=%d|order=%d|moments=%d" % (name, n, nsys, int(ctx.params.compensated),
+                                                          int(ctx.params.key_order), int(ctx.params.moments_mode))
 
 
 def _time(fn, reps):

@@ -92,6 +92,7 @@ class Context:
         """compensated: 0 plain FP32, 1 split compensation, 2 Kahan on every term."""
         check(lib().nbx_set_constants(self.h, theta_ref, eps2, int(compensated)),
               "nbx_set_constants", self.h)
+        self.params.compensated = int(compensated)
 
     def set_walk(self, warps_per_block: int = 8, variant: int = 0):
         """Walk launch shape (4/8/16 warps per block) and variant (0 production, 2 simple)."""
@@ -237,7 +238,7 @@ class Context:
         check(lib().nbx_checkpoint_restore(self.h, C.byref(s.c), b.ctypes.data_as(C.c_void_p), b.size,
                                            _stream_ptr(stream)), "nbx_checkpoint_restore", self.h)
         nsys = int(np.frombuffer(b[12:16].tobytes(), np.int32)[0])
-        self.offsets = [int(v) for v in np.frombuffer(b[56:56 + 8 * (nsys + 1)].tobytes(), np.int64)]
+        self.offsets = [int(v) for v in np.frombuffer(b[64:64 + 8 * (nsys + 1)].tobytes(), np.int64)]
 
     def diagnostics(self, s: "State", n: int | None = None, stream=None):
         out = torch.zeros(8, dtype=torch.float64, device=self.device)

@@ -240,7 +240,7 @@ int reset_ref_arrays(Ctx *ctx, int *mutex, float *x, float *y, float *z, float *
                      int *sorted, int *child, int *index, float *minX, float *maxX, float *minY, float *maxY,
                      float *minZ, float *maxZ, int n, int m, cudaStream_t st) {
     int grid = ceil_div(m, kBlock);
-    if (grid > 152 * 16) grid = 152 * 16;
+    if (grid > ctx->nsm * 16) grid = ctx->nsm * 16;
     k_reset_ref<<<grid, kBlock, 0, st>>>(mutex, x, y, z, mass, count, start, sorted, child, index, minX, maxX,
                                          minY, maxY, minZ, maxZ, n, m);
     ++ctx->launches;
@@ -253,7 +253,7 @@ int bbox_ref(Ctx *ctx, const float *x, const float *y, const float *z, float *mi
     k_bbox_ref_seed<<<1, 32, 0, st>>>(ctx->d_bbox_u, minX, maxX, minY, maxY, minZ, maxZ);
     ++ctx->launches;
     int grid = ceil_div(n, kBlock);
-    if (grid > 152 * 8) grid = 152 * 8;
+    if (grid > ctx->nsm * 8) grid = ctx->nsm * 8;
     if (grid > 0) {
         k_bbox_ref<<<grid, kBlock, 0, st>>>(x, y, z, n, ctx->d_bbox_u);
         ++ctx->launches;
@@ -268,7 +268,7 @@ int direct_fp64(Ctx *ctx, const float *x, const float *y, const float *z, const 
                 const int *targets, int nt, double eps2, double *acc, cudaStream_t st) {
     if (nt <= 0 || n <= 0) return NBX_OK;
     const int gx = ceil_div(nt, kBlock);
-    int gy = ceil_div(152 * 4, gx);
+    int gy = ceil_div(ctx->nsm * 4, gx);
     if (gy > ceil_div(n, kBlock)) gy = ceil_div(n, kBlock);
     if (gy < 1) gy = 1;
     k_direct_fp64<<<dim3(gx, gy), kBlock, 0, st>>>(x, y, z, m, n, targets, nt, eps2, acc);
@@ -280,7 +280,7 @@ int direct_fp64(Ctx *ctx, const float *x, const float *y, const float *z, const 
 int diagnostics_fp64(Ctx *ctx, const nbx_state *s, int n, double *out, cudaStream_t st) {
     NBX_CUDA(cudaMemsetAsync(out, 0, 8 * sizeof(double), st));
     int grid = ceil_div(n, kBlock);
-    if (grid > 152 * 4) grid = 152 * 4;
+    if (grid > ctx->nsm * 4) grid = ctx->nsm * 4;
     if (grid > 0) {
         k_diag_fp64<<<grid, kBlock, 0, st>>>(s->x, s->y, s->z, s->vx, s->vy, s->vz, s->m, n, out);
         ++ctx->launches;

@@ -19,11 +19,12 @@
 //    launch, the partials are always written before they are read, and two
 //    calls whose kernels overlap on the GPU (different streams, no ordering)
 //    race on it and may return wrong boxes;
-//  * the first call on each device resolves the array's device address
-//    (cudaGetSymbolAddress, with that device current), which may load the
-//    module on that device: make that first call before any stream capture.
-#include <mutex>
-
+//  * every call resolves the array's device address on the current device
+//    (cudaGetSymbolAddress).  Once the module is loaded on a device that is a
+//    host-side lookup; the first call on a device, and the first call after a
+//    device reset (cudaDeviceReset ends the context, and the module is loaded
+//    again, possibly at another address), may load the module: make those
+//    calls before any stream capture.
 #include "nbx_internal.cuh"
 
 namespace nbx {
@@ -35,27 +36,18 @@ constexpr int kMaxBoxBlocks = 4096;      // partial boxes the scratch can hold
 constexpr int kPartStride = 8;           // words per partial (6 used, 32-byte rows)
 constexpr int kTicketWord = kMaxBoxBlocks * kPartStride;
 constexpr int kScratchWords = kTicketWord + 64;  // ticket in its own 256-byte line
-constexpr int kMaxDevices = 64;
 
 // The scratch.  In host code this name is only a host-side stand-in for the
 // symbol; kernels get its device address from cudaGetSymbolAddress.
 static __device__ __align__(256) unsigned g_box_scratch[kScratchWords];
 
-std::mutex g_scratch_mu;
-unsigned *g_scratch_ptr[kMaxDevices] = {};
-
-// Device address of the scratch on the current device; resolved once per device.
+// Device address of the scratch in the current device's context, resolved on
+// every call: no address outlives a context (a cached one would be stale after
+// a device reset or in another context on the same device).
 int scratch_on_current_device(unsigned **out) {
-    int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess) return NBX_ERR_CUDA;
-    if (dev < 0 || dev >= kMaxDevices) return NBX_ERR_ARG;
-    std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_box_scratch) != cudaSuccess || !p) return NBX_ERR_CUDA;
-        g_scratch_ptr[dev] = static_cast<unsigned *>(p);
-    }
-    *out = g_scratch_ptr[dev];
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_box_scratch) != cudaSuccess || !p) return NBX_ERR_CUDA;
+    *out = static_cast<unsigned *>(p);
     return NBX_OK;
 }
 
@@ -147,9 +139,14 @@ extern "C" int nbx_compute_bounding_box_noalloc(int *mutex, const float *x, cons
     if (grid_size < 0) return NBX_ERR_ARG;
     if (grid_size > nbx::kMaxBoxBlocks) return NBX_ERR_SCRATCH;
     int grid = grid_size;
-    if (grid == 0) {  // the context path's launch shape
+    if (grid == 0) {  // the context path's launch shape: at most 8 blocks per multiprocessor
+        int dev = 0, nsm = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1)
+            return NBX_ERR_CUDA;
         grid = (n + nbx::kBoxBlock - 1) / nbx::kBoxBlock;
-        if (grid > 152 * 8) grid = 152 * 8;
+        if (grid > nsm * 8) grid = nsm * 8;
+        if (grid > nbx::kMaxBoxBlocks) grid = nbx::kMaxBoxBlocks;
     }
     unsigned *scratch = nullptr;
     int rc = nbx::scratch_on_current_device(&scratch);

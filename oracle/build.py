@@ -19,7 +19,12 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("NBX_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: NBX_REFERENCE_ROOT, else a directory named
+# "reference" beside the repository.  Where neither exists the recipes build
+# only what needs no checkout.
+REF_ROOT = os.environ.get("NBX_REFERENCE_ROOT") or os.path.join(
+    os.path.dirname(os.path.dirname(os.path.abspath(__file__))), os.pardir, "reference")
+REF_ROOT = os.path.normpath(REF_ROOT)
 REF_CUDA = os.path.join(REF_ROOT, "3D", "CUDA", "CUDA_NBody")
 
 

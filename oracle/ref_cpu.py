@@ -25,7 +25,12 @@ import tempfile
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("NBX_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: NBX_REFERENCE_ROOT, else a directory named
+# "reference" beside the repository.  Where neither exists the recipes build
+# only what needs no checkout.
+REF_ROOT = os.environ.get("NBX_REFERENCE_ROOT") or os.path.join(
+    os.path.dirname(os.path.dirname(os.path.abspath(__file__))), os.pardir, "reference")
+REF_ROOT = os.path.normpath(REF_ROOT)
 REF_OMP = os.path.join(REF_ROOT, "3D", "OpenMP", "OpenMP_NBody")
 STAGE = os.path.join(HERE, "_ref", "omp")
 RUNNER = os.path.join(STAGE, "runner")
@@ -35,13 +40,14 @@ SKIP = {"main.cpp", "ConfigParser.cpp", "Renderer.cpp", "InitializeDistribution.
 CONSTANTS_SHIM = """#ifndef CONSTANTS_H_
 #define CONSTANTS_H_
 /* staged shim: G = dt^2 and TO_METERS = 1 make one reference step one
- * kick-drift step of length dt with G = 1 (see omp_harness.cpp) */
+ * kick-drift step of length dt with G = 1 (see omp_harness.cpp, which sets G
+ * from the NBX_REF_DT environment variable, default NBX_DT) */
 #ifndef NBX_DT
 #define NBX_DT 5e-4
 #endif
 const double PI = 3.14159265358979323846;
 const double TO_METERS = 1.0;
-const double G = (NBX_DT) * (NBX_DT);
+extern double G;
 extern int NUM_BODIES;
 extern int NUM_SUNS;
 extern double SYSTEM_SIZE;
@@ -143,21 +149,21 @@ def stage() -> bool:
 
 
 def build(dt: float = 5e-4) -> str | None:
+    """Compile the staged OpenMP code with the harness (dt is set per run through
+    NBX_REF_DT, so one build serves every configuration)."""
+    del dt
     if not stage():
         return None
     srcs = sorted(os.path.join(STAGE, "src", f) for f in os.listdir(os.path.join(STAGE, "src"))
                   if f.endswith(".cpp"))
-    stamp = os.path.join(STAGE, "dt.txt")
-    newest = max(os.path.getmtime(x) for x in srcs + [HARNESS])
-    if (os.path.exists(RUNNER) and os.path.getmtime(RUNNER) >= newest and os.path.exists(stamp)
-            and open(stamp).read() == repr(dt)):
+    newest = max(os.path.getmtime(x) for x in srcs + [HARNESS, os.path.join(STAGE, "include", "Constants.h")])
+    if os.path.exists(RUNNER) and os.path.getmtime(RUNNER) >= newest:
         return RUNNER
-    cmd = ["g++", "-O3", "-std=c++14", "-fopenmp", "-DNBX_DT=%r" % dt,
-           "-I", os.path.join(STAGE, "include"), HARNESS] + srcs + ["-o", RUNNER]
+    cmd = ["g++", "-O3", "-std=c++14", "-fopenmp", "-I", os.path.join(STAGE, "include"), HARNESS] + srcs \
+        + ["-o", RUNNER]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("reference OpenMP build failed:\n" + r.stderr[-3000:])
-    open(stamp, "w").write(repr(dt))
     return RUNNER
 
 
@@ -178,6 +184,7 @@ def run(b, theta, eps, dt, steps, warmup, mode="sample", k=65536, threads=None, 
     if runner is None:
         return None
     env = dict(os.environ)
+    env["NBX_REF_DT"] = repr(float(dt))
     if threads:
         env["OMP_NUM_THREADS"] = str(threads)
     with tempfile.TemporaryDirectory() as td:
@@ -198,24 +205,61 @@ def _workload(n):
     return ic.binary_disk(n)
 
 
-def bench_openmp(n, steps, warmup, theta, eps, dt, k=16384):
-    """Reference arm: the reference's OpenMP code on all host cores.  The full
-    tree is built once (serially, as the reference does) and its time charged
-    to every step; each step runs the reference's parallel force loop on k
-    random bodies and its update; step time = build + force * n / k + update."""
-    b = _workload(n)
+def bench_openmp(n, steps, warmup, theta, eps, dt, k=16384, b=None):
+    """The n/k model of a reference OpenMP step (an extrapolation, not a
+    measured step): the full tree is built once (serially, as the reference
+    does) and its time charged to every step; each step runs the reference's
+    parallel force loop on k random bodies and its update; step time = build +
+    force * n / k + update."""
+    b = _workload(n) if b is None else b
     res = run(b, theta, eps, dt, steps, max(0, min(warmup, 1)), "sample", k)
     if res is None:
         return None
     per = [sum(s) for s in res["steps"]]
     t = float(np.median(per))
-    return {"steps_per_s": 1.0 / t, "cores": res["threads"],
+    return {"steps_per_s": 1.0 / t, "cores": res["threads"], "extrapolated": True, "k": k, "n_over_k": n / k,
             "sample": "reference serial tree build over all %d bodies (timed once) + per step "
                       "the reference OpenMP force loop over %d random bodies scaled by n/k + "
                       "update; median of %d steps" % (n, k, len(per)),
             "phases_s": {"build": float(np.median([s[0] for s in res["steps"]])),
                          "force_scaled": float(np.median([s[1] for s in res["steps"]])),
                          "update": float(np.median([s[2] for s in res["steps"]]))}}
+
+
+def full_openmp(b, theta, eps, dt, steps):
+    """Whole, unsampled reference OpenMP steps (Interaction::interactBodies: tree
+    build, parallel force loop over every body, update), timed per step."""
+    res = run(b, theta, eps, dt, steps, 0, "full")
+    if res is None:
+        return None
+    per = [float(sum(s)) for s in res["steps"]]
+    return {"steps": len(per), "s_per_step": per, "median_s_per_step": float(np.median(per)),
+            "steps_per_s": 1.0 / float(np.median(per)), "cores": res["threads"], "n": len(b.x)}
+
+
+def reference_arm(n, theta, eps, dt, k=16384):
+    """The reference arm: whole reference OpenMP steps, measured.
+
+    * the benchmark workload (binary star + disk of n bodies): one whole step;
+    * the n/k model of the same step (k sampled bodies), with its error against
+      the measured step;
+    * config 0 (star + disk, 16384 bodies, theta 0.5, eps 0.01, dt 1e-3): all 10
+      steps;
+    * config 1 (Plummer, 2^20 bodies, theta 0.6, eps 0.005, dt 1e-3): one step.
+    """
+    from nns_gb300 import ic
+    b = _workload(n)
+    full = full_openmp(b, theta, eps, dt, 1)
+    if full is None:
+        return None
+    model = bench_openmp(n, 1, 0, theta, eps, dt, k, b=b)
+    del b
+    t_full = full["median_s_per_step"]
+    t_model = 1.0 / model["steps_per_s"]
+    c0 = full_openmp(ic.star_disk(16384), 0.5, 0.01, 1e-3, 10)
+    c1 = full_openmp(ic.plummer(1 << 20), 0.6, 0.005, 1e-3, 1)
+    return {"full": full, "model": dict(model, rel_error_vs_full=(t_model - t_full) / t_full),
+            "config0_star_disk_16384": c0, "config1_plummer_2^20": c1}
 
 
 def bench_serial(n, theta, eps, dt, k=1024, steps=1):
@@ -253,9 +297,10 @@ def serial_forces(b, theta, eps):
 
 
 def cpu_baseline(n, theta, eps, dt, k=4096):
-    """One bounded sample (one step) for the cpu_baseline key of the GPU arm."""
+    """One bounded sample (one step of the n/k model) for the cpu_baseline key of
+    the GPU arm; the measured whole step is the reference arm's."""
     r = bench_openmp(n, 1, 0, theta, eps, dt, k)
     if r is None:
         return {"unavailable": "reference CPU code not staged on this host"}
     return {"value": r["steps_per_s"], "unit": "steps/s", "cores": r["cores"], "kind": "reference",
-            "sample": r["sample"], "phases_s": r["phases_s"]}
+            "extrapolated": True, "k": k, "n_over_k": n / k, "sample": r["sample"], "phases_s": r["phases_s"]}

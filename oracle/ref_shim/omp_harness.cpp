@@ -6,7 +6,8 @@
  *
  * Units: the reference's kick is v += TIME_STEP*G*m*d/((d^2+s^2)*d) and its
  * drift x += TIME_STEP*v/TO_METERS (Interaction.cpp:144-182, 346-381).  The
- * staged Constants.h sets TO_METERS = 1 and G = dt^2, TIME_STEP = 1, and the
+ * staged Constants.h sets TO_METERS = 1 and TIME_STEP = 1, this file sets
+ * G = dt^2 (dt from the environment variable NBX_REF_DT, else NBX_DT), and the
  * velocities handed in are dt*v, which makes one reference step one kick-drift
  * step of length dt with G = 1.
  *
@@ -30,6 +31,7 @@
 #include <random>
 #include <vector>
 
+double G = (NBX_DT) * (NBX_DT);
 int NUM_BODIES = 0;
 int NUM_SUNS = 0;
 double SYSTEM_SIZE = 1.0;
@@ -55,6 +57,10 @@ int main(int argc, char **argv) {
         return 2;
     }
     const bool sample = std::strcmp(argv[1], "sample") == 0;
+    if (const char *e = std::getenv("NBX_REF_DT")) {
+        const double dt = std::atof(e);
+        if (dt > 0.0) G = dt * dt;
+    }
     FILE *f = std::fopen(argv[2], "rb");
     if (!f) return 3;
     int n = 0;

@@ -1,0 +1,98 @@
+"""Parity at the benchmark's own size: the binary star + disk of 2^24 bodies.
+
+The benchmark times this workload (two 0.5-mass stars at separation 0.2 and
+2^24 - 2 disk bodies of mass 1e-8, theta 0.5, eps 0.005), so its keys, sort
+permutation and canonical tree are checked here bit for bit against the
+oracle at full size, not inferred from smaller cases.  Its distribution is
+unlike the other parity cases: a tight binary inside a thin disk of 2^24
+light bodies (about 8.1 million cells, 16 levels deep).
+
+The walk is checked on 128 random walk groups (4096 bodies): per-body
+interaction-list length and opened-cell count bit-exact (identical MAC
+decisions), and forces within 1e-5 median / 1e-4 max relative error, for the
+plain FP32 walk and both compensated forms.  The oracle restates
+3D/CUDA/CUDA_NBody/src/Kernels.cu:157-456 (build and sort) and :460-577 (walk).
+"""
+import numpy as np
+import pytest
+
+from nns_gb300 import ic
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+MED_TOL, MAX_TOL = 1e-5, 1e-4
+N = 1 << 24
+THETA, EPS = 0.5, 0.005
+
+
+def _rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-30)
+
+
+@pytest.fixture(scope="module")
+def workload():
+    return ic.binary_disk(N)
+
+
+@pytest.fixture(scope="module")
+def oracle_tree(workload):
+    b = workload
+    return O.build(b.x, b.y, b.z, b.m)
+
+
+def test_binary_disk_2p24_tree_and_walk(cuda, workload, oracle_tree):
+    from nns_gb300.barnes_hut import Context, State
+    b, ot = workload, oracle_tree
+    ctx = Context(max_bodies=N, theta=THETA, eps=EPS, dt=5e-4)
+    ctx.set_systems([0, N])
+    s = State.from_bodies(b)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    info = ctx.tree_info()
+    assert info["status"] == 0 and info["ncells"] == ot.ncells
+
+    # keys and permutation: the oracle's 42-level key order
+    keys, perm = ctx.export_keys()
+    assert np.array_equal(perm, ot.perm)
+    hi, lo = O.keys(b.x, b.y, b.z, ot.bbox, 42)
+    assert np.array_equal(perm, np.lexsort((lo, hi)))
+    assert np.array_equal(keys, hi[perm])
+    del hi, lo, keys
+
+    # the full canonical topology and the FP64-summed moments
+    gt = ctx.export_tree(0)
+    assert np.array_equal(gt["perm"], ot.perm)
+    assert np.array_equal(gt["root_child"], ot.root_child)
+    assert gt["ncells"] == ot.ncells
+    for k in ("cell_child", "cell_start", "cell_count", "cell_level", "cell_x", "cell_y", "cell_z", "cell_m"):
+        assert np.array_equal(gt[k], getattr(ot, k)), k
+    del gt
+
+    # the walk on 128 random groups: the same lists, forces within tolerance
+    theta_ref, eps2 = ctx.constants()
+    groups = np.random.default_rng(7).choice(N // 32, 128, replace=False)
+    f = O.forces(b.x, b.y, b.z, b.m, ot, theta_ref, eps2, groups=groups)
+    idx = np.concatenate([ot.perm[g * 32:(g + 1) * 32] for g in groups])
+    nl, no = ctx.walk_stats()
+    assert np.array_equal(nl[idx], f.nlist[idx])
+    assert np.array_equal(no[idx], f.nopen[idx])
+    rel = _rel(s.acc()[idx], f.a[idx])
+    assert np.median(rel) <= MED_TOL and rel.max() <= MAX_TOL, (np.median(rel), rel.max())
+    plain64 = _rel(s.acc()[idx], f.a64[idx])
+
+    # compensated forms: the same lists, and no less accurate than the plain walk
+    for mode in (1, 2):
+        ctx.set_constants(theta_ref, eps2, mode)
+        ctx.build(s)
+        ctx.forces(s)
+        ctx.sync()
+        nl, no = ctx.walk_stats()
+        assert np.array_equal(nl[idx], f.nlist[idx]), mode
+        assert np.array_equal(no[idx], f.nopen[idx]), mode
+        rel = _rel(s.acc()[idx], f.a64[idx])
+        assert np.median(rel) <= MED_TOL and rel.max() <= MAX_TOL, (mode, np.median(rel), rel.max())
+        assert np.median(rel) <= np.median(plain64) * 1.01, (mode, np.median(rel), np.median(plain64))

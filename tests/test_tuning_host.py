@@ -115,3 +115,19 @@ def test_digit_width_gives_the_same_stable_order():
     want = np.argsort(keys, kind="stable")
     assert np.array_equal(_lsd_order(keys, 8), want)
     assert np.array_equal(_lsd_order(keys, 9), want)
+
+
+def test_cache_key_separates_orders_and_moment_passes(monkeypatch):
+    """Hilbert and Lebesgue order (and the centre-of-mass pass) change the tree and
+    the walk's cost, so a tuning result for one is never reused for another."""
+    from types import SimpleNamespace
+
+    from nns_gb300 import autotune
+    monkeypatch.setattr(autotune.torch.cuda, "get_device_name", lambda dev: "fake")
+    keys = set()
+    for order in (0, 1):
+        for moments in (0, 1, 2):
+            for comp in (0, 1):
+                p = SimpleNamespace(compensated=comp, key_order=order, moments_mode=moments)
+                keys.add(autotune._key(SimpleNamespace(device=0, offsets=[0, 100], params=p), 100))
+    assert len(keys) == 12

@@ -4,7 +4,8 @@ context entry point nbx_compute_bounding_box, both through the C ABI.
 Two calls in a row on different body sets (the second smaller, so the first
 call's partials and ticket are still in the shared scratch): the boxes must be
 bit-identical (min/max are exact, so the tolerance is zero).  Oversized grids
-are rejected before anything is launched.
+are rejected before anything is launched, and calls after the first leave the
+device's free memory unchanged.
 """
 import ctypes as C
 
@@ -83,3 +84,21 @@ def test_noalloc_bounding_box_rejects_oversized_grid(cuda):
     assert _noalloc_box(L, xyz, out, grid=-1) == 1
     torch.cuda.synchronize()
     assert torch.equal(out, _box(1.0))  # nothing launched
+
+
+def test_noalloc_bounding_box_allocates_nothing(cuda):
+    """The property the entry point exists for: after a first call (which may load
+    the module), calls of several sizes leave the device's free memory unchanged."""
+    import torch
+    from nns_gb300._lib import lib
+    L = lib()
+    sets = [_bodies(n, ic.SEED0 + 10 + j, 0.5 * j) for j, n in enumerate((1 << 18, 3000, 1 << 16))]
+    out = _box(0.0)
+    assert _noalloc_box(L, sets[0], out) == 0  # warm-up
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for xyz in sets * 3:
+        for grid in (0, 1, 4096):
+            assert _noalloc_box(L, xyz, out, grid=grid) == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
