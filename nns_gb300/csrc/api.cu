@@ -56,6 +56,22 @@ __global__ void k_body_sys(const int *sys_off, int nsys, int n, int *body_sys) {
     }
 }
 
+// The walk records one (list length, opened cells) pair per walk group (the
+// values are the same for the group's bodies); the export writes them per body
+// in original index order.
+__global__ void k_expand_gstat(const int2 *gstat, const int *groups, int ngroups, const int *body_sys,
+                               const int *sys_off, const int *val, int *nlist, int *nopen) {
+    const int g = blockIdx.x;
+    if (g >= ngroups) return;
+    const int p0 = groups[g];
+    const int p = p0 + (int)threadIdx.x;
+    if (p >= min(sys_off[body_sys[p0] + 1], p0 + 32)) return;
+    const int2 v = gstat[g];
+    const int ob = val[p];
+    if (nlist) nlist[ob] = v.x;
+    if (nopen) nopen[ob] = v.y;
+}
+
 __global__ void k_depth0_from_ptrs(const float *minX, const float *maxX, float theta_ref, float *depth0) {
     if (threadIdx.x == 0) {
         float r = __fmul_rn(__fsub_rn(*maxX, *minX), 0.5f);
@@ -79,7 +95,7 @@ void free_all(Ctx *ctx) {
     void *ptrs[] = {ctx->d_sys_off, ctx->d_body_sys, ctx->d_tiles, ctx->d_sys_tiles, ctx->d_groups,
                     ctx->d_bbox_u, ctx->d_bbox, ctx->d_bbox64, ctx->d_depth0, ctx->d_root_first,
                     ctx->d_root_nch, ctx->d_key, ctx->d_key_alt, ctx->d_key_lo, ctx->d_val, ctx->d_val_alt,
-                    ctx->d_body4, ctx->d_delta, ctx->d_ecount, ctx->d_body_node, ctx->d_nlist, ctx->d_nopen,
+                    ctx->d_body4, ctx->d_delta, ctx->d_ecount, ctx->d_body_node, ctx->d_gstat,
                     ctx->d_ent, ctx->d_ent_alt, ctx->d_flags, ctx->d_node4, ctx->d_meta, ctx->d_parent,
                     ctx->d_sums, ctx->d_count, ctx->d_arrive, ctx->d_lvl8, ctx->d_fcl, ctx->d_cl, ctx->d_hist,
                     ctx->d_scan_blk, ctx->d_totals, ctx->d_totals64, ctx->d_status};
@@ -249,8 +265,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     rc |= nbx::dmalloc(ctx, &ctx->d_delta, B);
     rc |= nbx::dmalloc(ctx, &ctx->d_ecount, B);
     rc |= nbx::dmalloc(ctx, &ctx->d_body_node, B);
-    rc |= nbx::dmalloc(ctx, &ctx->d_nlist, B);
-    rc |= nbx::dmalloc(ctx, &ctx->d_nopen, B);
+    rc |= nbx::dmalloc(ctx, &ctx->d_gstat, G);
     rc |= nbx::dmalloc(ctx, &ctx->d_ent, NC);
     rc |= nbx::dmalloc(ctx, &ctx->d_ent_alt, NC);
     rc |= nbx::dmalloc(ctx, &ctx->d_flags, NC);
@@ -682,10 +697,14 @@ int nbx_export_keys(nbx_ctx *c, uint64_t *keys, int *perm, void *stream) {
 int nbx_export_walk_stats(nbx_ctx *c, int *nlist, int *nopen, void *stream) {
     if (!c) return NBX_ERR_ARG;
     Ctx *ctx = C(c);
-    if (nlist)
-        NBX_CUDA(cudaMemcpyAsync(nlist, ctx->d_nlist, sizeof(int) * ctx->nbodies, cudaMemcpyDeviceToDevice, S(stream)));
-    if (nopen)
-        NBX_CUDA(cudaMemcpyAsync(nopen, ctx->d_nopen, sizeof(int) * ctx->nbodies, cudaMemcpyDeviceToDevice, S(stream)));
+    if (!ctx->built) return NBX_ERR_STATE;
+    if ((nlist || nopen) && ctx->ngroups > 0) {
+        nbx::k_expand_gstat<<<ctx->ngroups, 32, 0, S(stream)>>>(ctx->d_gstat, ctx->d_groups, ctx->ngroups,
+                                                                ctx->d_body_sys, ctx->d_sys_off, ctx->d_val, nlist,
+                                                                nopen);
+        ++ctx->launches;
+        NBX_CUDA(cudaGetLastError());
+    }
     NBX_CUDA(cudaStreamSynchronize(S(stream)));
     return NBX_OK;
 }

@@ -95,8 +95,7 @@ struct Ctx {
     unsigned char *d_delta = nullptr;  // [B]
     unsigned *d_ecount = nullptr;      // [B] entries per position -> exclusive offsets
     int *d_body_node = nullptr;        // [B] node of sorted position
-    int *d_nlist = nullptr;            // [B] per original index (walk statistics)
-    int *d_nopen = nullptr;
+    int2 *d_gstat = nullptr;           // [G] per walk group: list length, opened cells (last walk)
 
     // per node (entry / BFS order)
     unsigned *d_ent = nullptr, *d_ent_alt = nullptr;  // [NC] packed level<<26 | position

@@ -92,8 +92,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32)
            const int *__restrict__ val, const int *__restrict__ groups, int ngroups,
            const int *__restrict__ body_sys, const int *__restrict__ sys_off, const float *__restrict__ depth0,
            const int *__restrict__ root_first, const int *__restrict__ root_nch, float eps2, int stack_cap,
-           float *__restrict__ ax, float *__restrict__ ay, float *__restrict__ az, int *__restrict__ nlist,
-           int *__restrict__ nopen, DevStatus *st, double *__restrict__ a64, int n64) {
+           float *__restrict__ ax, float *__restrict__ ay, float *__restrict__ az, int2 *__restrict__ gstat,
+           DevStatus *st, double *__restrict__ a64, int n64) {
     extern __shared__ int smem_stack[];
     if (st->code != 0) return;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -197,9 +197,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32)
                 ay[ob] = fy;
                 az[ob] = fz;
             }
-            if (nlist) nlist[ob] = len;
-            if (nopen) nopen[ob] = opened;
         }
+        if (gstat && lane == 0) gstat[g] = make_int2(len, opened);
         tot_len += (unsigned long long)len * (unsigned long long)(end - p0);
         tot_open += (unsigned long long)opened;
     }
@@ -242,13 +241,13 @@ int walk_forces(Ctx *ctx, const nbx_state *s, cudaStream_t st) {
         k_walk<1><<<grid, kWalkWarps * 32, smem, st>>>(
             ctx->d_node4, ctx->d_meta, ctx->d_lvl8, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
             ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay,
-            s->az, ctx->d_nlist, ctx->d_nopen, ctx->d_status, nullptr, 0);
+            s->az, ctx->d_gstat, ctx->d_status, nullptr, 0);
         ++ctx->launches;
     } else {
         k_walk<0><<<grid, kWalkWarps * 32, smem, st>>>(
             ctx->d_node4, ctx->d_meta, ctx->d_lvl8, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
             ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay,
-            s->az, ctx->d_nlist, ctx->d_nopen, ctx->d_status, nullptr, 0);
+            s->az, ctx->d_gstat, ctx->d_status, nullptr, 0);
         ++ctx->launches;
     }
     NBX_CUDA(cudaGetLastError());
@@ -268,7 +267,7 @@ int walk_fp64_lists(Ctx *ctx, const int *group_starts, int ngroups, double *a64,
     k_walk<2><<<grid, kWalkWarps * 32, smem, st>>>(
         ctx->d_node4, ctx->d_meta, ctx->d_lvl8, ctx->d_body4, ctx->d_val, group_starts, ngroups, ctx->d_body_sys, ctx->d_sys_off,
         ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, nullptr, nullptr, nullptr, nullptr,
-        nullptr, ctx->d_status, a64, (int)ctx->nbodies);
+        ctx->d_status, a64, (int)ctx->nbodies);
     ++ctx->launches;
     NBX_CUDA(cudaGetLastError());
     return NBX_OK;

@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             const int *__restrict__ body_sys, const int *__restrict__ sys_off, const float *__restrict__ depth0,
             const int *__restrict__ root_first, const int *__restrict__ root_nch, float eps2, int stack_cap,
             float *__restrict__ ax, float *__restrict__ ay, float *__restrict__ az, float *__restrict__ pot,
-            int *__restrict__ nlist, int *__restrict__ nopen, DevStatus *st, int *__restrict__ rec_list,
+            int2 *__restrict__ gstat, DevStatus *st, int *__restrict__ rec_list,
             int *__restrict__ rec_len, int rec_cap) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     if (st->code != 0) return;
@@ -497,9 +497,8 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 // remove the body's own term m * rsqrt(eps2), then phi = -sum
                 pot[ob] = -((a0 + a1) - me.w * rsq(eps2));
             }
-            if (nlist) nlist[ob] = len;
-            if (nopen) nopen[ob] = opened;
         }
+        if (lane == 0) gstat[g] = make_int2(len, opened);
         tot_len += (unsigned long long)len * (unsigned long long)(end - p0);
         tot_open += (unsigned long long)opened;
     }
@@ -530,7 +529,7 @@ int launch(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st,
     k_walk2<CB, Mode, Pot, Rec><<<grid, warps * 32, smem, st>>>(
         ctx->d_node4, ctx->d_meta, ctx->d_lvl8, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
         ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay, s->az,
-        pot, ctx->d_nlist, ctx->d_nopen, ctx->d_status, rec_list, rec_len, rec_cap);
+        pot, ctx->d_gstat, ctx->d_status, rec_list, rec_len, rec_cap);
     ++ctx->launches;
     NBX_CUDA(cudaGetLastError());
     return NBX_OK;

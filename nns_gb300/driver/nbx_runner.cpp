@@ -29,75 +29,26 @@
 
 namespace {
 
-// Counter-based SplitMix64 stream, draw k of body i under seed s (the same
-// generator as nns_gb300/ic.py).
-uint64_t mix(uint64_t z) {
-    z ^= z >> 30;
-    z *= 0xBF58476D1CE4E5B9ull;
-    z ^= z >> 27;
-    z *= 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-}
-double uniform(uint64_t seed, uint64_t i, uint64_t draw) {
-    const uint64_t base = mix(seed * 0x9E3779B97F4A7C15ull + draw * 0xD1B54A32D192ED03ull);
-    return (double)(mix(base + (i + 1) * 0x9E3779B97F4A7C15ull) >> 11) * (1.0 / 9007199254740992.0);
-}
+// Draw `draw` of body i under `seed` (the generator of nns_gb300/ic.py).
+double uniform(uint64_t seed, uint64_t i, uint64_t draw) { return nbx::detail::uniform01(seed, i, draw); }
 
 struct Bodies {
     std::vector<float> x, y, z, vx, vy, vz, m;
     explicit Bodies(int n) : x(n), y(n), z(n), vx(n), vy(n), vz(n), m(n) {}
 };
 
-// BarnesHut::diskModel: a 1e5 central mass at the origin, bodies of mass 2e5/n
-// with radius in [1.5, 12), z = +-i*1e-7 and clockwise circular speed sqrt(M/r).
+// The reference constructor's disk and its Plummer recipe (nbx::disk_model,
+// nbx::plummer_model in include/nbx/barnes_hut.hpp).
 Bodies ref_disk(int n, uint64_t seed) {
     Bodies b(n);
-    const double pi = 3.14159265358979323846, sun = 100000.0;
-    for (int i = 0; i < n; i++) {
-        const double th = 2 * pi * uniform(seed, i, 0), r = 1.5 + 10.5 * uniform(seed, i, 1);
-        if (i == 0) {
-            b.m[i] = (float)sun;
-            continue;
-        }
-        b.m[i] = (float)(2 * sun / n);
-        b.x[i] = (float)(r * std::cos(th));
-        b.y[i] = (float)(r * std::sin(th));
-        b.z[i] = (float)((i % 2 == 0 ? 1e-7 : -1e-7) * i);
-        const double v = std::sqrt(sun / r);
-        b.vx[i] = (float)(v * std::sin(th));
-        b.vy[i] = (float)(-v * std::cos(th));
-    }
+    nbx::disk_model(n, seed, b.x.data(), b.y.data(), b.z.data(), b.vx.data(), b.vy.data(), b.vz.data(), b.m.data());
     return b;
 }
 
-// BarnesHut::plummerModel (BarnesHut.cu:304-354; present but not called by the
-// reference): unit masses, r = a / sqrt(u^-2/3 - 1) in the x-y plane, z = +-i*1e-3,
-// in-plane speed 100 q sqrt(2) (1 + r^2)^-1/4 with q by rejection on
-// q^2 (1 - q^2)^3.5 (bound 0.1).
 Bodies ref_plummer(int n, uint64_t seed) {
     Bodies b(n);
-    const double pi = 3.14159265358979323846;
-    for (int i = 0; i < n; i++) {
-        const double phi = 2 * pi * uniform(seed, i, 0);
-        const double u = std::max(uniform(seed, i, 1), 1e-12);
-        const double r = 1.0 / std::sqrt(std::pow(u, -0.666666) - 1.0);
-        b.m[i] = 1.f;
-        b.x[i] = (float)(r * std::cos(phi));
-        b.y[i] = (float)(r * std::sin(phi));
-        b.z[i] = (float)((i % 2 == 0 ? 1e-3 : -1e-3) * i);
-        double q = 0.0;
-        for (int d = 2; d < 4000; d += 2) {
-            const double qq = uniform(seed, i, d), tt = 0.1 * uniform(seed, i, d + 1);
-            if (tt <= qq * qq * std::pow(1 - qq * qq, 3.5)) {
-                q = qq;
-                break;
-            }
-        }
-        const double v = 100 * q * std::sqrt(2.0) * std::pow(1 + r * r, -0.25);
-        const double ph2 = 2 * pi * uniform(seed, i, 4001);
-        b.vx[i] = (float)(v * std::cos(ph2));
-        b.vy[i] = (float)(v * std::sin(ph2));
-    }
+    nbx::plummer_model(n, seed, b.x.data(), b.y.data(), b.z.data(), b.vx.data(), b.vy.data(), b.vz.data(),
+                       b.m.data());
     return b;
 }
 
@@ -232,7 +183,7 @@ int main(int argc, char **argv) {
         }
         for (int i = 0; i < p.iterations; i++) {
             bh.update(i);
-            if (verbosity > 0) std::printf("Elapsed time for step %d : %g ms\n", i, bh.time_all.back());
+            if (verbosity > 0) std::printf("Elapsed time for step %d : %g ms\n", i, bh.time_all[i]);
             if (render && i % p.renderInterval == 0) {
                 nbx_state st{};
                 st.x = bh.d_x; st.y = bh.d_y; st.z = bh.d_z;
@@ -254,9 +205,9 @@ int main(int argc, char **argv) {
             cudaFree(d_accum);
             cudaFree(d_rgb);
         }
-        auto total = [](const std::vector<float> &v) {
+        auto total = [&](const float *v) {
             double t = 0;
-            for (float x : v) t += x;
+            for (int i = 0; i < p.iterations; i++) t += v[i];
             return t;
         };
         const double it = p.iterations;

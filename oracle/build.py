@@ -8,6 +8,9 @@
 * ``oracle/_ref/libref_render.so`` -- the reference's renderer
   (3D/CUDA/CUDA_NBody/src/Renderer.cpp, Body.cpp, Logger.cpp) with the C entry
   point ``ref_shim/render_harness.cpp``, for the headless-frame parity.
+* ``oracle/_ref/libref_sfc.so`` -- the reference's SpaceFillingCurves tree code
+  (MolecularDynamics/BarnesHutParallel/SpaceFillingCurves/src/Tree.cpp) against the
+  single-process ``ref_shim/mpi.h``, for its Lebesgue-to-Hilbert key conversion.
 * ``oracle/_ref/omp/`` -- the reference's 3D/OpenMP tree code, staged from the
   checkout (see ``ref_cpu.py``) and compiled against a harness for the timed
   CPU baseline.
@@ -26,6 +29,7 @@ REF_ROOT = os.environ.get("NBX_REFERENCE_ROOT") or os.path.join(
     os.path.dirname(os.path.dirname(os.path.abspath(__file__))), os.pardir, "reference")
 REF_ROOT = os.path.normpath(REF_ROOT)
 REF_CUDA = os.path.join(REF_ROOT, "3D", "CUDA", "CUDA_NBody")
+REF_SFC = os.path.join(REF_ROOT, "MolecularDynamics", "BarnesHutParallel", "SpaceFillingCurves")
 
 
 def _run(cmd):
@@ -83,10 +87,32 @@ def build_ref_renderer() -> str | None:
     return out
 
 
+def build_ref_sfc() -> str | None:
+    """Compile the reference's SpaceFillingCurves tree code (Tree.cpp with the
+    Logger, Particle and Domain sources it needs) for the CPU against the
+    single-process ref_shim/mpi.h, with the C entry point
+    ref_shim/sfc_harness.cpp (only where the checkout exists)."""
+    if not os.path.isfile(os.path.join(REF_SFC, "src", "Tree.cpp")):
+        return None
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "libref_sfc.so")
+    shim = os.path.join(HERE, "ref_shim")
+    harness = os.path.join(shim, "sfc_harness.cpp")
+    if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(harness),
+                                                            os.path.getmtime(os.path.join(shim, "mpi.h"))):
+        return out
+    srcs = [os.path.join(REF_SFC, "src", f) for f in ("Tree.cpp", "Logger.cpp", "Particle.cpp", "Domain.cpp")]
+    _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-w", "-Wl,--no-undefined", "-I", shim,
+          "-I", os.path.join(REF_SFC, "include")] + srcs + [harness, "-o", out])
+    return out
+
+
 def build_all() -> None:
     build_oracle()
     build_ref_kernels()
     build_ref_renderer()
+    build_ref_sfc()
     from . import ref_cpu  # noqa: WPS433 -- staged reference CPU code
     ref_cpu.build()
 

@@ -66,6 +66,70 @@ def ref_lib():
     return _ref
 
 
+_sfc = None
+
+
+def ref_sfc_lib():
+    """The reference's SpaceFillingCurves key code compiled for the CPU, or None."""
+    global _sfc
+    if _sfc is None:
+        path = os.path.join(os.path.dirname(__file__), "_ref", "libref_sfc.so")
+        if not os.path.exists(path):
+            path = _build.build_ref_sfc()
+        if not path or not os.path.exists(path):
+            return None
+        _sfc = C.CDLL(path)
+        _sfc.ref_lebesgue2hilbert.argtypes = [_u64p, _u64p, C.c_long, C.c_int]
+    return _sfc
+
+
+KEY_MASK = np.uint64((1 << 63) - 1)
+
+
+def md_key(cuda_key):
+    """The reference MD code's Lebesgue key of the same cell path: its child number
+    sonNumber = [x>=mid] + 2[y>=mid] + 4[z>=mid] (SpaceFillingCurves/src/Tree.cpp:442)
+    is 7 - c for the CUDA path's c = [x<mid] + 2[y<mid] + 4[z<mid], i.e. every
+    bit of the 63-bit key inverted."""
+    return np.asarray(cuda_key, np.uint64) ^ KEY_MASK
+
+
+# The 12-state Lebesgue-to-Hilbert tables of the reference (Tree.cpp:70-104):
+# Hilbert digit and next state, indexed [state][Lebesgue child number].
+HILBERT_DIGIT = np.array([[0, 7, 3, 4, 1, 6, 2, 5], [4, 3, 7, 0, 5, 2, 6, 1], [6, 1, 5, 2, 7, 0, 4, 3],
+                          [2, 5, 1, 6, 3, 4, 0, 7], [0, 1, 7, 6, 3, 2, 4, 5], [6, 7, 1, 0, 5, 4, 2, 3],
+                          [2, 3, 5, 4, 1, 0, 6, 7], [4, 5, 3, 2, 7, 6, 0, 1], [0, 3, 1, 2, 7, 4, 6, 5],
+                          [2, 1, 3, 0, 5, 6, 4, 7], [4, 7, 5, 6, 3, 0, 2, 1], [6, 5, 7, 4, 1, 2, 0, 3]])
+HILBERT_STATE = np.array([[8, 10, 3, 3, 4, 5, 4, 5], [2, 2, 11, 9, 4, 5, 4, 5], [7, 6, 7, 6, 8, 10, 1, 1],
+                          [7, 6, 7, 6, 0, 0, 11, 9], [0, 8, 1, 11, 6, 8, 6, 11], [10, 0, 9, 1, 10, 7, 9, 7],
+                          [10, 4, 9, 4, 10, 2, 9, 3], [5, 8, 5, 11, 2, 8, 3, 11], [4, 9, 0, 0, 7, 9, 2, 2],
+                          [1, 1, 8, 5, 3, 3, 8, 6], [11, 5, 0, 0, 11, 6, 2, 2], [1, 1, 4, 10, 3, 3, 7, 10]])
+
+
+def hilbert(md_lebesgue, levels=21):
+    """Lebesgue2Hilbert (Tree.cpp:90-104) restated: the Hilbert key of an MD
+    Lebesgue key, digit by digit from the top level, state 0 at the root."""
+    k = np.asarray(md_lebesgue, np.uint64)
+    out = np.zeros_like(k)
+    state = np.zeros(k.shape, np.int64)
+    for lv in range(levels, 0, -1):
+        cell = ((k >> np.uint64(3 * (lv - 1))) & np.uint64(7)).astype(np.int64)
+        out = (out << np.uint64(3)) | HILBERT_DIGIT[state, cell].astype(np.uint64)
+        state = HILBERT_STATE[state, cell]
+    return out
+
+
+def ref_hilbert(md_lebesgue, levels=21):
+    """The reference's own Lebesgue2Hilbert on the keys, or None where unavailable."""
+    L = ref_sfc_lib()
+    if L is None:
+        return None
+    k = np.ascontiguousarray(md_lebesgue, np.uint64)
+    out = np.zeros_like(k)
+    L.ref_lebesgue2hilbert(k, out, len(k), levels)
+    return out
+
+
 def _f32(a):
     return np.ascontiguousarray(a, dtype=np.float32)
 

@@ -11,7 +11,8 @@ force kernel a wider (minX, maxX) so that its opening radius equals that of
 theta_ref = 0.25 (theta = 0.5), see ``force_bounds``.
 
 Run from the repository root where the reference checkout is present:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            (every fixture)
+    python tests/golden/make_golden.py hilbert    (sfc_hilbert4096.npz only)
 """
 from __future__ import annotations
 
@@ -121,9 +122,31 @@ def make_frames():
         print(name, rgb.shape, int((rgb > 0).sum()), "lit bytes")
 
 
+# Hilbert keys of the reference's own Lebesgue2Hilbert
+# (MolecularDynamics/BarnesHutParallel/SpaceFillingCurves/src/Tree.cpp:90-104,
+# compiled for the CPU by oracle/build.py): the 21-level keys of a seeded disk
+# (converted to the MD code's child numbering) and random 63-bit keys.
+def make_hilbert():
+    b = ic.star_disk(4096)
+    bb = O.bbox(b.x, b.y, b.z)
+    hi, _ = O.keys(b.x, b.y, b.z, bb, 21)
+    rnd = np.random.default_rng(20261203).integers(0, 2 ** 63, size=4096, dtype=np.uint64)
+    leb = np.concatenate([O.md_key(hi), rnd])
+    hil = O.ref_hilbert(leb)
+    if hil is None:
+        raise SystemExit("the reference SpaceFillingCurves code could not be built")
+    path = os.path.join(HERE, "sfc_hilbert4096.npz")
+    np.savez_compressed(path, n_disk=np.int64(len(b.x)), lebesgue_md=leb, hilbert=hil)
+    print("sfc_hilbert4096", len(leb), "keys", "%.1f KB" % (os.path.getsize(path) / 1024))
+
+
 def main():
     if O.ref_lib() is None:
         raise SystemExit("the reference checkout is needed to generate fixtures")
+    if sys.argv[1:] == ["hilbert"]:
+        make_hilbert()
+        return
+    make_hilbert()
     make_frames()
     for name, (gen, tight) in CASES.items():
         path, n, nc = make(name, gen, tight)

@@ -619,25 +619,23 @@ def test_fp64_list_evaluation_matches_oracle(cuda):
     assert np.median(rel) <= MED_TOL and rel.max() <= MAX_TOL
 
 
-_HD = np.array([[0, 7, 3, 4, 1, 6, 2, 5], [4, 3, 7, 0, 5, 2, 6, 1], [6, 1, 5, 2, 7, 0, 4, 3],
-                [2, 5, 1, 6, 3, 4, 0, 7], [0, 1, 7, 6, 3, 2, 4, 5], [6, 7, 1, 0, 5, 4, 2, 3],
-                [2, 3, 5, 4, 1, 0, 6, 7], [4, 5, 3, 2, 7, 6, 0, 1], [0, 3, 1, 2, 7, 4, 6, 5],
-                [2, 1, 3, 0, 5, 6, 4, 7], [4, 7, 5, 6, 3, 0, 2, 1], [6, 5, 7, 4, 1, 2, 0, 3]])
-_HS = np.array([[8, 10, 3, 3, 4, 5, 4, 5], [2, 2, 11, 9, 4, 5, 4, 5], [7, 6, 7, 6, 8, 10, 1, 1],
-                [7, 6, 7, 6, 0, 0, 11, 9], [0, 8, 1, 11, 6, 8, 6, 11], [10, 0, 9, 1, 10, 7, 9, 7],
-                [10, 4, 9, 4, 10, 2, 9, 3], [5, 8, 5, 11, 2, 8, 3, 11], [4, 9, 0, 0, 7, 9, 2, 2],
-                [1, 1, 8, 5, 3, 3, 8, 6], [11, 5, 0, 0, 11, 6, 2, 2], [1, 1, 4, 10, 3, 3, 7, 10]])
-
-
-def _hilbert(morton):
-    """Lebesgue -> Hilbert digit by digit (12-state tables, MD code Tree.cpp:70-104)."""
-    out = np.zeros_like(morton)
-    state = np.zeros(len(morton), np.int64)
-    for lv in range(1, 22):
-        b = 7 - ((morton >> np.uint64(3 * (21 - lv))) & np.uint64(7)).astype(np.int64)
-        out = (out << np.uint64(3)) | _HD[state, b].astype(np.uint64)
-        state = _HS[state, b]
-    return out
+def test_hilbert_keys_match_reference_fixture(cuda):
+    """key_order = 1 on the fixture's disk: every body's Hilbert key equals the
+    reference's own Lebesgue2Hilbert of its Lebesgue key (tests/golden/
+    sfc_hilbert4096.npz, made from SpaceFillingCurves/src/Tree.cpp:90-104)."""
+    import os
+    from nns_gb300.barnes_hut import Context
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "sfc_hilbert4096.npz")))
+    n = int(g["n_disk"])
+    b = ic.star_disk(n)
+    ctx = Context(max_bodies=n, theta=0.5, eps=0.01, key_order=1)
+    ctx.set_systems([0, n])
+    s = _state(b)
+    ctx.build(s)
+    ctx.sync()
+    keys, perm = ctx.export_keys()
+    assert np.array_equal(keys, g["hilbert"][:n][perm])
+    assert np.array_equal(perm, np.argsort(g["hilbert"][:n], kind="stable"))
 
 
 def test_hilbert_order_option(cuda):
@@ -656,7 +654,7 @@ def test_hilbert_order_option(cuda):
         outs[order] = (keys, perm, s.acc(), ctx.tree_info())
     bb = O.bbox(b.x, b.y, b.z)
     hi, _ = O.keys(b.x, b.y, b.z, bb, 21)
-    hk = _hilbert(hi)
+    hk = O.hilbert(O.md_key(hi))  # the reference's conversion (pinned on the CPU)
     keys, perm, acc_h, info_h = outs[1]
     assert np.array_equal(keys, hk[perm])
     assert np.all(np.diff(keys.astype(np.float64)) >= 0)

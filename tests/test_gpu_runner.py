@@ -41,3 +41,23 @@ def test_runner_models(cuda, tmp_path, model):
     assert out.returncode == 0, out.stderr
     m = re.search(r"final position of body 1: (\S+) (\S+) (\S+)", out.stdout)
     assert m and all(abs(float(v)) < 1e6 for v in m.groups())
+
+
+def test_reference_driver_runs_on_libnbx(cuda, tmp_path):
+    """The reference's main.cu, relinked against libnbx (oracle/drop_in.py), runs
+    a few steps of its own disk model through BarnesHut(parameters) and prints
+    its TIME report (main.cu:125-181) through the reference's Logger."""
+    from oracle import drop_in
+    path = drop_in.build()
+    if path is None:
+        pytest.skip("the reference driver is not staged on this host")
+    out = subprocess.run([path, "-n", "4096", "-i", "3"], cwd=tmp_path, capture_output=True, text=True,
+                         timeout=300)
+    assert out.returncode == 0, out.stderr
+    text = out.stdout
+    for phase in ("reset arrays", "compute bounding boxes", "build tree", "compute COM", "sort",
+                  "compute forces", "update bodies", "copy from device to host"):
+        m = re.search(r"Time to %s: ([0-9.e+-]+)ms" % phase, text)
+        assert m and float(m.group(1)) >= 0.0, phase
+    assert float(re.search(r"Time to compute forces: ([0-9.e+-]+)ms", text).group(1)) > 0.0
+    assert "TOTAL TIME" in text

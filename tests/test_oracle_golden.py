@@ -22,7 +22,7 @@ from oracle import oracle as O
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURES = sorted(p for p in glob.glob(os.path.join(HERE, "golden", "*.npz"))
-                  if not os.path.basename(p).startswith("frame_"))
+                  if not os.path.basename(p).startswith(("frame_", "sfc_")))
 REF_THETA, REF_EPS2 = 1.5, 0.0025  # Kernels.cu:17-18
 
 
@@ -120,3 +120,16 @@ def test_direct_fp64_self_consistency():
     # total force of a self-gravitating system is zero (Newton's third law)
     tot = (a * b.m[:, None].astype(np.float64)).sum(0)
     assert np.abs(tot).max() < 1e-12
+
+
+def test_hilbert_keys_are_the_reference_conversion():
+    """The oracle's Lebesgue-to-Hilbert conversion equals the reference's own
+    Lebesgue2Hilbert (SpaceFillingCurves/src/Tree.cpp:90-104) on its fixture
+    (a seeded disk's keys and random 63-bit keys) and, where the reference code
+    builds here, on fresh random keys."""
+    g = _load(os.path.join(HERE, "golden", "sfc_hilbert4096.npz"))
+    assert np.array_equal(O.hilbert(g["lebesgue_md"]), g["hilbert"])
+    rnd = np.random.default_rng(11).integers(0, 2 ** 63, size=100000, dtype=np.uint64)
+    live = O.ref_hilbert(rnd)
+    if live is not None:
+        assert np.array_equal(O.hilbert(rnd), live)
