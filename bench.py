@@ -178,24 +178,27 @@ def bench_batched(args, local):
     ctx.set_systems(off)
     s = State.from_bodies(bodies, device="cuda:%d" % local)
     tune = autotune.tune_walk(ctx, s, use_cache=False)
-    # per-system forces of the batch against single-system runs (bit for bit)
+    # per-system forces of the batch against single-system runs of every system
+    # (bit for bit); the single-system contexts are then timed one at a time
     ctx.build(s)
     ctx.forces(s)
     ctx.sync()
     accb = s.acc()
-    checks = []
-    for i in range(min(4, nsys)):
+    ctxs, states = [], []
+    for i in range(nsys):
         a, b = int(off[i]), int(off[i + 1])
         sub = ic.Bodies(*(arr[a:b] for arr in bodies.arrays()))
         c1 = Context(max_bodies=b - a, theta=0.5, eps=0.01, dt=1e-3, device=local)
         c1.set_walk(tune["warps"], tune["variant"])
         c1.set_systems([0, b - a])
-        s1 = State.from_bodies(sub, device="cuda:%d" % local)
+        ctxs.append(c1)
+        states.append(State.from_bodies(sub, device="cuda:%d" % local))
+    equal = 0
+    for i, (c1, s1) in enumerate(zip(ctxs, states)):
         c1.build(s1)
         c1.forces(s1)
         c1.sync()
-        checks.append(bool(np.array_equal(accb[a:b], s1.acc())))
-        del c1, s1
+        equal += bool(np.array_equal(accb[int(off[i]):int(off[i + 1])], s1.acc()))
     steps = max(2, args.steps)
     ctx.graph_step(s, max(1, args.warmup))
     torch.cuda.synchronize()
@@ -208,15 +211,6 @@ def bench_batched(args, local):
     t_batch = e0.elapsed_time(e1) / steps
     inter = ctx.tree_info()["interactions"]
     # one system at a time (eager launches, one context per system)
-    ctxs, states = [], []
-    for i in range(nsys):
-        a, b = int(off[i]), int(off[i + 1])
-        sub = ic.Bodies(*(arr[a:b] for arr in bodies.arrays()))
-        c1 = Context(max_bodies=b - a, theta=0.5, eps=0.01, dt=1e-3, device=local)
-        c1.set_walk(tune["warps"], tune["variant"])
-        c1.set_systems([0, b - a])
-        ctxs.append(c1)
-        states.append(State.from_bodies(sub, device="cuda:%d" % local))
     for c1, s1 in zip(ctxs, states):
         c1.step(s1, 1)
     torch.cuda.synchronize()
@@ -252,7 +246,7 @@ def bench_batched(args, local):
             "one_at_a_time_graphs_ms_per_step": round(t_single_graph, 3),
             "speedup_vs_one_at_a_time_graphs": round(t_single_graph / t_batch, 3),
             "interactions_per_step": inter,
-            "per_system_forces_bitwise_equal_unbatched": checks,
+            "per_system_forces_bitwise_equal_unbatched": {"systems_checked": nsys, "equal": equal},
             "walk_config": {k: tune[k] for k in ("warps", "variant", "stack_depth", "radix_bits")}}
 
 
@@ -367,26 +361,35 @@ def bench_hilbert(args, local, b, targets, acc64, tune) -> dict:
 
 
 ACCURACY_TARGET = 1e-4
-ACCURACY_THETAS = (0.4, 0.3, 0.25, 0.2, 0.15)
+ACCURACY_THETAS = {0: (0.4, 0.3, 0.25, 0.2, 0.15, 0.125, 0.1),
+                   1: (0.5, 0.45, 0.4, 0.35, 0.3, 0.25, 0.2)}
 
 
-def bench_accuracy(args, local, b, targets, acc64, tune) -> dict:
+def bench_accuracy(args, local, b, targets, acc64, tune, multipole=0) -> dict:
     """The same workload at smaller opening angles, until the median force error
     against the FP64 direct sum reaches 1e-4 (the headline's theta 0.5 meets
-    1e-4 only as FP32 arithmetic error of its own lists).  The parity-mode walk
-    (monopoles, the reference's MAC with theta_ref = theta^2): per theta the
-    error on the same 8192 targets, then plain FP32 steps timed with CUDA events
-    after one warm-up step."""
+    1e-4 only as FP32 arithmetic error of its own lists).  multipole 0: the
+    parity-mode walk (monopoles, the reference's MAC with theta_ref = theta^2);
+    1: the same lists with cell quadrupoles.  Per theta the error on the same
+    8192 targets, then plain FP32 steps timed with CUDA events after one
+    warm-up step."""
     import torch
     from nns_gb300.barnes_hut import Context, State
     n = len(b.x)
-    ctx = Context(max_bodies=n, theta=THETA, eps=EPS, dt=DT, device=local)
-    if tune:
-        ctx.set_walk(tune["warps"], tune["variant"])
+    ctx = Context(max_bodies=n, theta=THETA, eps=EPS, dt=DT, device=local, multipole=multipole)
     ctx.set_systems([0, n])
+    walk = None
+    if multipole:
+        # the quadrupole walk stages more per candidate: its own launch shape
+        from nns_gb300 import autotune
+        tq = autotune.tune_walk(ctx, State.from_bodies(b, device="cuda:%d" % local), use_cache=False,
+                                stack_depths=(512,), radix_bits=(8,))
+        walk = {"warps": tq["warps"], "variant": tq["variant"], "ms": tq["ms"]}
+    elif tune:
+        ctx.set_walk(tune["warps"], tune["variant"])
     _, eps2 = ctx.constants()
     points, at_target = [], None
-    for th in ACCURACY_THETAS:
+    for th in ACCURACY_THETAS[multipole]:
         ctx.set_constants(float(np.float32(th) * np.float32(th)), eps2, 0)
         s = State.from_bodies(b, device="cuda:%d" % local)
         ctx.build(s)
@@ -418,17 +421,25 @@ def bench_accuracy(args, local, b, targets, acc64, tune) -> dict:
         if np.median(rel) <= ACCURACY_TARGET:
             at_target = pt
             break
-    return {"target_median": ACCURACY_TARGET, "points": points, "at_target": at_target,
-            "note": "parity-mode walk (monopoles, the reference MAC) at smaller theta; "
-                    "the first theta in %s whose median error meets the target" % (list(ACCURACY_THETAS),)}
+    kind = ("parity-mode walk (monopoles, the reference MAC)" if multipole == 0 else
+            "quadrupole mode (the reference MAC and lists, plus cell quadrupoles; not the parity mode)")
+    return {"multipole": multipole, "target_median": ACCURACY_TARGET, "points": points, "at_target": at_target,
+            "walk_config": walk,
+            "note": "%s; the first theta in %s whose median error meets the target"
+                    % (kind, list(ACCURACY_THETAS[multipole]))}
 
 
-def error_target(errs, errs32, accuracy) -> dict:
+def error_target(errs, errs32, accuracy, accuracy_quad) -> dict:
     """Which reading of the metric's 1e-4 force error the headline meets: the FP32
     arithmetic error against an FP64 evaluation of the same interaction lists
     (met), and the total error against the FP64 direct sum (not at theta 0.5;
-    the accuracy section gives the steps/s at the theta that meets it)."""
-    at = accuracy.get("at_target") if isinstance(accuracy, dict) else None
+    the accuracy sections give the steps/s at the theta that meets it, with
+    monopoles and with quadrupoles)."""
+    def at_target(acc):
+        at = acc.get("at_target") if isinstance(acc, dict) else None
+        return None if at is None else {"theta": at["theta"], "median": at["force_error_vs_fp64_direct"]["median"],
+                                        "steps_per_s": at["steps_per_s"],
+                                        "interactions_per_step": at["interactions_per_step"]}
     return {"target_median_rel": ACCURACY_TARGET,
             "fp32_vs_fp64_same_lists": {"theta": THETA,
                                         "plain": errs32["plain"]["median"],
@@ -438,9 +449,8 @@ def error_target(errs, errs32, accuracy) -> dict:
             "vs_fp64_direct": {"theta": THETA, "plain": errs["plain"]["median"],
                                "compensated": errs["compensated"]["median"],
                                "met": bool(errs["plain"]["median"] <= ACCURACY_TARGET)},
-            "vs_fp64_direct_at_target": None if at is None else
-            {"theta": at["theta"], "median": at["force_error_vs_fp64_direct"]["median"],
-             "steps_per_s": at["steps_per_s"], "interactions_per_step": at["interactions_per_step"]}}
+            "vs_fp64_direct_at_target": at_target(accuracy),
+            "vs_fp64_direct_at_target_quadrupole": at_target(accuracy_quad)}
 
 
 def _section(fn, *a):
@@ -701,10 +711,13 @@ def main():
     batched = None
     del ctx, s
     torch.cuda.empty_cache()
-    accuracy = None
+    accuracy = accuracy_quad = None
     if not args.no_accuracy:
         accuracy = _section(bench_accuracy, args, local, b, targets, acc64,
-                            tune if tune and "warps" in tune else None)
+                            tune if tune and "warps" in tune else None, 0)
+        torch.cuda.empty_cache()
+        accuracy_quad = _section(bench_accuracy, args, local, b, targets, acc64,
+                                 tune if tune and "warps" in tune else None, 1)
         torch.cuda.empty_cache()
     hilbert = None
     if not args.no_hilbert:
@@ -743,8 +756,9 @@ def main():
                         "ratio_to_plain_time": round(ms_comp / ms_plain, 4)},
         "force_error_vs_fp64_direct": errs,
         "fp32_error_vs_fp64_same_lists": errs32,
-        "error_target": error_target(errs, errs32, accuracy),
+        "error_target": error_target(errs, errs32, accuracy, accuracy_quad),
         "accuracy": accuracy,
+        "accuracy_quadrupole": accuracy_quad,
         "frame": frame,
         "energy_drift": energy,
         "interactions_per_step": inter_per_step,

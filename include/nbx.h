@@ -82,6 +82,11 @@ typedef struct nbx_params {
                           per level above); 1 one launch per tree level; 2 one launch in
                           which the last child to finish sums its parent.  The sums are
                           the same FP64 additions in the same order in every mode */
+    int multipole;     /* 0: monopoles, the reference's force (Kernels.cu:538-551; the parity
+                          mode); 1: monopoles plus the traceless quadrupole of every accepted
+                          cell (FP64 second moments, FP32 terms).  The interaction lists are
+                          the same in both; quadrupoles only change what an accepted cell adds.
+                          Not available with walk_variant 2 or the adjoint */
 } nbx_params;
 
 /* SoA device state of all systems; systems are contiguous ranges. */
@@ -124,6 +129,12 @@ int nbx_set_walk_config(nbx_ctx *ctx, int warps_per_block, int variant);
  * stacks and buffers exceed the device's shared memory per block fails with
  * NBX_ERR_ARG).  A built tree stays valid.  Used by the autotuner. */
 int nbx_set_tuning(nbx_ctx *ctx, int radix_bits, int stack_depth);
+/* Multipole order of the force (nbx_params.multipole: 0 monopoles, 1 with
+ * quadrupoles).  The context needs a new build before its next walk
+ * (NBX_ERR_STATE otherwise); switching to 1 allocates the quadrupole arrays
+ * on first use (NBX_ERR_NOMEM if that fails).  No counterpart in the
+ * reference, whose kernels carry monopoles only. */
+int nbx_set_multipole(nbx_ctx *ctx, int multipole);
 
 /* ---- reference-compatible phase entry points (KernelsWrapper.cu) ---- */
 /* KernelsWrapper::resetArrays (KernelsWrapper.cu:28; Kernels.cu:21-64) */

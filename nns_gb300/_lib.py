@@ -27,7 +27,7 @@ class nbx_params(C.Structure):
                 ("leaf_size", C.c_int), ("radix_bits", C.c_int), ("walk_warps", C.c_int),
                 ("device", C.c_int), ("block_size", C.c_int), ("grid_size", C.c_int),
                 ("walk_variant", C.c_int), ("key_order", C.c_int), ("node_capacity", C.c_int),
-                ("moments_mode", C.c_int)]
+                ("moments_mode", C.c_int), ("multipole", C.c_int)]
 
 
 class nbx_state(C.Structure):
@@ -72,6 +72,7 @@ SIGNATURES = {
     "nbx_update": (_I, [_P] + [_P] * 9 + [_I, _F, _F, _P, _PF]),
     "nbx_set_walk_config": (_I, [_P, _I, _I]),
     "nbx_set_tuning": (_I, [_P, _I, _I]),
+    "nbx_set_multipole": (_I, [_P, _I]),
     "nbx_set_systems": (_I, [_P, _I, C.POINTER(C.c_int64)]),
     "nbx_build": (_I, [_P, C.POINTER(nbx_state), _P]),
     "nbx_forces": (_I, [_P, C.POINTER(nbx_state), _P]),

@@ -36,8 +36,9 @@ def _cache_path():
 def _key(ctx, n):
     name = torch.cuda.get_device_name(ctx.device)
     nsys = 1 if ctx.offsets is None else len(ctx.offsets) - 1
-    return "%s|n=%d|sys=%d|comp=%d|order=%d|moments=%d" % (name, n, nsys, int(ctx.params.compensated),
-                                                          int(ctx.params.key_order), int(ctx.params.moments_mode))
+    return "%s|n=%d|sys=%d|comp=%d|order=%d|moments=%d|multipole=%d" % (
+        name, n, nsys, int(ctx.params.compensated), int(ctx.params.key_order), int(ctx.params.moments_mode),
+        int(getattr(ctx.params, "multipole", 0)))
 
 
 def _time(fn, reps):

@@ -46,7 +46,7 @@ class Context:
                  theta_ref: float | None = None, eps: float = 0.05, eps2: float | None = None,
                  dt: float = 1e-3, dampening: float = 1.0, compensated: int = 0,
                  stack_depth: int = 512, device: int = 0, key_order: int = 0, node_capacity: int = 0,
-                 moments_mode: int = 0, radix_bits: int = 8):
+                 moments_mode: int = 0, radix_bits: int = 8, multipole: int = 0):
         p = L.nbx_params()
         lib().nbx_params_default(C.byref(p))
         p.max_bodies = int(max_bodies)
@@ -64,6 +64,7 @@ class Context:
         p.moments_mode = moments_mode
         p.device = device
         p.key_order = int(key_order)
+        p.multipole = int(multipole)
         self.params = p
         h = C.c_void_p()
         check(lib().nbx_create(C.byref(p), C.byref(h)), "nbx_create")
@@ -105,6 +106,12 @@ class Context:
         check(lib().nbx_set_tuning(self.h, int(radix_bits), int(stack_depth)), "nbx_set_tuning", self.h)
         self.params.radix_bits = int(radix_bits)
         self.params.stack_depth = int(stack_depth)
+
+    def set_multipole(self, multipole: int):
+        """0 monopoles (the reference's force), 1 with cell quadrupoles; the next
+        walk needs a new build."""
+        check(lib().nbx_set_multipole(self.h, int(multipole)), "nbx_set_multipole", self.h)
+        self.params.multipole = int(multipole)
 
     def set_systems(self, offsets):
         off = np.ascontiguousarray(offsets, dtype=np.int64)

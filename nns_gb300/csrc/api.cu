@@ -98,7 +98,8 @@ void free_all(Ctx *ctx) {
                     ctx->d_body4, ctx->d_delta, ctx->d_ecount, ctx->d_body_node, ctx->d_gstat,
                     ctx->d_ent, ctx->d_ent_alt, ctx->d_flags, ctx->d_node4, ctx->d_meta, ctx->d_parent,
                     ctx->d_sums, ctx->d_count, ctx->d_arrive, ctx->d_lvl8, ctx->d_fcl, ctx->d_cl, ctx->d_hist,
-                    ctx->d_scan_blk, ctx->d_totals, ctx->d_totals64, ctx->d_status};
+                    ctx->d_scan_blk, ctx->d_totals, ctx->d_totals64, ctx->d_status, ctx->d_m2, ctx->d_quad4,
+                    ctx->d_quad2};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
@@ -133,6 +134,25 @@ struct Timer {
         return rc;
     }
 };
+
+// The quadrupole arrays (second moments and FP32 terms), allocated when the
+// multipole mode is first used.
+int alloc_quadrupoles(Ctx *ctx) {
+    if (ctx->d_m2) return NBX_OK;
+    const size_t nc = (size_t)ctx->cap_nodes;
+    int rc = dmalloc(ctx, &ctx->d_m2, 3 * nc);
+    if (rc == 0) rc = dmalloc(ctx, &ctx->d_quad4, nc);
+    if (rc == 0) rc = dmalloc(ctx, &ctx->d_quad2, nc);
+    if (rc) {
+        cudaFree(ctx->d_m2);
+        cudaFree(ctx->d_quad4);
+        cudaFree(ctx->d_quad2);
+        ctx->d_m2 = nullptr;
+        ctx->d_quad4 = nullptr;
+        ctx->d_quad2 = nullptr;
+    }
+    return rc;
+}
 
 int ensure_single_system(Ctx *ctx, int n) {
     if (ctx->nsys == 1 && ctx->nbodies == n) return NBX_OK;
@@ -172,6 +192,7 @@ void nbx_params_default(nbx_params *p) {
     p->device = 0;
     p->block_size = 256;
     p->grid_size = 1024;
+    p->multipole = 0;
 }
 
 const char *nbx_status_string(int s) {
@@ -201,7 +222,8 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     if (p->max_bodies < 1 || p->max_bodies > (1 << 26) || p->max_systems < 1 ||
         p->max_systems > p->max_bodies || p->group != 32 || p->leaf_size != 1 || (p->radix_bits != 8 && p->radix_bits != 9) ||
         p->stack_depth < 360 || p->stack_depth > 4096 || p->walk_variant < 0 || p->walk_variant > 3 ||
-        p->moments_mode < 0 || p->moments_mode > 2 ||
+        p->moments_mode < 0 || p->moments_mode > 2 || p->multipole < 0 || p->multipole > 1 ||
+        (p->multipole == 1 && p->walk_variant == 2) ||
         (p->node_capacity != 0 && (p->node_capacity < p->max_bodies + 1 || p->node_capacity > nbx::kMaxNodes)))
         return NBX_ERR_ARG;
     Ctx *ctx = new (std::nothrow) Ctx();
@@ -213,6 +235,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     ctx->walk_variant = p->walk_variant;
     ctx->key_order = p->key_order;
     ctx->radix_bits = p->radix_bits;
+    ctx->multipole = p->multipole;
     if (p->key_order < 0 || p->key_order > 1) {
         delete ctx;
         return NBX_ERR_ARG;
@@ -286,6 +309,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     if (rc == 0 && cudaMallocHost((void **)&ctx->h_status, sizeof(nbx::DevStatus)) != cudaSuccess) rc = NBX_ERR_NOMEM;
     if (rc == 0 && cudaMemset(ctx->d_status, 0, sizeof(nbx::DevStatus)) != cudaSuccess) rc = NBX_ERR_CUDA;
     if (rc == 0 && cudaMemset(ctx->d_totals, 0, 8 * sizeof(unsigned)) != cudaSuccess) rc = NBX_ERR_CUDA;
+    if (rc == 0 && ctx->multipole) rc = nbx::alloc_quadrupoles(ctx);
     if (rc == 0) rc = nbx::walk_init(ctx);
     if (rc == 0) rc = nbx::radix_init(ctx);
     if (rc != 0) {
@@ -328,11 +352,34 @@ int nbx_set_constants(nbx_ctx *c, float theta_ref, float eps2, int compensated) 
     return NBX_OK;
 }
 
+int nbx_set_multipole(nbx_ctx *c, int multipole) {
+    if (!c || multipole < 0 || multipole > 1) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    if (multipole == 1 && ctx->walk_variant == 2) return NBX_ERR_ARG;
+    if (multipole == 1) {
+        const int rc = nbx::alloc_quadrupoles(ctx);
+        if (rc) return rc;
+    }
+    if (multipole != ctx->multipole) {
+        ctx->multipole = multipole;
+        ctx->p.multipole = multipole;
+        ctx->built = false;  // the next walk needs moments of this order
+        ctx->ref_m = 0;
+        ++ctx->graph_gen;
+        if (ctx->graph_exec) {
+            cudaGraphExecDestroy(ctx->graph_exec);
+            ctx->graph_exec = nullptr;
+        }
+    }
+    return NBX_OK;
+}
+
 int nbx_set_walk_config(nbx_ctx *c, int warps_per_block, int variant) {
     if (!c || !(warps_per_block == 4 || warps_per_block == 8 || warps_per_block == 16) ||
         !(variant >= 0 && variant <= 3))
         return NBX_ERR_ARG;
     Ctx *ctx = C(c);
+    if (variant == 2 && ctx->multipole) return NBX_ERR_ARG;
     ctx->walk_warps = warps_per_block;
     ctx->walk_variant = variant;
     ++ctx->graph_gen;
@@ -738,6 +785,10 @@ int nbx_adjoint_create(nbx_ctx *c, int nsteps, int checkpoint_every, int list_ca
     if (!c || !out) return NBX_ERR_ARG;
     Ctx *ctx = C(c);
     if (ctx->nsys < 1) return NBX_ERR_STATE;
+    if (ctx->multipole) {
+        ctx->last_error = "adjoint: the recorded walk is monopole-only (set multipole 0)";
+        return NBX_ERR_ARG;
+    }
     nbx::Adj *a = nullptr;
     int rc = nbx::adjoint_create(ctx, nsteps, checkpoint_every, list_capacity, tape_steps, &a);
     if (rc) {
@@ -759,6 +810,7 @@ int nbx_adjoint_destroy(nbx_adjoint *a) {
 int nbx_adjoint_forward(nbx_ctx *c, nbx_adjoint *a, const nbx_state *s, const float *tx, const float *ty,
                         const float *tz, double *loss, void *stream) {
     if (!c || !a || !s || !tx || !ty || !tz || !loss) return NBX_ERR_ARG;
+    if (C(c)->multipole) return NBX_ERR_ARG;  // the recorded walk is monopole-only
     int rc = nbx::adjoint_forward(C(c), reinterpret_cast<nbx::Adj *>(a), s, tx, ty, tz, loss, S(stream));
     if (rc) return rc;
     return nbx_sync_status(c, stream);
@@ -775,6 +827,7 @@ int nbx_adjoint_backward(nbx_ctx *c, nbx_adjoint *a, const nbx_state *s, float *
 
 int nbx_adjoint_record(nbx_ctx *c, nbx_adjoint *a, const nbx_state *s, void *stream) {
     if (!c || !a || !s) return NBX_ERR_ARG;
+    if (C(c)->multipole) return NBX_ERR_ARG;  // the recorded walk is monopole-only
     int rc = nbx::adjoint_record_all(C(c), reinterpret_cast<nbx::Adj *>(a), s, S(stream));
     if (rc) return rc;
     return nbx_sync_status(c, stream);

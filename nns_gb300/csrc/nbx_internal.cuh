@@ -59,6 +59,7 @@ struct Ctx {
     int walk_warps = 8;    // warps per block of the production walk
     int key_order = 0;     // 0 the reference's (Lebesgue) order, 1 Hilbert
     int radix_bits = 8;    // digit width of the body-key sort (8: 8 passes, 9: 7 passes)
+    int multipole = 0;     // 0 monopoles (the reference's force), 1 with cell quadrupoles
     std::string last_error;
 
     // capacity
@@ -107,6 +108,10 @@ struct Ctx {
     int *d_count = nullptr;                           // [NC]
     int *d_arrive = nullptr;                          // [NC]
     unsigned char *d_lvl8 = nullptr;                  // [NC] tree level of each node (root children: 1)
+    double2 *d_m2 = nullptr;       // [3 NC] quadrupole mode: FP64 second moments about the cell's centre of
+                                   // mass, (xx, yy) (zz, xy) (xz, yz)
+    float4 *d_quad4 = nullptr;     // [NC] quadrupole mode: traceless Q of cells in FP32, (xx, yy, zz, xy)
+    float2 *d_quad2 = nullptr;     // [NC]                                              (xz, yz)
     int *d_fcl = nullptr;                             // [NC+S+1] first-child list
     int *d_cl = nullptr;                              // [NC+S] cell list (BFS index)
 

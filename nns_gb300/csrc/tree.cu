@@ -413,17 +413,74 @@ __global__ void __launch_bounds__(kBlock) k_nodes_b(const unsigned *__restrict__
     }
 }
 
+// Quadrupole mode: the FP64 second moments of a cell about its centre of mass c,
+// composed from its children in child order -- M2 = sum over children of
+// [M2_child + m_child d d^T], d = c_child - c (a body child: M2 = 0, c_child =
+// its position) -- and the cell's traceless FP32 quadrupole Q = 3 M2 - tr(M2) I.
+// Every FP64 operation is rounded explicitly (no contraction), in the order of
+// the oracle's restatement, so both give the same bits.
+__device__ __forceinline__ void m2_add_point(double *a, double mc, double dx, double dy, double dz) {
+    a[0] = __dadd_rn(a[0], __dmul_rn(__dmul_rn(mc, dx), dx));
+    a[1] = __dadd_rn(a[1], __dmul_rn(__dmul_rn(mc, dy), dy));
+    a[2] = __dadd_rn(a[2], __dmul_rn(__dmul_rn(mc, dz), dz));
+    a[3] = __dadd_rn(a[3], __dmul_rn(__dmul_rn(mc, dx), dy));
+    a[4] = __dadd_rn(a[4], __dmul_rn(__dmul_rn(mc, dx), dz));
+    a[5] = __dadd_rn(a[5], __dmul_rn(__dmul_rn(mc, dy), dz));
+}
+
+// b: the cell; its children [first, first + nch); (cx, cy, cz) its FP64 centre of mass
+__device__ __forceinline__ void quad_cell(int b, int first, int nch, double cx, double cy, double cz,
+                                          const int *__restrict__ meta, const float4 *node4, const double4 *sums,
+                                          double2 *m2, float4 *quad4, float2 *quad2) {
+    double a[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int c = first; c < first + nch; c++) {
+        double mc, dx, dy, dz;
+        if (meta[c] < 0) {
+            const float4 q = node4[c];
+            mc = (double)q.w;
+            dx = __dsub_rn((double)q.x, cx);
+            dy = __dsub_rn((double)q.y, cy);
+            dz = __dsub_rn((double)q.z, cz);
+        } else {
+            const double2 *vp = reinterpret_cast<const double2 *>(&sums[c]);
+            const double2 v0 = __ldcg(vp), v1 = __ldcg(vp + 1);
+            mc = v0.x;
+            dx = __dsub_rn(__ddiv_rn(v0.y, mc), cx);
+            dy = __dsub_rn(__ddiv_rn(v1.x, mc), cy);
+            dz = __dsub_rn(__ddiv_rn(v1.y, mc), cz);
+            const double2 w0 = __ldcg(&m2[3 * (size_t)c]), w1 = __ldcg(&m2[3 * (size_t)c + 1]),
+                          w2 = __ldcg(&m2[3 * (size_t)c + 2]);
+            a[0] = __dadd_rn(a[0], w0.x);
+            a[1] = __dadd_rn(a[1], w0.y);
+            a[2] = __dadd_rn(a[2], w1.x);
+            a[3] = __dadd_rn(a[3], w1.y);
+            a[4] = __dadd_rn(a[4], w2.x);
+            a[5] = __dadd_rn(a[5], w2.y);
+        }
+        m2_add_point(a, mc, dx, dy, dz);
+    }
+    m2[3 * (size_t)b] = make_double2(a[0], a[1]);
+    m2[3 * (size_t)b + 1] = make_double2(a[2], a[3]);
+    m2[3 * (size_t)b + 2] = make_double2(a[4], a[5]);
+    const double tr = __dadd_rn(__dadd_rn(a[0], a[1]), a[2]);
+    quad4[b] = make_float4((float)__dsub_rn(__dmul_rn(3.0, a[0]), tr), (float)__dsub_rn(__dmul_rn(3.0, a[1]), tr),
+                           (float)__dsub_rn(__dmul_rn(3.0, a[2]), tr), (float)__dmul_rn(3.0, a[3]));
+    quad2[b] = make_float2((float)__dmul_rn(3.0, a[4]), (float)__dmul_rn(3.0, a[5]));
+}
+
 // Bottom-up FP64 moments, one BFS level per launch (deepest first): a cell sums
 // its children -- contiguous, one level below, already final -- in child order,
 // so the result is deterministic.  Level L occupies BFS indices
 // [start(L), start(L+1)); start(L) is the scanned count of level-sort digit 4L.
+template <bool Quad>
 __global__ void __launch_bounds__(kBlock) k_moments_level(int level, const unsigned *__restrict__ lvl_off,
                                                            int ntiles, const unsigned *__restrict__ totals,
                                                            const unsigned long long *__restrict__ totals64,
                                                            const unsigned long long *__restrict__ flags_ex,
                                                            const int *__restrict__ cl, int nsys,
                                                            const int *__restrict__ meta, float4 *node4,
-                                                           double4 *sums, int *count, const DevStatus *st) {
+                                                           double4 *sums, int *count, double2 *m2, float4 *quad4,
+                                                           float2 *quad2, const DevStatus *st) {
     if (st->code != 0) return;  // an inconsistent tree is never summed
     const unsigned T = totals[1];
     unsigned beg = lvl_off[(size_t)(level << 2) * ntiles];
@@ -464,6 +521,7 @@ __global__ void __launch_bounds__(kBlock) k_moments_level(int level, const unsig
         sums[b] = make_double4(sm, sx, sy, sz);
         count[b] = cnt;
         node4[b] = make_float4((float)(sx / sm), (float)(sy / sm), (float)(sz / sm), (float)sm);
+        if (Quad) quad_cell(b, first, nch, sx / sm, sy / sm, sz / sm, meta, node4, sums, m2, quad4, quad2);
     }
 }
 
@@ -486,8 +544,9 @@ __device__ __forceinline__ int arrive_acq_rel(int *p) {
 // A cell's sums from its children in child order.  Every child's body record
 // and cell sums are loaded at once and the child's kind picks one (a body's
 // sums entry is never read for its value), so the loads take one round trip.
+template <bool Quad>
 __device__ __forceinline__ void sum_cell(int b, int first, int nch, const int *__restrict__ meta, float4 *node4,
-                                         double4 *sums, int *count) {
+                                         double4 *sums, int *count, double2 *m2, float4 *quad4, float2 *quad2) {
     int mk[8], ck[8];
     float4 q[8];
     double2 v0[8], v1[8];
@@ -527,14 +586,16 @@ __device__ __forceinline__ void sum_cell(int b, int first, int nch, const int *_
     sums[b] = make_double4(sm, sx, sy, sz);
     count[b] = cnt;
     node4[b] = make_float4((float)(sx / sm), (float)(sy / sm), (float)(sz / sm), (float)sm);
+    if (Quad) quad_cell(b, first, nch, sx / sm, sy / sm, sz / sm, meta, node4, sums, m2, quad4, quad2);
 }
 
+template <bool Quad>
 __global__ void __launch_bounds__(kBlock) k_moments_up(const unsigned long long *__restrict__ totals64,
                                                        const int *__restrict__ cl, int nsys,
                                                        const int *__restrict__ parent,
                                                        const int *__restrict__ meta, float4 *node4,
-                                                       double4 *sums, int *count, int *counter,
-                                                       const DevStatus *st) {
+                                                       double4 *sums, int *count, int *counter, double2 *m2,
+                                                       float4 *quad4, float2 *quad2, const DevStatus *st) {
     if (st->code != 0) return;  // an inconsistent tree is never summed
     const int ncell = (int)(totals64[0] >> 32);
     for (int k = grid_stride_start(); k < ncell; k += grid_stride()) {
@@ -551,7 +612,7 @@ __global__ void __launch_bounds__(kBlock) k_moments_up(const unsigned long long 
         for (;;) {
             // the parent and its meta load while the sums do
             const int up = parent[b];
-            sum_cell(b, first, nch, meta, node4, sums, count);
+            sum_cell<Quad>(b, first, nch, meta, node4, sums, count, m2, quad4, quad2);
             if (up < 0) break;
             pm = meta[up];
             if (arrive_acq_rel(&counter[up]) != ((pm >> 28) & 7)) break;  // last of its children?
@@ -630,17 +691,22 @@ int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox
     // bottom-up launch (2^16: 0.37 against 0.55 ms per build); above, the
     // per-level launches stream the levels and are faster
     const int mode = ctx->p.moments_mode;
+    const bool quad = ctx->multipole != 0;
+    if (quad && !ctx->d_m2) return NBX_ERR_STATE;
     if (mode == 2 || (mode == 0 && n <= kMomentsUpMaxBodies)) {
-        k_moments_up<<<gn, kBlock, 0, st>>>(ctx->d_totals64, ctx->d_cl, S, ctx->d_parent, ctx->d_meta, ctx->d_node4,
-                                            ctx->d_sums, ctx->d_count, ctx->d_arrive, ctx->d_status);
+        auto kern = quad ? k_moments_up<true> : k_moments_up<false>;
+        kern<<<gn, kBlock, 0, st>>>(ctx->d_totals64, ctx->d_cl, S, ctx->d_parent, ctx->d_meta, ctx->d_node4,
+                                    ctx->d_sums, ctx->d_count, ctx->d_arrive, ctx->d_m2, ctx->d_quad4, ctx->d_quad2,
+                                    ctx->d_status);
         ++ctx->launches;
     } else {
         // cells exist at levels 1..41 (two bodies share at most 41 levels without error)
+        auto kern = quad ? k_moments_level<true> : k_moments_level<false>;
         for (int level = kMaxLevel - 2; level >= 1; level--) {
-            k_moments_level<<<ctx->nsm * 4, kBlock, 0, st>>>(level, ctx->d_hist, ctx->cap_tiles_node,
-                                                             ctx->d_totals, ctx->d_totals64, ctx->d_flags,
-                                                             ctx->d_cl, S, ctx->d_meta, ctx->d_node4, ctx->d_sums,
-                                                             ctx->d_count, ctx->d_status);
+            kern<<<ctx->nsm * 4, kBlock, 0, st>>>(level, ctx->d_hist, ctx->cap_tiles_node, ctx->d_totals,
+                                                  ctx->d_totals64, ctx->d_flags, ctx->d_cl, S, ctx->d_meta,
+                                                  ctx->d_node4, ctx->d_sums, ctx->d_count, ctx->d_m2, ctx->d_quad4,
+                                                  ctx->d_quad2, ctx->d_status);
             ++ctx->launches;
         }
     }

@@ -102,6 +102,29 @@ __device__ __forceinline__ void put4(ulonglong2 *a, ulonglong2 *b, int slot, flo
     pb[2 + h] = q.w;
 }
 
+// Quadrupole mode: the traceless quadrupoles of the cell buffer's slots, in
+// pairs: (xx, yy), (zz, xy), (xz, yz).
+template <int CB>
+struct QuadBuf {
+    static constexpr int kPairs = CB / 2;
+    ulonglong2 qa[kPairs];
+    ulonglong2 qb[kPairs];
+    ulonglong2 qc[kPairs];
+};
+
+__device__ __forceinline__ void putq(ulonglong2 *qa, ulonglong2 *qb, ulonglong2 *qc, int slot, float4 q4, float2 q2) {
+    float *pa = reinterpret_cast<float *>(&qa[slot >> 1]);
+    float *pb = reinterpret_cast<float *>(&qb[slot >> 1]);
+    float *pc = reinterpret_cast<float *>(&qc[slot >> 1]);
+    const int h = slot & 1;
+    pa[h] = q4.x;
+    pa[2 + h] = q4.y;
+    pb[h] = q4.z;
+    pb[2 + h] = q4.w;
+    pc[h] = q2.x;
+    pc[2 + h] = q2.y;
+}
+
 struct Sums {
     u64 x = 0ull, y = 0ull, z = 0ull, p = 0ull;  // packed partial sums (+0.0f, +0.0f)
     float kx = 0.f, ky = 0.f, kz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;  // Kahan totals
@@ -129,6 +152,29 @@ __device__ __forceinline__ void accumulate(Sums &a, u64 f, u64 mm, u64 ri, u64 d
     if (Pot) a.p = fma2(mm, ri, a.p);
 }
 
+// Accumulate F d + n q for two candidates: the quadrupole mode's contribution,
+// with F = m r^-3 + 5/2 (d.Q.d) r^-7 and n = -r^-5 (d = cell - body, q = Q d).
+template <int Mode>
+__device__ __forceinline__ void accumulate_quad(Sums &a, u64 F, u64 n5, u64 dx, u64 dy, u64 dz, u64 qx, u64 qy,
+                                                u64 qz) {
+    if (Mode == 2) {
+        float xa, xb, ya, yb, za, zb;
+        upk(fma2(F, dx, mul2(n5, qx)), xa, xb);
+        upk(fma2(F, dy, mul2(n5, qy)), ya, yb);
+        upk(fma2(F, dz, mul2(n5, qz)), za, zb);
+        kahan(a.kx, a.cx, xa);
+        kahan(a.kx, a.cx, xb);
+        kahan(a.ky, a.cy, ya);
+        kahan(a.ky, a.cy, yb);
+        kahan(a.kz, a.cz, za);
+        kahan(a.kz, a.cz, zb);
+    } else {
+        a.x = fma2(n5, qx, fma2(F, dx, a.x));
+        a.y = fma2(n5, qy, fma2(F, dy, a.y));
+        a.z = fma2(n5, qz, fma2(F, dz, a.z));
+    }
+}
+
 // CB = 64 and 96: 64-register budget (two 16-warp or four 8-warp blocks per SM);
 // CB = 128: up to 85 registers for more loads in flight (three 8-warp blocks).
 template <int CB>
@@ -137,10 +183,10 @@ struct WalkBounds {
     static constexpr int kMinBlocks = CB <= 96 ? NBX_WALK64_MINB : NBX_WALK128_MINB;
 };
 
-template <int CB, int Mode, bool Pot, bool Rec>
+template <int CB, int Mode, bool Pot, bool Rec, bool Quad = false>
 __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMinBlocks)
     k_walk2(const float4 *__restrict__ node4, const int *__restrict__ meta, const unsigned char *__restrict__ lvl8,
-            const float4 *__restrict__ body4,
+            const float4 *__restrict__ quad4, const float2 *__restrict__ quad2, const float4 *__restrict__ body4,
             const int *__restrict__ val, const int *__restrict__ groups, int ngroups,
             const int *__restrict__ body_sys, const int *__restrict__ sys_off, const float *__restrict__ depth0,
             const int *__restrict__ root_first, const int *__restrict__ root_nch, float eps2, int stack_cap,
@@ -153,7 +199,9 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int kCB = CB;
     WarpBuf<CB> &buf = reinterpret_cast<WarpBuf<CB> *>(smem_raw)[w];
-    int *stack = reinterpret_cast<int *>(smem_raw + sizeof(WarpBuf<CB>) * warps) + w * stack_cap;
+    constexpr size_t kQuadBytes = Quad ? sizeof(QuadBuf<CB>) : 0;
+    QuadBuf<CB> &qbuf = reinterpret_cast<QuadBuf<CB> *>(smem_raw + sizeof(WarpBuf<CB>) * warps)[w];
+    int *stack = reinterpret_cast<int *>(smem_raw + (sizeof(WarpBuf<CB>) + kQuadBytes) * warps) + w * stack_cap;
     const unsigned lt = (1u << lane) - 1u;
     const u64 eps2x2 = pk(eps2, eps2);
     unsigned long long tot_len = 0ull, tot_open = 0ull, tot_rounds = 0ull, tot_cand = 0ull;
@@ -321,6 +369,12 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 const int cm = ok ? meta[c] : 0;
                 const float4 q = ok ? node4[c] : make_float4(0.f, 0.f, 0.f, 0.f);
                 const bool isc = ok && cm >= 0;
+                float4 qq4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                float2 qq2 = make_float2(0.f, 0.f);
+                if (Quad && isc) {
+                    qq4 = quad4[c];
+                    qq2 = quad2[c];
+                }
                 bool sacc = false, srej = false;
                 {  // on every lane, without a branch; the results are masked by isc below
                     const float4 lo = buf.cls[0], hi = buf.cls[1];
@@ -342,8 +396,10 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                         srej = ra < dpc || rb < dpc;
                     }
                 }
-                const bool tob = ok && (cm < 0 || (isc && sacc));
-                const bool toc = isc && !sacc && !srej;
+                // quadrupole mode: accepted cells need their quadrupoles, so a surely
+                // accepted cell goes to the cell buffer with a threshold that always passes
+                const bool tob = ok && (cm < 0 || (!Quad && isc && sacc));
+                const bool toc = isc && (Quad ? (sacc || !srej) : (!sacc && !srej));
                 const bool tos = isc && !sacc && srej;
                 const unsigned bm = __ballot_sync(0xffffffffu, tob);
                 const unsigned cmk = __ballot_sync(0xffffffffu, toc);
@@ -355,8 +411,9 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 if (toc) {
                     const int slot = ncell + __popc(cmk & lt);
                     put4(buf.ca, buf.cb, slot, q);
-                    reinterpret_cast<float *>(&buf.cd[slot >> 1])[slot & 1] = dpc;
+                    reinterpret_cast<float *>(&buf.cd[slot >> 1])[slot & 1] = (Quad && sacc) ? -INFINITY : dpc;
                     buf.cid[slot] = c;
+                    if (Quad) putq(qbuf.qa, qbuf.qb, qbuf.qc, slot, qq4, qq2);
                 }
                 if (tos) stack[top + nsrej + __popc(smk & lt)] = c;
                 nbody += __popc(bm);
@@ -369,6 +426,8 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             if (lane == 1 && (ncell & 1)) {
                 put4(buf.ca, buf.cb, ncell, make_float4(1e18f, 1e18f, 1e18f, 0.f));
                 reinterpret_cast<float *>(&buf.cd[ncell >> 1])[1] = -INFINITY;
+                if (Quad)
+                    putq(qbuf.qa, qbuf.qb, qbuf.qc, ncell, make_float4(0.f, 0.f, 0.f, 0.f), make_float2(0.f, 0.f));
             }
             __syncwarp();
 
@@ -425,8 +484,25 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                     upk(B.y, ma, mb);
                     const u64 ri = pk(rsq(ra), rsq(rb));
                     const u64 mm = pk(oka ? ma : 0.f, okb ? mb : 0.f);
-                    const u64 f = mul2(mul2(mul2(mm, ri), ri), ri);
-                    accumulate<Mode, Pot>(acc, f, mm, ri, dx, dy, dz);
+                    if (!Quad) {
+                        const u64 f = mul2(mul2(mul2(mm, ri), ri), ri);
+                        accumulate<Mode, Pot>(acc, f, mm, ri, dx, dy, dz);
+                    } else {
+                        // a += m d r^-3 - Q d r^-5 + 5/2 (d.Q.d) d r^-7, the rejected
+                        // half of the pair masked through m and r^-5
+                        const ulonglong2 QA = qbuf.qa[q], QB = qbuf.qb[q], QC = qbuf.qc[q];
+                        const u64 ri2 = mul2(ri, ri);
+                        const u64 ri3 = mul2(ri2, ri);
+                        float r5a, r5b;
+                        upk(mul2(ri3, ri2), r5a, r5b);
+                        const u64 n5 = pk(oka ? -r5a : 0.f, okb ? -r5b : 0.f);
+                        const u64 qx = fma2(QC.x, dz, fma2(QB.y, dy, mul2(QA.x, dx)));
+                        const u64 qy = fma2(QC.y, dz, fma2(QA.y, dy, mul2(QB.y, dx)));
+                        const u64 qz = fma2(QB.x, dz, fma2(QC.y, dy, mul2(QC.x, dx)));
+                        const u64 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));
+                        const u64 F = fma2(mul2(dqd, mul2(n5, ri2)), pk(-2.5f, -2.5f), mul2(mm, ri3));
+                        accumulate_quad<Mode>(acc, F, n5, dx, dy, dz, qx, qy, qz);
+                    }
                 }
                 if (!oka) {
                     if (lane == 0) stack[top + nrej] = buf.cid[2 * q];
@@ -510,24 +586,26 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
     }
 }
 
-template <int CB, int Mode, bool Pot, bool Rec = false>
+template <int CB, int Mode, bool Pot, bool Rec = false, bool Quad = false>
 int launch(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st, int *rec_list = nullptr,
            int *rec_len = nullptr, int rec_cap = 0) {
     const int cap = ctx->p.stack_depth;
-    const size_t smem = (size_t)warps * (sizeof(WarpBuf<CB>) + (size_t)cap * sizeof(int));
+    const size_t smem = (size_t)warps * (sizeof(WarpBuf<CB>) + (Quad ? sizeof(QuadBuf<CB>) : 0) +
+                                         (size_t)cap * sizeof(int));
     if (smem > (size_t)ctx->smem_optin) {
         ctx->last_error = "walk: stack_depth too large for the launch shape's shared memory";
         return NBX_ERR_ARG;
     }
     const int blocks_needed = ceil_div(ctx->ngroups, warps);
     int per_sm = 1;
-    NBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk2<CB, Mode, Pot, Rec>, warps * 32, smem));
+    NBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk2<CB, Mode, Pot, Rec, Quad>, warps * 32,
+                                                           smem));
     if (per_sm < 1) per_sm = 1;
     const int grid = blocks_needed < ctx->nsm * per_sm ? blocks_needed : ctx->nsm * per_sm;
     if (grid <= 0) return NBX_OK;
     NBX_CUDA(cudaMemsetAsync(&ctx->d_status->walk_next, 0, sizeof(unsigned), st));
-    k_walk2<CB, Mode, Pot, Rec><<<grid, warps * 32, smem, st>>>(
-        ctx->d_node4, ctx->d_meta, ctx->d_lvl8, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
+    k_walk2<CB, Mode, Pot, Rec, Quad><<<grid, warps * 32, smem, st>>>(
+        ctx->d_node4, ctx->d_meta, ctx->d_lvl8, ctx->d_quad4, ctx->d_quad2, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
         ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay, s->az,
         pot, ctx->d_gstat, ctx->d_status, rec_list, rec_len, rec_cap);
     ++ctx->launches;
@@ -535,15 +613,24 @@ int launch(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st,
     return NBX_OK;
 }
 
-template <int CB, int Mode, bool Pot, bool Rec = false>
+template <int CB, int Mode, bool Pot, bool Rec = false, bool Quad = false>
 int set_attr(Ctx *ctx, int smem_max) {
-    NBX_CUDA(cudaFuncSetAttribute(k_walk2<CB, Mode, Pot, Rec>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
+    NBX_CUDA(cudaFuncSetAttribute(k_walk2<CB, Mode, Pot, Rec, Quad>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  smem_max));
     return NBX_OK;
 }
 
 template <int CB>
 int forces_cb(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st) {
     if (pot) return launch<CB, 0, true>(ctx, s, pot, warps, st);
+    if (ctx->multipole) {
+        if (!ctx->d_quad4) return NBX_ERR_STATE;
+        switch (ctx->compensated) {
+            case 1: return launch<CB, 1, false, false, true>(ctx, s, nullptr, warps, st);
+            case 2: return launch<CB, 2, false, false, true>(ctx, s, nullptr, warps, st);
+            default: return launch<CB, 0, false, false, true>(ctx, s, nullptr, warps, st);
+        }
+    }
     switch (ctx->compensated) {
         case 1: return launch<CB, 1, false>(ctx, s, nullptr, warps, st);
         case 2: return launch<CB, 2, false>(ctx, s, nullptr, warps, st);
@@ -569,6 +656,15 @@ int walk2_init(Ctx *ctx) {
     rc |= set_attr<96, 2, false>(ctx, smem_optin);
     rc |= set_attr<96, 0, true>(ctx, smem_optin);
     rc |= set_attr<96, 0, false, true>(ctx, smem_optin);
+    rc |= set_attr<64, 0, false, false, true>(ctx, smem_optin);
+    rc |= set_attr<64, 1, false, false, true>(ctx, smem_optin);
+    rc |= set_attr<64, 2, false, false, true>(ctx, smem_optin);
+    rc |= set_attr<128, 0, false, false, true>(ctx, smem_optin);
+    rc |= set_attr<128, 1, false, false, true>(ctx, smem_optin);
+    rc |= set_attr<128, 2, false, false, true>(ctx, smem_optin);
+    rc |= set_attr<96, 0, false, false, true>(ctx, smem_optin);
+    rc |= set_attr<96, 1, false, false, true>(ctx, smem_optin);
+    rc |= set_attr<96, 2, false, false, true>(ctx, smem_optin);
     return rc;
 }
 

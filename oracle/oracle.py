@@ -40,7 +40,9 @@ def lib():
                                  _i32p, _f32p, _f32p, _f32p, _f32p, C.c_float, C.c_float, C.c_int,
                                  C.c_void_p, C.c_int, _f32p, _f32p, _f32p, _f64p, _f64p, _f64p,
                                  _i32p, _i32p]
+        L.orc_forces.argtypes = L.orc_forces.argtypes + [C.c_void_p]
         L.orc_forces.restype = C.c_longlong
+        L.orc_quad.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, _i32p, _f64p, _f64p, _f64p]
         L.orc_update.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p,
                                  _f32p, C.c_float, C.c_float]
         L.orc_direct_fp64.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_double, C.c_int,
@@ -220,7 +222,26 @@ class Forces:
     total: int           # sum over evaluated bodies of the list length
 
 
-def forces(x, y, z, m, tree: Tree, theta_ref, eps2, group=32, groups=None, depth0_value=None):
+def quadrupoles(x, y, z, m, tree: Tree):
+    """Traceless FP64 quadrupole moments of the tree's cells about their FP64
+    centres of mass, (ncells, 6) as (xx, yy, zz, xy, xz, yz) (orc_quad; the
+    reference has monopoles only)."""
+    k = tree.ncells
+    q = np.zeros(6 * max(k, 1))
+    cc = np.ascontiguousarray(tree.cell_child.reshape(-1), np.int32)
+    if k == 0:
+        return q[:0].reshape(0, 6)
+    rc = lib().orc_quad(len(x), _f32(x), _f32(y), _f32(z), _f32(m), k, cc,
+                        np.ascontiguousarray(tree.cell_m64), np.ascontiguousarray(tree.cell_com64.reshape(-1)), q)
+    if rc:
+        raise OracleError(rc, "orc_quad")
+    return q.reshape(k, 6)
+
+
+def forces(x, y, z, m, tree: Tree, theta_ref, eps2, group=32, groups=None, depth0_value=None, quad=None):
+    """The warp-coherent walk (FP32 and an FP64 evaluation of the same lists).
+    ``quad``: per-cell quadrupoles (quadrupoles()) added to the FP64 evaluation
+    of accepted cells; the lists do not depend on it."""
     n = len(x)
     x, y, z, m = _f32(x), _f32(y), _f32(z), _f32(m)
     d0 = depth0(tree.bbox, theta_ref) if depth0_value is None else depth0_value
@@ -241,7 +262,8 @@ def forces(x, y, z, m, tree: Tree, theta_ref, eps2, group=32, groups=None, depth
     tot = lib().orc_forces(n, x, y, z, m, np.ascontiguousarray(tree.perm, np.int32), tree.ncells,
                            np.ascontiguousarray(tree.root_child, np.int32), cc,
                            _f32(cxa), _f32(cya), _f32(cza), _f32(cma), C.c_float(d0),
-                           C.c_float(eps2), group, gptr, ng, ax, ay, az, gx, gy, gz, nl, no)
+                           C.c_float(eps2), group, gptr, ng, ax, ay, az, gx, gy, gz, nl, no,
+                           None if quad is None else np.ascontiguousarray(quad, np.float64).ctypes.data_as(C.c_void_p))
     if tot < 0:
         raise ValueError("orc_forces failed")
     return Forces(np.stack([ax, ay, az], 1), np.stack([gx, gy, gz], 1), nl, no, int(tot))

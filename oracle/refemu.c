@@ -285,6 +285,51 @@ float orc_depth0(const float *bb, float theta_ref)
     return (radius * radius) / theta_ref;
 }
 
+/* Traceless quadrupole moments of the canonical cells (an extension: the
+ * reference's kernels carry monopoles only).  Per cell, about its FP64 centre
+ * of mass c: M2 = sum over children in child order of [M2_child +
+ * m_child (c_child - c)(c_child - c)^T] (a body child has M2 = 0 and c_child
+ * = its position), all in FP64; Q = 3 M2 - tr(M2) I, stored per cell as
+ * (xx, yy, zz, xy, xz, yz).  Cells are in depth-first pre-order, so every
+ * child cell has a larger index than its parent and a reverse sweep composes
+ * each cell from finished children. */
+int orc_quad(int n, const float *x, const float *y, const float *z, const float *m, int ncells,
+             const int *cell_child, const double *cell_m64, const double *cell_com64, double *q)
+{
+    double *m2 = (double *)malloc(sizeof(double) * 6 * (size_t)(ncells > 0 ? ncells : 1));
+    if (!m2) return ORC_ERR_CAPACITY;
+    for (int k = ncells - 1; k >= 0; k--) {
+        const double cx = cell_com64[3 * k], cy = cell_com64[3 * k + 1], cz = cell_com64[3 * k + 2];
+        double a[6] = {0, 0, 0, 0, 0, 0};
+        for (int s = 0; s < 8; s++) {
+            int ch = cell_child[8 * k + s];
+            if (ch < 0) continue;
+            double mc, dx, dy, dz;
+            if (ch < n) {
+                mc = (double)m[ch];
+                dx = (double)x[ch] - cx; dy = (double)y[ch] - cy; dz = (double)z[ch] - cz;
+            } else {
+                int j = ch - n;
+                mc = cell_m64[j];
+                dx = cell_com64[3 * j] - cx; dy = cell_com64[3 * j + 1] - cy; dz = cell_com64[3 * j + 2] - cz;
+                for (int t = 0; t < 6; t++) a[t] += m2[6 * j + t];
+            }
+            a[0] += mc * dx * dx; a[1] += mc * dy * dy; a[2] += mc * dz * dz;
+            a[3] += mc * dx * dy; a[4] += mc * dx * dz; a[5] += mc * dy * dz;
+        }
+        for (int t = 0; t < 6; t++) m2[6 * k + t] = a[t];
+        const double tr = a[0] + a[1] + a[2];
+        q[6 * k + 0] = 3.0 * a[0] - tr;
+        q[6 * k + 1] = 3.0 * a[1] - tr;
+        q[6 * k + 2] = 3.0 * a[2] - tr;
+        q[6 * k + 3] = 3.0 * a[3];
+        q[6 * k + 4] = 3.0 * a[4];
+        q[6 * k + 5] = 3.0 * a[5];
+    }
+    free(m2);
+    return ORC_OK;
+}
+
 /* ------------------------------------------------------------------ force */
 static inline float mac_r(float dx, float dy, float dz, float eps2)
 {
@@ -302,7 +347,8 @@ long long orc_forces(int n, const float *x, const float *y, const float *z, cons
                      const float *cell_m, float depth0, float eps2, int group,
                      const int *groups, int ngroups,
                      float *ax, float *ay, float *az,
-                     double *ax64, double *ay64, double *az64, int *nlist, int *nopen)
+                     double *ax64, double *ay64, double *az64, int *nlist, int *nopen,
+                     const double *cell_q)
 {
     (void)ncells;
     if (group < 1 || group > 1024) return -1;
@@ -332,8 +378,9 @@ long long orc_forces(int n, const float *x, const float *y, const float *z, cons
         else { int k_ = (ch) - n; cx = cell_x[k_]; cy = cell_y[k_]; cz = cell_z[k_];  \
                cm = cell_m[k_]; }                                                     \
     } while (0)
-#define INTERACT(cx, cy, cz, cm)                                                      \
+#define INTERACT(cx, cy, cz, cm, ch)                                                  \
     do {                                                                              \
+        const double *q_ = (cell_q && (ch) >= n) ? cell_q + 6 * (size_t)((ch) - n) : 0; \
         for (int l = 0; l < L; l++) {                                                 \
             float dx = cx - px[l], dy = cy - py[l], dz = cz - pz[l];                  \
             float r = mac_r(dx, dy, dz, eps2);                                        \
@@ -345,7 +392,19 @@ long long orc_forces(int n, const float *x, const float *y, const float *z, cons
                    ddz = (double)cz - (double)pz[l];                                  \
             double rr = ddx * ddx + ddy * ddy + ddz * ddz + (double)eps2;             \
             double f64 = (double)cm / (rr * sqrt(rr));                                \
-            gx[l] += f64 * ddx; gy[l] += f64 * ddy; gz[l] += f64 * ddz;               \
+            if (q_) {                                                                 \
+                /* a += -Q d / r^5 + 5/2 (d.Q.d) d / r^7, d = cell - body */          \
+                double qx = q_[0] * ddx + q_[3] * ddy + q_[4] * ddz;                  \
+                double qy = q_[3] * ddx + q_[1] * ddy + q_[5] * ddz;                  \
+                double qz = q_[4] * ddx + q_[5] * ddy + q_[2] * ddz;                  \
+                double r5 = 1.0 / (rr * rr * sqrt(rr));                               \
+                double c = 2.5 * (ddx * qx + ddy * qy + ddz * qz) * r5 / rr;          \
+                gx[l] += (f64 + c) * ddx - r5 * qx;                                   \
+                gy[l] += (f64 + c) * ddy - r5 * qy;                                   \
+                gz[l] += (f64 + c) * ddz - r5 * qz;                                   \
+            } else {                                                                  \
+                gx[l] += f64 * ddx; gy[l] += f64 * ddy; gz[l] += f64 * ddz;           \
+            }                                                                         \
         }                                                                             \
         len++;                                                                        \
     } while (0)
@@ -355,7 +414,7 @@ long long orc_forces(int n, const float *x, const float *y, const float *z, cons
             if (ch < n) {
                 float cx, cy, cz, cm;
                 NODE_POS(ch, cx, cy, cz, cm);
-                INTERACT(cx, cy, cz, cm);
+                INTERACT(cx, cy, cz, cm, ch);
             } else {
                 stack[top].node = ch; stack[top].dp = depth0; top++;
                 opened++;
@@ -378,7 +437,7 @@ long long orc_forces(int n, const float *x, const float *y, const float *z, cons
                     }
                 }
                 if (accept) {
-                    INTERACT(cx, cy, cz, cm);
+                    INTERACT(cx, cy, cz, cm, ch);
                 } else {
                     if (top == cap) {
                         cap *= 2;

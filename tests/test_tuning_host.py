@@ -118,8 +118,9 @@ def test_digit_width_gives_the_same_stable_order():
 
 
 def test_cache_key_separates_orders_and_moment_passes(monkeypatch):
-    """Hilbert and Lebesgue order (and the centre-of-mass pass) change the tree and
-    the walk's cost, so a tuning result for one is never reused for another."""
+    """Hilbert and Lebesgue order, the centre-of-mass pass and the multipole order
+    change the tree or the walk's cost, so a tuning result for one is never
+    reused for another."""
     from types import SimpleNamespace
 
     from nns_gb300 import autotune
@@ -128,6 +129,7 @@ def test_cache_key_separates_orders_and_moment_passes(monkeypatch):
     for order in (0, 1):
         for moments in (0, 1, 2):
             for comp in (0, 1):
-                p = SimpleNamespace(compensated=comp, key_order=order, moments_mode=moments)
-                keys.add(autotune._key(SimpleNamespace(device=0, offsets=[0, 100], params=p), 100))
-    assert len(keys) == 12
+                for mp in (0, 1):
+                    p = SimpleNamespace(compensated=comp, key_order=order, moments_mode=moments, multipole=mp)
+                    keys.add(autotune._key(SimpleNamespace(device=0, offsets=[0, 100], params=p), 100))
+    assert len(keys) == 24
