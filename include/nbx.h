@@ -64,7 +64,11 @@ typedef struct nbx_params {
                           one walk block must fit its shared memory (NBX_ERR_ARG otherwise) */
     int compensated;   /* 0 plain FP32; 1 split compensation (FP32 partial sums per
                           walk round, Kahan across rounds); 2 Kahan on every term */
-    int leaf_size;     /* bodies per leaf: 1 */
+    int leaf_size;     /* bodies per leaf: 1, the reference's tree (Kernels.cu:284-362; the parity
+                          mode); 2..8: every cell holding at most leaf_size bodies whose parent
+                          holds more is a leaf with its bodies as children (fewer cells, longer
+                          lists; trees and lists differ from the reference's, nbx_export_tree
+                          refuses them).  Not available with the adjoint */
     int radix_bits;    /* radix digit width of the key sort: 8 (8 passes) or 9 (7 passes) */
     int walk_warps;    /* warps per block of the walk kernel (0 = autotuned default) */
     int device;        /* CUDA device ordinal */
@@ -135,6 +139,9 @@ int nbx_set_tuning(nbx_ctx *ctx, int radix_bits, int stack_depth);
  * on first use (NBX_ERR_NOMEM if that fails).  No counterpart in the
  * reference, whose kernels carry monopoles only. */
 int nbx_set_multipole(nbx_ctx *ctx, int multipole);
+/* Bodies per leaf bucket (nbx_params.leaf_size, 1..8); the context needs a new
+ * build before its next walk.  Used by the autotuner outside the parity mode. */
+int nbx_set_leaf_size(nbx_ctx *ctx, int leaf_size);
 
 /* ---- reference-compatible phase entry points (KernelsWrapper.cu) ---- */
 /* KernelsWrapper::resetArrays (KernelsWrapper.cu:28; Kernels.cu:21-64) */
@@ -274,12 +281,13 @@ int nbx_diagnostics_fp64(nbx_ctx *ctx, const nbx_state *s, int n, double *out, v
  * The reference has none (it only writes frames).  A checkpoint is a raw dump
  * of every system's bodies (x, y, z, vx, vy, vz, m: the state a kick-drift step
  * needs) plus the system offsets, the step's constants (MAC constant,
- * softening, dt, dampening, compensation, key order) and the walk's launch
- * shape and buffer variant (which fix the order of the force sums), into a
- * caller-owned host buffer: a versioned header (64 bytes), the offsets, the
+ * softening, dt, dampening, compensation, key order), the walk's launch
+ * shape and buffer variant (which fix the order of the force sums), the
+ * multipole order and the leaf bucket size, into a caller-owned host buffer: a
+ * versioned header (72 bytes), the offsets, the
  * seven float arrays, and 64-bit checksums of header and payload.  Restoring
- * it into a context (capacity permitting) sets the systems, constants and walk
- * configuration and copies the bodies into the caller's device state, so that
+ * it into a context (capacity permitting) sets the systems, constants, walk
+ * configuration, multipole order and leaf size and copies the bodies into the caller's device state, so that
  * the run continues bit for bit.  The sort's digit width and the stack depth
  * change no result and are not recorded. */
 int64_t nbx_checkpoint_bytes(int64_t nbodies, int nsystems);

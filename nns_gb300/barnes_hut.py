@@ -40,13 +40,15 @@ class Context:
     ``key_order`` 1 orders bodies along the Hilbert curve (faster walk; lists
     differ from the reference's); ``moments_mode`` picks the centre-of-mass pass
     (0 by size, 1 per tree level, 2 one launch), all with the same sums;
-    ``radix_bits`` 8 or 9 sorts the keys in 8 or 7 passes, to the same order."""
+    ``radix_bits`` 8 or 9 sorts the keys in 8 or 7 passes, to the same order;
+    ``multipole`` 1 adds cell quadrupoles to the force and ``leaf_size`` 2..8 makes
+    cells of at most that many bodies leaves (both outside the parity mode)."""
 
     def __init__(self, max_bodies: int, max_systems: int = 1, theta: float = 0.5,
                  theta_ref: float | None = None, eps: float = 0.05, eps2: float | None = None,
                  dt: float = 1e-3, dampening: float = 1.0, compensated: int = 0,
                  stack_depth: int = 512, device: int = 0, key_order: int = 0, node_capacity: int = 0,
-                 moments_mode: int = 0, radix_bits: int = 8, multipole: int = 0):
+                 moments_mode: int = 0, radix_bits: int = 8, multipole: int = 0, leaf_size: int = 1):
         p = L.nbx_params()
         lib().nbx_params_default(C.byref(p))
         p.max_bodies = int(max_bodies)
@@ -65,6 +67,7 @@ class Context:
         p.device = device
         p.key_order = int(key_order)
         p.multipole = int(multipole)
+        p.leaf_size = int(leaf_size)
         self.params = p
         h = C.c_void_p()
         check(lib().nbx_create(C.byref(p), C.byref(h)), "nbx_create")
@@ -112,6 +115,12 @@ class Context:
         walk needs a new build."""
         check(lib().nbx_set_multipole(self.h, int(multipole)), "nbx_set_multipole", self.h)
         self.params.multipole = int(multipole)
+
+    def set_leaf_size(self, leaf_size: int):
+        """Bodies per leaf bucket, 1 (the reference's tree) to 8; the next walk
+        needs a new build."""
+        check(lib().nbx_set_leaf_size(self.h, int(leaf_size)), "nbx_set_leaf_size", self.h)
+        self.params.leaf_size = int(leaf_size)
 
     def set_systems(self, offsets):
         off = np.ascontiguousarray(offsets, dtype=np.int64)
@@ -245,7 +254,7 @@ class Context:
         check(lib().nbx_checkpoint_restore(self.h, C.byref(s.c), b.ctypes.data_as(C.c_void_p), b.size,
                                            _stream_ptr(stream)), "nbx_checkpoint_restore", self.h)
         nsys = int(np.frombuffer(b[12:16].tobytes(), np.int32)[0])
-        self.offsets = [int(v) for v in np.frombuffer(b[64:64 + 8 * (nsys + 1)].tobytes(), np.int64)]
+        self.offsets = [int(v) for v in np.frombuffer(b[72:72 + 8 * (nsys + 1)].tobytes(), np.int64)]
 
     def diagnostics(self, s: "State", n: int | None = None, stream=None):
         out = torch.zeros(8, dtype=torch.float64, device=self.device)

@@ -95,7 +95,7 @@ void free_all(Ctx *ctx) {
     void *ptrs[] = {ctx->d_sys_off, ctx->d_body_sys, ctx->d_tiles, ctx->d_sys_tiles, ctx->d_groups,
                     ctx->d_bbox_u, ctx->d_bbox, ctx->d_bbox64, ctx->d_depth0, ctx->d_root_first,
                     ctx->d_root_nch, ctx->d_key, ctx->d_key_alt, ctx->d_key_lo, ctx->d_val, ctx->d_val_alt,
-                    ctx->d_body4, ctx->d_delta, ctx->d_ecount, ctx->d_body_node, ctx->d_gstat,
+                    ctx->d_body4, ctx->d_delta, ctx->d_bucket, ctx->d_ecount, ctx->d_body_node, ctx->d_gstat,
                     ctx->d_ent, ctx->d_ent_alt, ctx->d_flags, ctx->d_node4, ctx->d_meta, ctx->d_parent,
                     ctx->d_sums, ctx->d_count, ctx->d_arrive, ctx->d_lvl8, ctx->d_fcl, ctx->d_cl, ctx->d_hist,
                     ctx->d_scan_blk, ctx->d_totals, ctx->d_totals64, ctx->d_status, ctx->d_m2, ctx->d_quad4,
@@ -220,7 +220,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     if (!p || !out) return NBX_ERR_ARG;
     *out = nullptr;
     if (p->max_bodies < 1 || p->max_bodies > (1 << 26) || p->max_systems < 1 ||
-        p->max_systems > p->max_bodies || p->group != 32 || p->leaf_size != 1 || (p->radix_bits != 8 && p->radix_bits != 9) ||
+        p->max_systems > p->max_bodies || p->group != 32 || p->leaf_size < 1 || p->leaf_size > 8 || (p->radix_bits != 8 && p->radix_bits != 9) ||
         p->stack_depth < 360 || p->stack_depth > 4096 || p->walk_variant < 0 || p->walk_variant > 3 ||
         p->moments_mode < 0 || p->moments_mode > 2 || p->multipole < 0 || p->multipole > 1 ||
         (p->multipole == 1 && p->walk_variant == 2) ||
@@ -236,6 +236,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     ctx->key_order = p->key_order;
     ctx->radix_bits = p->radix_bits;
     ctx->multipole = p->multipole;
+    ctx->leaf_size = p->leaf_size;
     if (p->key_order < 0 || p->key_order > 1) {
         delete ctx;
         return NBX_ERR_ARG;
@@ -286,6 +287,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     rc |= nbx::dmalloc(ctx, &ctx->d_val_alt, B);
     rc |= nbx::dmalloc(ctx, &ctx->d_body4, B);
     rc |= nbx::dmalloc(ctx, &ctx->d_delta, B);
+    rc |= nbx::dmalloc(ctx, &ctx->d_bucket, B);
     rc |= nbx::dmalloc(ctx, &ctx->d_ecount, B);
     rc |= nbx::dmalloc(ctx, &ctx->d_body_node, B);
     rc |= nbx::dmalloc(ctx, &ctx->d_gstat, G);
@@ -364,6 +366,23 @@ int nbx_set_multipole(nbx_ctx *c, int multipole) {
         ctx->multipole = multipole;
         ctx->p.multipole = multipole;
         ctx->built = false;  // the next walk needs moments of this order
+        ctx->ref_m = 0;
+        ++ctx->graph_gen;
+        if (ctx->graph_exec) {
+            cudaGraphExecDestroy(ctx->graph_exec);
+            ctx->graph_exec = nullptr;
+        }
+    }
+    return NBX_OK;
+}
+
+int nbx_set_leaf_size(nbx_ctx *c, int leaf_size) {
+    if (!c || leaf_size < 1 || leaf_size > 8) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    if (leaf_size != ctx->leaf_size) {
+        ctx->leaf_size = leaf_size;
+        ctx->p.leaf_size = leaf_size;
+        ctx->built = false;  // the next walk needs a tree with these leaves
         ctx->ref_m = 0;
         ++ctx->graph_gen;
         if (ctx->graph_exec) {
@@ -785,8 +804,8 @@ int nbx_adjoint_create(nbx_ctx *c, int nsteps, int checkpoint_every, int list_ca
     if (!c || !out) return NBX_ERR_ARG;
     Ctx *ctx = C(c);
     if (ctx->nsys < 1) return NBX_ERR_STATE;
-    if (ctx->multipole) {
-        ctx->last_error = "adjoint: the recorded walk is monopole-only (set multipole 0)";
+    if (ctx->multipole || ctx->leaf_size != 1) {
+        ctx->last_error = "adjoint: needs monopoles and one body per leaf (multipole 0, leaf_size 1)";
         return NBX_ERR_ARG;
     }
     nbx::Adj *a = nullptr;
@@ -810,7 +829,7 @@ int nbx_adjoint_destroy(nbx_adjoint *a) {
 int nbx_adjoint_forward(nbx_ctx *c, nbx_adjoint *a, const nbx_state *s, const float *tx, const float *ty,
                         const float *tz, double *loss, void *stream) {
     if (!c || !a || !s || !tx || !ty || !tz || !loss) return NBX_ERR_ARG;
-    if (C(c)->multipole) return NBX_ERR_ARG;  // the recorded walk is monopole-only
+    if (C(c)->multipole || C(c)->leaf_size != 1) return NBX_ERR_ARG;  // monopoles, one body per leaf
     int rc = nbx::adjoint_forward(C(c), reinterpret_cast<nbx::Adj *>(a), s, tx, ty, tz, loss, S(stream));
     if (rc) return rc;
     return nbx_sync_status(c, stream);
@@ -827,7 +846,7 @@ int nbx_adjoint_backward(nbx_ctx *c, nbx_adjoint *a, const nbx_state *s, float *
 
 int nbx_adjoint_record(nbx_ctx *c, nbx_adjoint *a, const nbx_state *s, void *stream) {
     if (!c || !a || !s) return NBX_ERR_ARG;
-    if (C(c)->multipole) return NBX_ERR_ARG;  // the recorded walk is monopole-only
+    if (C(c)->multipole || C(c)->leaf_size != 1) return NBX_ERR_ARG;  // monopoles, one body per leaf
     int rc = nbx::adjoint_record_all(C(c), reinterpret_cast<nbx::Adj *>(a), s, S(stream));
     if (rc) return rc;
     return nbx_sync_status(c, stream);

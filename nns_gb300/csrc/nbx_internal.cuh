@@ -60,6 +60,7 @@ struct Ctx {
     int key_order = 0;     // 0 the reference's (Lebesgue) order, 1 Hilbert
     int radix_bits = 8;    // digit width of the body-key sort (8: 8 passes, 9: 7 passes)
     int multipole = 0;     // 0 monopoles (the reference's force), 1 with cell quadrupoles
+    int leaf_size = 1;     // bodies per leaf bucket: 1 the reference's tree, 2..8 bucket leaves
     std::string last_error;
 
     // capacity
@@ -94,6 +95,7 @@ struct Ctx {
     int *d_val = nullptr, *d_val_alt = nullptr;                 // [B] permutation
     float4 *d_body4 = nullptr;   // [B] sorted bodies (x,y,z,m)
     unsigned char *d_delta = nullptr;  // [B]
+    unsigned char *d_bucket = nullptr; // [B] leaf buckets: level of the bucket cell of each sorted position
     unsigned *d_ecount = nullptr;      // [B] entries per position -> exclusive offsets
     int *d_body_node = nullptr;        // [B] node of sorted position
     int2 *d_gstat = nullptr;           // [G] per walk group: list length, opened cells (last walk)

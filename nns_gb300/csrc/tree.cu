@@ -276,18 +276,53 @@ __global__ void __launch_bounds__(kBlock) k_delta(const float4 *__restrict__ pos
     if ((threadIdx.x & 31) == 0 && lvl_max > 0) atomicMax(&st->max_level, lvl_max);
 }
 
-__device__ __forceinline__ void levels_of(const unsigned char *delta, int p, int beg, int &lo, int &hi,
-                                          int &dp) {
+// Node levels owned by sorted position p: the cells starting at p (levels
+// lo..hi-1) and the body (level hi).  With leaf buckets (bucket != nullptr) the
+// body hangs directly below its bucket cell (level bucket[p]): deeper cells
+// are dropped and the body's level is at most bucket[p] + 1.
+__device__ __forceinline__ void levels_of(const unsigned char *delta, const unsigned char *bucket, int p, int beg,
+                                          int &lo, int &hi, int &dp) {
     dp = p > beg ? (int)delta[p - 1] : 0;
     const int di = delta[p];
     lo = dp + 1;
     hi = max(dp, di) + 1;
+    if (bucket) {
+        hi = min(hi, (int)bucket[p] + 1);
+        lo = min(lo, hi);
+    }
+}
+
+// Leaf buckets (nbx_params.leaf_size k > 1; not the reference's tree, which has
+// one body per leaf): the bucket of a body is the shallowest cell around it
+// holding at most k bodies.  The cell at level L around p holds more than k
+// bodies exactly when some window of k+1 consecutive positions of the system
+// containing p shares at least L levels, i.e. all k deltas inside the window
+// are >= L; so the bucket level is 1 + the largest inner-delta minimum over
+// those windows.  Rewrites the node entries per position accordingly.
+__global__ void __launch_bounds__(kBlock) k_bucket(const int *__restrict__ body_sys, const int *__restrict__ sys_off,
+                                                    int n, int k, const unsigned char *__restrict__ delta,
+                                                    unsigned char *__restrict__ bucket, unsigned *__restrict__ ecount) {
+    for (int p = grid_stride_start(); p < n; p += grid_stride()) {
+        const int s = body_sys[p];
+        const int beg = sys_off[s], end = sys_off[s + 1];
+        int best = 0;
+        for (int a = max(p - k, beg); a <= p && a + k <= end - 1; a++) {
+            int mn = 255;
+            for (int j = a; j < a + k; j++) mn = min(mn, (int)delta[j]);
+            best = max(best, mn);
+        }
+        bucket[p] = (unsigned char)(best + 1);
+        int lo, hi, dp;
+        levels_of(delta, bucket, p, beg, lo, hi, dp);
+        ecount[p] = (unsigned)(hi - lo + 1);
+    }
 }
 
 // Node entries (level << 26 | position) in position order = depth-first pre-order.
 __global__ void __launch_bounds__(kBlock) k_entries(const int *__restrict__ body_sys,
                                                      const int *__restrict__ sys_off, int n,
                                                      const unsigned char *__restrict__ delta,
+                                                     const unsigned char *__restrict__ bucket,
                                                      const unsigned *__restrict__ eoff, unsigned *totals,
                                                      int cap_nodes, unsigned *__restrict__ ent,
                                                      DevStatus *st) {
@@ -302,7 +337,7 @@ __global__ void __launch_bounds__(kBlock) k_entries(const int *__restrict__ body
     for (int p = grid_stride_start(); p < n; p += grid_stride()) {
         const int beg = sys_off[body_sys[p]];
         int lo, hi, dp;
-        levels_of(delta, p, beg, lo, hi, dp);
+        levels_of(delta, bucket, p, beg, lo, hi, dp);
         const unsigned e = eoff[p];
         if (e + (unsigned)(hi - lo + 1) > (unsigned)cap_nodes) continue;
         for (int l = lo; l <= hi; l++) ent[e + (l - lo)] = ((unsigned)l << kLevelShift) | (unsigned)p;
@@ -310,13 +345,13 @@ __global__ void __launch_bounds__(kBlock) k_entries(const int *__restrict__ body
 }
 
 __device__ __forceinline__ void node_kind(unsigned u, const int *body_sys, const int *sys_off,
-                                          const unsigned char *delta, int &p, int &l, bool &is_cell,
-                                          bool &first) {
+                                          const unsigned char *delta, const unsigned char *bucket, int &p, int &l,
+                                          bool &is_cell, bool &first) {
     l = (int)(u >> kLevelShift);
     p = (int)(u & ((1u << kLevelShift) - 1u));
     const int beg = sys_off[body_sys[p]];
     int lo, hi, dp;
-    levels_of(delta, p, beg, lo, hi, dp);
+    levels_of(delta, bucket, p, beg, lo, hi, dp);
     is_cell = l < hi;
     first = (l == 1) ? (p == beg) : (dp < l - 1);
 }
@@ -326,12 +361,13 @@ __global__ void __launch_bounds__(kBlock) k_node_flags(const unsigned *__restric
                                                         const int *__restrict__ body_sys,
                                                         const int *__restrict__ sys_off,
                                                         const unsigned char *__restrict__ delta,
+                                                     const unsigned char *__restrict__ bucket,
                                                         unsigned long long *__restrict__ flags) {
     const int T = (int)totals[1];
     for (int b = grid_stride_start(); b < T; b += grid_stride()) {
         int p, l;
         bool c, f;
-        node_kind(ent_bfs[b], body_sys, sys_off, delta, p, l, c, f);
+        node_kind(ent_bfs[b], body_sys, sys_off, delta, bucket, p, l, c, f);
         flags[b] = ((unsigned long long)c << 32) | (unsigned long long)f;
     }
 }
@@ -342,6 +378,7 @@ __global__ void __launch_bounds__(kBlock) k_nodes_a(const unsigned *__restrict__
                                                      const int *__restrict__ body_sys,
                                                      const int *__restrict__ sys_off,
                                                      const unsigned char *__restrict__ delta,
+                                                     const unsigned char *__restrict__ bucket,
                                                      const unsigned long long *__restrict__ flags_ex,
                                                      const float4 *__restrict__ body4, int nsys,
                                                      int *__restrict__ fcl, int *__restrict__ cl,
@@ -359,7 +396,7 @@ __global__ void __launch_bounds__(kBlock) k_nodes_a(const unsigned *__restrict__
     for (int b = grid_stride_start(); b < T; b += grid_stride()) {
         int p, l;
         bool c, f;
-        node_kind(ent_bfs[b], body_sys, sys_off, delta, p, l, c, f);
+        node_kind(ent_bfs[b], body_sys, sys_off, delta, bucket, p, l, c, f);
         const unsigned long long ex = flags_ex[b];
         if (f) fcl[(int)(ex & 0xffffffffull)] = b;
         arrive[b] = 0;
@@ -380,6 +417,7 @@ __global__ void __launch_bounds__(kBlock) k_nodes_b(const unsigned *__restrict__
                                                      const int *__restrict__ body_sys,
                                                      const int *__restrict__ sys_off,
                                                      const unsigned char *__restrict__ delta,
+                                                     const unsigned char *__restrict__ bucket,
                                                      const unsigned long long *__restrict__ flags_ex,
                                                      int nsys, const int *__restrict__ fcl,
                                                      const int *__restrict__ cl, int *__restrict__ meta,
@@ -394,7 +432,7 @@ __global__ void __launch_bounds__(kBlock) k_nodes_b(const unsigned *__restrict__
     for (int b = grid_stride_start(); b < T; b += grid_stride()) {
         int p, l;
         bool c, f;
-        node_kind(ent_bfs[b], body_sys, sys_off, delta, p, l, c, f);
+        node_kind(ent_bfs[b], body_sys, sys_off, delta, bucket, p, l, c, f);
         const unsigned long long ex = flags_ex[b];
         const int fcx = (int)(ex & 0xffffffffull);
         if (c) {
@@ -664,27 +702,33 @@ int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox
                                    ctx->d_key_lo, ctx->d_val, ctx->d_body4, ctx->d_delta, ctx->d_ecount,
                                    ctx->d_status);
     ++ctx->launches;
+    const unsigned char *bucket = ctx->leaf_size > 1 ? ctx->d_bucket : nullptr;
+    if (bucket) {
+        k_bucket<<<gb, kBlock, 0, st>>>(ctx->d_body_sys, ctx->d_sys_off, n, ctx->leaf_size, ctx->d_delta,
+                                        ctx->d_bucket, ctx->d_ecount);
+        ++ctx->launches;
+    }
     rc = scan_exclusive_u32(ctx, ctx->d_ecount, ctx->d_ecount, n, nullptr, &ctx->d_totals[0], st);
     if (rc) return rc;
-    k_entries<<<gb, kBlock, 0, st>>>(ctx->d_body_sys, ctx->d_sys_off, n, ctx->d_delta, ctx->d_ecount,
+    k_entries<<<gb, kBlock, 0, st>>>(ctx->d_body_sys, ctx->d_sys_off, n, ctx->d_delta, bucket, ctx->d_ecount,
                                      ctx->d_totals, ctx->cap_nodes, ctx->d_ent, ctx->d_status);
     ++ctx->launches;
     rc = radix_sort_entries(ctx, st);  // d_ent -> d_ent_alt (BFS order)
     if (rc) return rc;
     const int gn = ceil_div(ctx->cap_nodes, kBlock) < ctx->nsm * 8 ? ceil_div(ctx->cap_nodes, kBlock) : ctx->nsm * 8;
     k_node_flags<<<gn, kBlock, 0, st>>>(ctx->d_ent_alt, ctx->d_totals, ctx->d_body_sys, ctx->d_sys_off,
-                                        ctx->d_delta, ctx->d_flags);
+                                        ctx->d_delta, bucket, ctx->d_flags);
     ++ctx->launches;
     rc = scan_exclusive_u64(ctx, ctx->d_flags, ctx->d_flags, ctx->cap_nodes, &ctx->d_totals[1],
                             &ctx->d_totals64[0], st);
     if (rc) return rc;
     k_nodes_a<<<gn, kBlock, 0, st>>>(ctx->d_ent_alt, ctx->d_totals, ctx->d_totals64, ctx->d_body_sys,
-                                     ctx->d_sys_off, ctx->d_delta, ctx->d_flags, ctx->d_body4, S, ctx->d_fcl,
+                                     ctx->d_sys_off, ctx->d_delta, bucket, ctx->d_flags, ctx->d_body4, S, ctx->d_fcl,
                                      ctx->d_cl, ctx->d_node4, ctx->d_meta, ctx->d_body_node, ctx->d_count,
                                      ctx->d_arrive, ctx->d_lvl8, ctx->d_status);
     ++ctx->launches;
     k_nodes_b<<<gn, kBlock, 0, st>>>(ctx->d_ent_alt, ctx->d_totals, ctx->d_body_sys, ctx->d_sys_off,
-                                     ctx->d_delta, ctx->d_flags, S, ctx->d_fcl, ctx->d_cl, ctx->d_meta,
+                                     ctx->d_delta, bucket, ctx->d_flags, S, ctx->d_fcl, ctx->d_cl, ctx->d_meta,
                                      ctx->d_parent, ctx->d_root_first, ctx->d_root_nch, ctx->d_status);
     ++ctx->launches;
     // up to 2^21 bodies the 41 per-level launches cost more than the sums: one
@@ -743,7 +787,7 @@ __global__ void __launch_bounds__(kBlock) k_export(const unsigned *__restrict__ 
         const int p = (int)(u & ((1u << kLevelShift) - 1u));
         if (body_sys[p] != sys) continue;
         int lo, hi, dp;
-        levels_of(delta, p, beg, lo, hi, dp);
+        levels_of(delta, nullptr, p, beg, lo, hi, dp);
         const bool is_cell = l < hi;
         const int pre = (int)(eoff[p] - (unsigned)p) - cells_before + (l - lo);
         int value;
@@ -779,7 +823,7 @@ __global__ void __launch_bounds__(kBlock) k_export(const unsigned *__restrict__ 
             const int pl = (int)(pu >> kLevelShift);
             const int pp = (int)(pu & ((1u << kLevelShift) - 1u));
             int plo, phi, pdp;
-            levels_of(delta, pp, beg, plo, phi, pdp);
+            levels_of(delta, nullptr, pp, beg, plo, phi, pdp);
             const int ppre = (int)(eoff[pp] - (unsigned)pp) - cells_before + (pl - plo);
             if (ppre < cap_cells) cell_child[8 * ppre + slot] = value;
         }
@@ -795,7 +839,8 @@ __global__ void k_perm_export(const int *val, int beg, int n, int *perm) {
 int export_tree_impl(Ctx *ctx, int sys, int *perm, int *root_child, int *cell_child, int *cell_start,
                      int *cell_count, int *cell_level, float *cx, float *cy, float *cz, float *cm,
                      int cap_cells, int64_t *ncells, cudaStream_t st, int sum_mode) {
-    if (!ctx->built || ctx->key_order != 0) return NBX_ERR_STATE;
+    // the reference's array format holds the reference's tree: Lebesgue order, one body per leaf
+    if (!ctx->built || ctx->key_order != 0 || ctx->leaf_size != 1) return NBX_ERR_STATE;
     if (sys < 0 || sys >= ctx->nsys) return NBX_ERR_ARG;
     int off[2];
     NBX_CUDA(cudaMemcpyAsync(off, ctx->d_sys_off + sys, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));

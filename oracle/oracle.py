@@ -7,6 +7,7 @@ leg of ``bench.py`` use this module, as a checker.
 """
 from __future__ import annotations
 
+import copy
 import ctypes as C
 import os
 from dataclasses import dataclass
@@ -207,6 +208,41 @@ def build(x, y, z, m, bb=None, max_depth=42):
     return Tree(n, bb, perm, k, rootc, cc[: 8 * k].reshape(k, 8).copy(), cs[:k].copy(),
                 cn[:k].copy(), cl[:k].copy(), cx[:k].copy(), cy[:k].copy(), cz[:k].copy(),
                 cm[:k].copy(), m64[:k].copy(), com64[: 3 * k].reshape(k, 3).copy())
+
+
+def bucket_tree(tree: Tree, k: int) -> Tree:
+    """The tree with leaf buckets of at most k bodies (nbx_params.leaf_size; the
+    reference keeps one body per leaf): every cell holding at most k bodies
+    whose parent holds more (or which is a root child) becomes a leaf whose
+    child slots are its bodies in sorted order; the cells below it become
+    unreachable.  Moments are unchanged (a bucket is the same cell)."""
+    if k <= 1:
+        return tree
+    n, nc = tree.n, tree.ncells
+    cc = tree.cell_child.copy()
+    parent = np.full(nc, -1, np.int64)
+    rows, cols = np.nonzero(cc >= n)
+    parent[cc[rows, cols] - n] = rows
+    cnt = tree.cell_count
+    bucket = (cnt <= k) & ((parent < 0) | (cnt[np.maximum(parent, 0)] > k))
+    for c in np.nonzero(bucket)[0]:
+        cc[c, :] = -1
+        cc[c, :cnt[c]] = tree.perm[tree.cell_start[c]:tree.cell_start[c] + cnt[c]]
+    out = copy.copy(tree)
+    out.cell_child = cc
+    return out
+
+
+def reachable_cells(tree: Tree) -> int:
+    """Cells reachable from the root children (bucket_tree leaves some unreachable)."""
+    n = tree.n
+    todo = [c - n for c in tree.root_child if c >= n]
+    seen = 0
+    while todo:
+        c = todo.pop()
+        seen += 1
+        todo.extend(int(ch) - n for ch in tree.cell_child[c] if ch >= n)
+    return seen
 
 
 def depth0(bb, theta_ref):

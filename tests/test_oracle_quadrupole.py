@@ -46,3 +46,33 @@ def test_quadrupole_evaluation_same_lists_and_closer_to_direct_sum():
         e0 = np.linalg.norm(f0.a64[tg] - d, axis=1) / np.linalg.norm(d, axis=1)
         e1 = np.linalg.norm(f1.a64[tg] - d, axis=1) / np.linalg.norm(d, axis=1)
         assert np.median(e1) < 0.5 * np.median(e0), (np.median(e0), np.median(e1))
+
+
+def test_bucket_tree_invariants():
+    """oracle.bucket_tree (the leaf buckets of nbx_params.leaf_size): every leaf
+    cell holds at most k bodies, its parent more, its child slots are its own
+    bodies; k = 1 is the reference's tree and gives its walk."""
+    b = ic.plummer(4000, seed=ic.SEED0 + 5)
+    t = O.build(b.x, b.y, b.z, b.m)
+    n = t.n
+    for k in (1, 2, 4, 8):
+        bt = O.bucket_tree(t, k)
+        todo = [(c - n, -1) for c in bt.root_child if c >= n]
+        cells = 0
+        while todo:
+            c, par = todo.pop()
+            cells += 1
+            ch = bt.cell_child[c]
+            if (ch[ch >= 0] < n).all() and t.cell_count[c] <= k:
+                assert par < 0 or t.cell_count[par] > k
+                want = t.perm[t.cell_start[c]:t.cell_start[c] + t.cell_count[c]]
+                assert np.array_equal(ch[ch >= 0], want)
+            else:
+                assert t.cell_count[c] > k or k == 1
+            todo.extend((int(x) - n, c) for x in ch if x >= n)
+        assert cells == O.reachable_cells(bt)
+        if k == 1:
+            assert cells == t.ncells
+    f1 = O.forces(b.x, b.y, b.z, b.m, O.bucket_tree(t, 1), 0.25, 1e-4)
+    f0 = O.forces(b.x, b.y, b.z, b.m, t, 0.25, 1e-4)
+    assert np.array_equal(f0.nlist, f1.nlist) and np.array_equal(f0.a, f1.a)
