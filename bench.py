@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-hilbert", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-buckets", action="store_true")
     ap.add_argument("--fd-directions", type=int, default=16)
     ap.add_argument("--adjoint-steps", type=int, default=100)
     ap.add_argument("--adjoint-checkpoint", type=int, default=10)
@@ -189,7 +190,10 @@ def bench_batched(args, local):
         a, b = int(off[i]), int(off[i + 1])
         sub = ic.Bodies(*(arr[a:b] for arr in bodies.arrays()))
         c1 = Context(max_bodies=b - a, theta=0.5, eps=0.01, dt=1e-3, device=local)
+        # the same walk configuration: the launch shape, buffer width and stack depth
+        # set the order of the force sums (not the lists)
         c1.set_walk(tune["warps"], tune["variant"])
+        c1.set_tuning(tune["radix_bits"], tune["stack_depth"])
         c1.set_systems([0, b - a])
         ctxs.append(c1)
         states.append(State.from_bodies(sub, device="cuda:%d" % local))
@@ -362,7 +366,7 @@ def bench_hilbert(args, local, b, targets, acc64, tune) -> dict:
 
 ACCURACY_TARGET = 1e-4
 ACCURACY_THETAS = {0: (0.4, 0.3, 0.25, 0.2, 0.15, 0.125, 0.1),
-                   1: (0.5, 0.45, 0.4, 0.35, 0.3, 0.25, 0.2)}
+                   1: (0.7, 0.65, 0.6, 0.55, 0.5, 0.45, 0.4, 0.35, 0.3)}
 
 
 def bench_accuracy(args, local, b, targets, acc64, tune, multipole=0) -> dict:
@@ -427,6 +431,68 @@ def bench_accuracy(args, local, b, targets, acc64, tune, multipole=0) -> dict:
             "walk_config": walk,
             "note": "%s; the first theta in %s whose median error meets the target"
                     % (kind, list(ACCURACY_THETAS[multipole]))}
+
+
+LEAF_SIZES = (1, 2, 4, 8)
+
+
+def bench_buckets(args, local, b, targets, acc64, tune) -> dict:
+    """Leaf buckets (nbx_params.leaf_size; outside the parity mode): the same
+    workload at theta 0.5 with cells of at most k bodies as leaves.  Per k the
+    error against the FP64 direct sum on the same targets, the cells and
+    interactions, and plain FP32 steps timed with CUDA events after one warm-up
+    step; then the autotuner's leaf-size stage picks k over build + walk steps."""
+    import torch
+    from nns_gb300 import autotune
+    from nns_gb300.barnes_hut import Context, State
+    n = len(b.x)
+    ctx = Context(max_bodies=n, theta=THETA, eps=EPS, dt=DT, device=local)
+    if tune:
+        ctx.set_walk(tune["warps"], tune["variant"])
+    ctx.set_systems([0, n])
+    points = []
+    for k in LEAF_SIZES:
+        ctx.set_leaf_size(k)
+        s = State.from_bodies(b, device="cuda:%d" % local)
+        ctx.build(s)
+        ctx.forces(s)
+        ctx.sync()
+        a = s.acc()[targets].astype(np.float64)
+        rel = np.linalg.norm(a - acc64, axis=1) / np.linalg.norm(acc64, axis=1)
+        ctx.step(s)
+        reps = 3
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(reps)]
+        torch.cuda.synchronize()
+        for e in ev:
+            e[0].record()
+            ctx.build(s)
+            ctx.forces(s)
+            e[1].record()
+            ctx.integrate(s)
+            e[2].record()
+        torch.cuda.synchronize()
+        info = ctx.tree_info()
+        ctx.sync()
+        ms = sum(e[0].elapsed_time(e[2]) for e in ev) / reps
+        points.append({"leaf_size": k, "steps_per_s": round(1000.0 / ms, 4), "ms_per_step": round(ms, 3),
+                       "steps": reps, "cells": info["ncells"], "interactions_per_step": info["interactions"],
+                       "opened_cells_per_step": info["opened"],
+                       "force_error_vs_fp64_direct": {"median": float(np.median(rel)),
+                                                      "p99": float(np.quantile(rel, 0.99))}})
+        del s
+    s = State.from_bodies(b, device="cuda:%d" % local)
+    tb = autotune.tune_walk(ctx, s, use_cache=False, candidates=((ctx_warps(tune), ctx_variant(tune)),),
+                            stack_depths=(512,), radix_bits=(8,), leaf_sizes=LEAF_SIZES)
+    return {"theta": THETA, "points": points, "autotune_leaf_size": tb["leaf_size"], "autotune_ms": tb["ms_leaf"],
+            "note": "leaf_size 1 is the reference's tree (the parity mode); k > 1 changes the tree and the lists"}
+
+
+def ctx_warps(tune):
+    return tune["warps"] if tune and "warps" in tune else 8
+
+
+def ctx_variant(tune):
+    return tune["variant"] if tune and "variant" in tune else 3
 
 
 def error_target(errs, errs32, accuracy, accuracy_quad) -> dict:
@@ -719,6 +785,10 @@ def main():
         accuracy_quad = _section(bench_accuracy, args, local, b, targets, acc64,
                                  tune if tune and "warps" in tune else None, 1)
         torch.cuda.empty_cache()
+    buckets = None
+    if not args.no_buckets:
+        buckets = _section(bench_buckets, args, local, b, targets, acc64, tune if tune and "warps" in tune else None)
+        torch.cuda.empty_cache()
     hilbert = None
     if not args.no_hilbert:
         hilbert = _section(bench_hilbert, args, local, b, targets, acc64, tune if tune and "warps" in tune else None)
@@ -780,6 +850,7 @@ def main():
                 "pipeline": "two device states: the copies of one step overlap the compute of the other",
                 "d2h_bytes_per_step": d2h},
         "hilbert": hilbert,
+        "buckets": buckets,
         "batched": batched,
         "adjoint": adjoint,
         "autotune": tune,

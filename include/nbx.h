@@ -131,7 +131,10 @@ int nbx_set_walk_config(nbx_ctx *ctx, int warps_per_block, int variant);
 /* Sort digit width (8: 8 passes, 9: 7 passes over the 63-bit keys; both give the
  * same stable order) and walk stack entries per warp (360..4096; a launch whose
  * stacks and buffers exceed the device's shared memory per block fails with
- * NBX_ERR_ARG).  A built tree stays valid.  Used by the autotuner. */
+ * NBX_ERR_ARG).  The stack depth never changes the interaction lists, but it
+ * sets how the walk groups candidates into rounds near the depth-first reserve,
+ * so forces can differ in their last bits between depths.  A built tree stays
+ * valid.  Used by the autotuner. */
 int nbx_set_tuning(nbx_ctx *ctx, int radix_bits, int stack_depth);
 /* Multipole order of the force (nbx_params.multipole: 0 monopoles, 1 with
  * quadrupoles).  The context needs a new build before its next walk
@@ -282,14 +285,14 @@ int nbx_diagnostics_fp64(nbx_ctx *ctx, const nbx_state *s, int n, double *out, v
  * of every system's bodies (x, y, z, vx, vy, vz, m: the state a kick-drift step
  * needs) plus the system offsets, the step's constants (MAC constant,
  * softening, dt, dampening, compensation, key order), the walk's launch
- * shape and buffer variant (which fix the order of the force sums), the
- * multipole order and the leaf bucket size, into a caller-owned host buffer: a
- * versioned header (72 bytes), the offsets, the
+ * shape, buffer variant and stack depth (which fix the order of the force
+ * sums), the multipole order and the leaf bucket size, into a caller-owned host
+ * buffer: a versioned header (80 bytes), the offsets, the
  * seven float arrays, and 64-bit checksums of header and payload.  Restoring
  * it into a context (capacity permitting) sets the systems, constants, walk
- * configuration, multipole order and leaf size and copies the bodies into the caller's device state, so that
- * the run continues bit for bit.  The sort's digit width and the stack depth
- * change no result and are not recorded. */
+ * configuration, multipole order and leaf size and copies the bodies into the
+ * caller's device state, so that the run continues bit for bit.  The sort's
+ * digit width changes no result and is not recorded. */
 int64_t nbx_checkpoint_bytes(int64_t nbodies, int nsystems);
 /* Synchronises `stream`; *written receives the bytes used. */
 int nbx_checkpoint_save(nbx_ctx *ctx, const nbx_state *s, void *host, int64_t capacity, int64_t *written,

@@ -1,17 +1,23 @@
 """Autotuner for the launch parameters of the force walk and the key sort.
 
-The interaction lists are fixed by the reference's semantics (group of 32,
-leaf bucket of one body), so the tunable knobs are the ones that change only
-speed:
+In the parity mode the interaction lists are fixed by the reference's
+semantics (group of 32, one body per leaf), so the tunable knobs are the ones
+that leave the lists unchanged (the buffer size and the stack depth regroup
+the candidates into rounds, which can change the last bits of the FP32 force
+sums; the launch shape and the digit width change nothing):
   * warps per block of the walk (4, 8, 16) -- occupancy vs. shared memory,
   * candidate buffer size of the walk (64, 96 or 128 slots per warp),
   * walk stack entries per warp (a deeper stack keeps more rounds wide, a
     shallower one leaves shared memory for more blocks),
   * sort digit width (8 bits in 8 passes or 9 bits in 7 passes; a stable LSD
     sort gives the same order for any width).
+Outside the parity mode the caller may also offer leaf bucket sizes
+(``leaf_sizes``, nbx_params.leaf_size 1..8): they change the tree and the
+lists (and the error), so the default offers only one body per leaf.
 Candidates are timed with CUDA events on the caller's workload after one
-build, in that order, each stage with the winners of the stages before it;
-the winner is applied to the context and cached per (device, n, systems) in
+build, in that order, each stage with the winners of the stages before it
+(leaf sizes first, over whole build + walk steps); the winner is applied to
+the context and cached per (device, n, systems, modes) in
 ``~/.cache/nbx_autotune.json`` (override with NBX_AUTOTUNE_CACHE).
 """
 from __future__ import annotations
@@ -55,12 +61,15 @@ def _time(fn, reps):
 
 
 def tune_walk(ctx, state, reps: int = 2, candidates=CANDIDATES, use_cache: bool = True,
-              stack_depths=STACK_DEPTHS, radix_bits=RADIX_BITS, timer=None) -> dict:
+              stack_depths=STACK_DEPTHS, radix_bits=RADIX_BITS, timer=None, leaf_sizes=None) -> dict:
     """Times the candidate configurations and applies the fastest.  ``timer(fn,
-    reps)`` returns milliseconds per call (CUDA events by default)."""
+    reps)`` returns milliseconds per call (CUDA events by default).
+    ``leaf_sizes`` (None: keep the context's) are leaf bucket sizes to try."""
     timer = timer or _time
     n = int(ctx.offsets[-1])
     key = _key(ctx, n)
+    if leaf_sizes is not None:
+        key += "|leaves=" + ",".join(str(int(k)) for k in leaf_sizes)
     path = _cache_path()
     cache = {}
     if use_cache and os.path.exists(path):
@@ -70,11 +79,25 @@ def tune_walk(ctx, state, reps: int = 2, candidates=CANDIDATES, use_cache: bool 
             cache = {}
     if use_cache and key in cache and "stack_depth" in cache[key]:
         best = cache[key]
+        if "leaf_size" in best:
+            ctx.set_leaf_size(best["leaf_size"])
         ctx.set_walk(best["warps"], best["variant"])
         ctx.set_tuning(best["radix_bits"], best["stack_depth"])
         return dict(best, cached=True)
     bits0 = int(ctx.params.radix_bits)
     depth0 = int(ctx.params.stack_depth)
+    # 0. leaf bucket size (outside the parity mode only), over build + walk
+    ltimes = {}
+    if leaf_sizes:
+        for k in leaf_sizes:
+            ctx.set_leaf_size(int(k))
+
+            def step():
+                ctx.build(state)
+                ctx.forces(state)
+            ltimes[str(int(k))] = timer(step, reps)
+        ctx.sync()
+        ctx.set_leaf_size(int(min(ltimes, key=ltimes.get)))
     ctx.build(state)
     ctx.sync()
     # 1. walk launch shape
@@ -108,6 +131,9 @@ def tune_walk(ctx, state, reps: int = 2, candidates=CANDIDATES, use_cache: bool 
     ctx.build(state)
     best = {"warps": warps, "variant": variant, "stack_depth": depth, "radix_bits": bits,
             "ms": times, "ms_stack": stimes, "ms_build": btimes}
+    if leaf_sizes:
+        best["leaf_size"] = int(ctx.params.leaf_size)
+        best["ms_leaf"] = ltimes
     if use_cache:
         cache[key] = best
         try:

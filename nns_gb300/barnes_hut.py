@@ -254,7 +254,7 @@ class Context:
         check(lib().nbx_checkpoint_restore(self.h, C.byref(s.c), b.ctypes.data_as(C.c_void_p), b.size,
                                            _stream_ptr(stream)), "nbx_checkpoint_restore", self.h)
         nsys = int(np.frombuffer(b[12:16].tobytes(), np.int32)[0])
-        self.offsets = [int(v) for v in np.frombuffer(b[72:72 + 8 * (nsys + 1)].tobytes(), np.int64)]
+        self.offsets = [int(v) for v in np.frombuffer(b[80:80 + 8 * (nsys + 1)].tobytes(), np.int64)]
 
     def diagnostics(self, s: "State", n: int | None = None, stream=None):
         out = torch.zeros(8, dtype=torch.float64, device=self.device)

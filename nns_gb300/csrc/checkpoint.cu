@@ -3,9 +3,10 @@
 //
 // Layout (little-endian, 8-byte aligned sections):
 //   Header   magic "NBXCKPT1", version, nsys, nbodies, the step constants,
-//            the walk's launch shape and buffer variant (the buffer width sets
-//            the order of the force sums, so a bit-exact resume needs it), the
-//            multipole order and the leaf bucket size,
+//            the walk's launch shape, buffer variant and stack depth (the
+//            buffer width and the stack depth set how the walk's rounds group
+//            the candidates, i.e. the order of the force sums, so a bit-exact
+//            resume needs them), the multipole order and the leaf bucket size,
 //            FNV-1a 64 of the header bytes before it and of the offsets
 //   int64    offsets[nsys + 1]
 //   float    x, y, z, vx, vy, vz, m   [nbodies] each
@@ -31,12 +32,13 @@ struct CkptHeader {
     int32_t compensated, key_order;
     int32_t walk_warps, walk_variant;
     int32_t multipole, leaf_size;
+    int32_t stack_depth, reserved;
     uint64_t header_hash;  // of the bytes above and of the offsets
 };
-static_assert(sizeof(CkptHeader) == 72, "checkpoint header layout");
+static_assert(sizeof(CkptHeader) == 80, "checkpoint header layout");
 
 constexpr char kMagic[8] = {'N', 'B', 'X', 'C', 'K', 'P', 'T', '1'};
-constexpr uint32_t kVersion = 3;
+constexpr uint32_t kVersion = 4;
 constexpr int kArrays = 7;
 
 uint64_t fnv1a(const void *p, size_t n, uint64_t h = 1469598103934665603ull) {
@@ -115,6 +117,7 @@ extern "C" int nbx_checkpoint_save(nbx_ctx *c, const nbx_state *s, void *host, i
     h.walk_variant = ctx->walk_variant;
     h.multipole = ctx->multipole;
     h.leaf_size = ctx->leaf_size;
+    h.stack_depth = ctx->p.stack_depth;
     h.header_hash = nbx::header_hash(h, offs, nsys);
     std::memcpy(out, &h, sizeof(h));
     const uint64_t sum = nbx::payload_sum(payload, (size_t)nbx::kArrays * n);
@@ -157,6 +160,8 @@ extern "C" int nbx_checkpoint_restore(nbx_ctx *c, nbx_state *s, const void *host
     rc = nbx_set_walk_config(c, h.walk_warps, h.walk_variant);
     if (rc) return rc;
     rc = nbx_set_leaf_size(c, h.leaf_size);
+    if (rc) return rc;
+    rc = nbx_set_tuning(c, ctx->radix_bits, h.stack_depth);
     if (rc) return rc;
     ctx->p.dt = h.dt;
     ctx->p.dampening = h.dampening;

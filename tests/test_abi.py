@@ -87,10 +87,10 @@ def test_set_tuning_validates_without_gpu():
 
 
 def test_checkpoint_size_without_gpu():
-    """nbx_checkpoint_bytes: the 72-byte header, nsys + 1 int64 offsets, seven float
+    """nbx_checkpoint_bytes: the 80-byte header, nsys + 1 int64 offsets, seven float
     arrays and the 8-byte payload checksum; 0 for an empty request."""
     from nns_gb300 import _lib
     L = _lib.lib()
     for n, nsys in ((1, 1), (4096, 1), (14499946, 512), (1 << 26, 1)):
-        assert L.nbx_checkpoint_bytes(n, nsys) == 72 + 8 * (nsys + 1) + 7 * 4 * n + 8
+        assert L.nbx_checkpoint_bytes(n, nsys) == 80 + 8 * (nsys + 1) + 7 * 4 * n + 8
     assert L.nbx_checkpoint_bytes(0, 1) == 0 and L.nbx_checkpoint_bytes(5, 0) == 0

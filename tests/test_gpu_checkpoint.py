@@ -1,7 +1,8 @@
 """Checkpoint / resume (nbx_checkpoint_*) and the node-pool overflow guard.
 
 * A run resumed from a checkpoint continues bit for bit (batched systems,
-  compensated forces).
+  compensated forces), also into a context with another walk configuration,
+  multipole order or leaf size (the checkpoint restores them).
 * A corrupted or truncated checkpoint is refused with NBX_ERR_FORMAT and
   changes nothing; a context too small for it is refused with NBX_ERR_ARG.
 * A tree larger than the node pool reports NBX_ERR_CAPACITY; the failed tree is
@@ -38,6 +39,33 @@ def test_resume_is_bit_exact(cuda):
     assert ctx2.offsets == [int(v) for v in off]
     assert ctx2.constants() == ctx.constants()
     got = _run(ctx2, s2, 4)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("mode", ["tuned", "quadrupole_buckets"])
+def test_resume_restores_the_walk_configuration(cuda, mode):
+    """The checkpoint carries what sets the force bits beyond the constants: the
+    walk's buffer variant and stack depth (they group candidates into rounds),
+    the multipole order and the leaf size; a context with other settings resumes
+    bit for bit."""
+    from nns_gb300.barnes_hut import Context, State
+    b = ic.plummer(30000, seed=ic.SEED0 + 41)
+    n = len(b.x)
+    ctx = Context(max_bodies=n, theta=0.5, eps=0.01, dt=1e-3)
+    ctx.set_systems([0, n])
+    ctx.set_walk(4, 1)
+    ctx.set_tuning(8, 384)
+    if mode == "quadrupole_buckets":
+        ctx.set_multipole(1)
+        ctx.set_leaf_size(4)
+    s = State.from_bodies(b)
+    _run(ctx, s, 2)
+    buf = ctx.checkpoint(s)
+    want = _run(ctx, s, 3)
+    ctx2 = Context(max_bodies=n, theta=0.5, eps=0.01, dt=1e-3)
+    s2 = State.empty(n)
+    ctx2.restore(s2, buf)
+    got = _run(ctx2, s2, 3)
     assert np.array_equal(got, want)
 
 

@@ -21,6 +21,7 @@ class FakeParams:
     compensated = 0
     radix_bits = 8
     stack_depth = 512
+    leaf_size = 1
 
 
 class FakeCtx:
@@ -38,6 +39,9 @@ class FakeCtx:
 
     def set_tuning(self, bits, depth):
         self.params.radix_bits, self.params.stack_depth = bits, depth
+
+    def set_leaf_size(self, k):
+        self.params.leaf_size = k
 
     def build(self, state):
         self.calls.append(("build", self.params.radix_bits))
@@ -133,3 +137,33 @@ def test_cache_key_separates_orders_and_moment_passes(monkeypatch):
                     p = SimpleNamespace(compensated=comp, key_order=order, moments_mode=moments, multipole=mp)
                     keys.add(autotune._key(SimpleNamespace(device=0, offsets=[0, 100], params=p), 100))
     assert len(keys) == 24
+
+
+def test_leaf_sizes_are_offered_only_on_request(tmp_path, monkeypatch):
+    """The leaf bucket stage runs only when the caller offers leaf sizes (outside
+    the parity mode); it times build + walk steps, applies the fastest size
+    before the other stages and caches it under its own key."""
+    monkeypatch.setenv("NBX_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    monkeypatch.setattr(autotune, "_key", lambda ctx, n: "fake|n=%d" % n)
+    step_ms = {1: 9.0, 4: 6.0, 8: 7.0}
+
+    def timer_for(ctx):
+        def timer(fn, reps):
+            n0 = len(ctx.calls)
+            fn()
+            kinds = [c[0] for c in ctx.calls[n0:]]
+            if kinds == ["build", "forces"]:
+                return step_ms[ctx.params.leaf_size]
+            return 1.0
+        return timer
+
+    ctx = FakeCtx()
+    r = autotune.tune_walk(ctx, None, timer=timer_for(ctx))
+    assert "leaf_size" not in r and ctx.params.leaf_size == 1
+    ctx = FakeCtx()
+    r = autotune.tune_walk(ctx, None, timer=timer_for(ctx), leaf_sizes=(1, 4, 8))
+    assert r["leaf_size"] == 4 and ctx.params.leaf_size == 4 and r["ms_leaf"] == {"1": 9.0, "4": 6.0, "8": 7.0}
+    ctx2 = FakeCtx()
+    r2 = autotune.tune_walk(ctx2, None, timer=lambda fn, reps: pytest.fail("timed a cached entry"),
+                            leaf_sizes=(1, 4, 8))
+    assert r2["cached"] and ctx2.params.leaf_size == 4
