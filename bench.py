@@ -551,18 +551,32 @@ def hbm_roofline(n: int, integ_ms: float, peaks: dict) -> dict:
             "bytes_per_body": 60, "peak_kind": "measured copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"}
 
 
+def _git_blob_sha1(path: str) -> str:
+    """The git blob hash of a file (sha1 of "blob <size>\\0" + content)."""
+    import hashlib
+    data = open(path, "rb").read()
+    return hashlib.sha1(b"blob %d\0" % len(data) + data).hexdigest()
+
+
 def walk_traffic(n: int):
     """DRAM bytes (read + write) of one walk launch at this size, from the committed
-    ncu summary of the benchmark workload (profiles/), or None for other sizes."""
+    ncu summary of the benchmark workload (profiles/), or None for other sizes or
+    when the walk's source differs from the captured one (the summary records the
+    git blob hash of walk2.cu)."""
     if n != N_DEFAULT:
         return None
+    traffic = blob = None
     try:
         for line in open(os.path.join(ROOT, "profiles", "k_walk2_traffic_binary_disk_2p24.md")):
             if line.startswith("traffic_bytes_per_launch:"):
-                return int(line.split(":")[1])
+                traffic = int(line.split(":")[1])
+            elif line.startswith("walk2_cu_blob:"):
+                blob = line.split(":")[1].strip()
     except (OSError, ValueError):
-        pass
-    return None
+        return None
+    if blob != _git_blob_sha1(os.path.join(ROOT, "nns_gb300", "csrc", "walk2.cu")):
+        return None
+    return traffic
 
 
 def bench_frame(ctx, s, b, reps: int = 5) -> dict:

@@ -1,6 +1,7 @@
 """Host-side helpers of bench.py (no GPU): the committed walk-traffic figure is
-read from its profile, the HBM roofline arithmetic, and the guard that keeps a
-failing extension section from losing the JSON line."""
+read from its profile (only while the walk's source has the captured git blob
+hash), the HBM roofline arithmetic, and the guard that keeps a failing
+extension section from losing the JSON line."""
 import os
 import sys
 
@@ -10,9 +11,23 @@ sys.path.insert(0, os.path.dirname(HERE))
 import bench  # noqa: E402
 
 
-def test_walk_traffic_is_read_from_the_profile():
+def test_walk_traffic_is_read_from_the_profile(monkeypatch):
+    """The figure is reported only for the walk source it was captured from."""
+    blob = [ln.split(":")[1].strip() for ln in open(os.path.join(HERE, "..", "profiles",
+                                                                "k_walk2_traffic_binary_disk_2p24.md"))
+            if ln.startswith("walk2_cu_blob:")][0]
+    monkeypatch.setattr(bench, "_git_blob_sha1", lambda path: blob)
     t = bench.walk_traffic(1 << 24)
     assert isinstance(t, int) and t > 10 ** 9
+    assert bench.walk_traffic(1 << 20) is None
+    monkeypatch.setattr(bench, "_git_blob_sha1", lambda path: "0" * 40)
+    assert bench.walk_traffic(1 << 24) is None
+
+
+def test_git_blob_hash(tmp_path):
+    p = tmp_path / "f"
+    p.write_bytes(b"hello\n")
+    assert bench._git_blob_sha1(str(p)) == "ce013625030ba8dba906f756967f9e9ca394464a"
 
 
 def test_hbm_roofline_arithmetic():
