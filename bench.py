@@ -35,7 +35,7 @@ FLOP_PER_INTERACTION = 20
 def workload_config(n, world):
     return {"workload": "binary_disk_2^24 precision form", "n": n, "theta": THETA, "eps": EPS,
             "dt": DT, "group": 32, "l2": "inputs larger than L2 (no flush)",
-            "parallelism": "replicas" if world > 1 else "single"}
+            "parallelism": ("key-range split of one system over %d GPUs" % world) if world > 1 else "single"}
 
 
 def parse():
@@ -173,6 +173,15 @@ def bench_batched(args, local):
     from nns_gb300 import autotune, ic
     from nns_gb300.barnes_hut import Context, State
     bodies, off = ic.batched_star_disks(args.batched_systems)
+    rank, world, _ = dist_info()
+    nsys_all = len(off) - 1
+    if world > 1:
+        # several ranks: each steps its own contiguous share of the systems (no exchange)
+        from nns_gb300.dist import shard_systems
+        s0, s1, loc = shard_systems(off, rank, world)
+        a0, a1 = int(off[s0]), int(off[s1])
+        bodies = ic.Bodies(*(arr[a0:a1] for arr in bodies.arrays()))
+        off = loc
     nsys = len(off) - 1
     ntot = int(off[-1])
     ctx = Context(max_bodies=ntot, max_systems=nsys, theta=0.5, eps=0.01, dt=1e-3, device=local)
@@ -214,6 +223,10 @@ def bench_batched(args, local):
     ctx.sync()
     t_batch = e0.elapsed_time(e1) / steps
     inter = ctx.tree_info()["interactions"]
+    if world > 1:
+        from nns_gb300.dist import max_over_ranks, sum_over_ranks
+        t_batch = max_over_ranks(t_batch, device="cuda")
+        inter = int(sum_over_ranks(float(inter), device="cuda"))
     # one system at a time (eager launches, one context per system)
     for c1, s1 in zip(ctxs, states):
         c1.step(s1, 1)
@@ -241,12 +254,12 @@ def bench_batched(args, local):
         g1.record(gs)
     torch.cuda.synchronize()
     t_single_graph = g0.elapsed_time(g1) / single_steps
-    return {"systems": nsys, "bodies": ntot, "steps": steps,
+    return {"systems": nsys_all, "bodies": ntot, "steps": steps, "ranks": world,
             "ms_per_step": round(t_batch, 3),
-            "systems_steps_per_s": round(nsys * 1000.0 / t_batch, 2),
+            "systems_steps_per_s": round(nsys_all * 1000.0 / t_batch, 2),
             "one_at_a_time_ms_per_step": round(t_single, 3),
             "one_at_a_time_systems_steps_per_s": round(nsys * 1000.0 / t_single, 2),
-            "speedup_vs_one_at_a_time": round(t_single / t_batch, 3),
+            "speedup_vs_one_at_a_time": round(t_single / t_batch, 3),  # this rank's systems
             "one_at_a_time_graphs_ms_per_step": round(t_single_graph, 3),
             "speedup_vs_one_at_a_time_graphs": round(t_single_graph / t_batch, 3),
             "interactions_per_step": inter,
@@ -638,7 +651,17 @@ def main():
         except Exception as e:  # noqa: BLE001 -- the default launch shape stays; reported
             tune = {"unavailable": str(e)[:200]}
 
+    # several ranks: the system is split by key ranges of walk groups (each rank
+    # walks its share of a replicated tree; the accelerations are summed over
+    # NCCL); one rank: the plain step
+    split = None
+    if world > 1:
+        from nns_gb300.dist import SplitSystem
+        split = SplitSystem(ctx, s, rank, world)
+
     def timed(nsteps, phase=True):
+        if split is not None:
+            return timed_split(nsteps)
         ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(nsteps)]
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
@@ -670,6 +693,29 @@ def main():
                     rounds=info["rounds"], candidates=info["candidates"],
                     launches=info["launches"] - launches0,
                     ncells=info["ncells"], max_level=info["max_level"])
+
+    def timed_split(nsteps):
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        launches0 = ctx.tree_info()["launches"]
+        torch.distributed.barrier()
+        torch.cuda.synchronize()
+        t0.record()
+        inter = 0
+        for _ in range(nsteps):
+            split.forces()
+            inter += ctx.tree_info()["interactions"]  # this rank's groups
+            ctx.integrate(s)
+        t1.record()
+        torch.cuda.synchronize()
+        torch.distributed.barrier()
+        total = t0.elapsed_time(t1)
+        info = ctx.tree_info()
+        from nns_gb300.dist import sum_over_ranks
+        inter = int(sum_over_ranks(float(inter), device="cuda")) // max(nsteps, 1)
+        return dict(ms=total, build_ms=0.0, walk_ms=total, integ_ms=0.0, interactions=inter, opened=0,
+                    rounds=0, candidates=0, launches=info["launches"] - launches0, ncells=info["ncells"],
+                    max_level=info["max_level"])
 
     # ---- error at the initial state (outside any timed region)
     rng = np.random.default_rng(12345)
@@ -784,9 +830,10 @@ def main():
     steps_per_s = 1000.0 / ms_plain
 
     if world > 1:
+        # one system walked by all ranks: its steps/s is the job's (strong scaling)
         from nns_gb300.dist import max_over_ranks
         ms_plain = max_over_ranks(ms_plain, device="cuda")
-        steps_per_s = world * 1000.0 / ms_plain
+        steps_per_s = 1000.0 / ms_plain
 
     batched = None
     del ctx, s
@@ -832,7 +879,7 @@ def main():
     line = {
         "metric": METRIC, "value": round(steps_per_s, 4), "unit": "steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_plain, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "higher_is_better": True, "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (nns_gb300.ic binary_disk, seed 20261203)",
         "config": workload_config(n, world),
         "compensated": {"value": round(1000.0 / ms_comp, 4), "unit": "steps/s",

@@ -203,6 +203,23 @@ int nbx_set_systems(nbx_ctx *ctx, int nsys, const int64_t *offsets);
 int nbx_build(nbx_ctx *ctx, const nbx_state *s, void *stream);
 /* tree walk of the last build -> s->ax, s->ay, s->az */
 int nbx_forces(nbx_ctx *ctx, const nbx_state *s, void *stream);
+/* Walk groups: runs of up to 32 consecutive sorted bodies of one system (the
+ * warp-coherent MAC's group), numbered system by system in sorted order, so a
+ * range of groups is a range of keys.  nbx_group_count gives their number. */
+int nbx_group_count(nbx_ctx *ctx, int *ngroups);
+/* The walk of groups [first_group, first_group + ngroups) of the last build
+ * only: the forces of those groups' bodies are written, every other body's
+ * acceleration is left as it was.  One rank's share when one system is split
+ * over several GPUs by key ranges (the reference's SFC decomposition,
+ * MolecularDynamics/BarnesHutParallel/SpaceFillingCurves/src/Tree.cpp:165-317,
+ * here over a replicated tree): each rank zeroes the accelerations, walks its
+ * groups and the ranks sum the accelerations (nns_gb300/dist.py).  Not for
+ * walk_variant 2. */
+int nbx_forces_groups(nbx_ctx *ctx, const nbx_state *s, int first_group, int ngroups, void *stream);
+/* Per-group interaction-list length and opened cells of the last walk (device
+ * int arrays of nbx_group_count entries; either may be NULL): the work
+ * measure for balancing key ranges.  Synchronises `stream`. */
+int nbx_export_group_stats(nbx_ctx *ctx, int *list_len, int *opened, void *stream);
 /* kick-drift with the context's dt and dampening */
 int nbx_integrate(nbx_ctx *ctx, const nbx_state *s, void *stream);
 /* nsteps x (build, forces, integrate).  One step is launched kernel by kernel;

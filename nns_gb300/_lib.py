@@ -74,6 +74,9 @@ SIGNATURES = {
     "nbx_set_tuning": (_I, [_P, _I, _I]),
     "nbx_set_multipole": (_I, [_P, _I]),
     "nbx_set_leaf_size": (_I, [_P, _I]),
+    "nbx_group_count": (_I, [_P, _P]),
+    "nbx_forces_groups": (_I, [_P, _P, _I, _I, _P]),
+    "nbx_export_group_stats": (_I, [_P, _P, _P, _P]),
     "nbx_set_systems": (_I, [_P, _I, C.POINTER(C.c_int64)]),
     "nbx_build": (_I, [_P, C.POINTER(nbx_state), _P]),
     "nbx_forces": (_I, [_P, C.POINTER(nbx_state), _P]),

@@ -136,6 +136,27 @@ class Context:
     def forces(self, s: "State", stream=None):
         check(lib().nbx_forces(self.h, C.byref(s.c), _stream_ptr(stream)), "nbx_forces", self.h)
 
+    def group_count(self) -> int:
+        """Walk groups (up to 32 consecutive sorted bodies of one system)."""
+        g = C.c_int()
+        check(lib().nbx_group_count(self.h, C.byref(g)), "nbx_group_count", self.h)
+        return g.value
+
+    def forces_groups(self, s: "State", first: int, count: int, stream=None):
+        """The walk of groups [first, first + count) only (a rank's share of a
+        split system); other bodies' accelerations are left as they were."""
+        check(lib().nbx_forces_groups(self.h, C.byref(s.c), int(first), int(count), _stream_ptr(stream)),
+              "nbx_forces_groups", self.h)
+
+    def group_stats(self, stream=None):
+        """Per-group list length and opened cells of the last walk (int32 tensors on the device)."""
+        ng = self.group_count()
+        ln = torch.empty(max(ng, 1), dtype=torch.int32, device=self.device)
+        op = torch.empty(max(ng, 1), dtype=torch.int32, device=self.device)
+        check(lib().nbx_export_group_stats(self.h, _ptr(ln), _ptr(op), _stream_ptr(stream)),
+              "nbx_export_group_stats", self.h)
+        return ln[:ng], op[:ng]
+
     def integrate(self, s: "State", stream=None):
         check(lib().nbx_integrate(self.h, C.byref(s.c), _stream_ptr(stream)), "nbx_integrate",
               self.h)

@@ -72,6 +72,14 @@ __global__ void k_expand_gstat(const int2 *gstat, const int *groups, int ngroups
     if (nopen) nopen[ob] = v.y;
 }
 
+__global__ void k_split_gstat(const int2 *gstat, int ngroups, int *list_len, int *opened) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ngroups) return;
+    const int2 v = gstat[g];
+    if (list_len) list_len[g] = v.x;
+    if (opened) opened[g] = v.y;
+}
+
 __global__ void k_depth0_from_ptrs(const float *minX, const float *maxX, float theta_ref, float *depth0) {
     if (threadIdx.x == 0) {
         float r = __fmul_rn(__fsub_rn(*maxX, *minX), 0.5f);
@@ -591,6 +599,32 @@ int nbx_forces(nbx_ctx *c, const nbx_state *s, void *stream) {
     if (!c || !s || !s->ax || !s->ay || !s->az) return NBX_ERR_ARG;
     Range r("nbx_forces");
     return nbx::walk_forces(C(c), s, S(stream));
+}
+
+int nbx_group_count(nbx_ctx *c, int *ngroups) {
+    if (!c || !ngroups) return NBX_ERR_ARG;
+    *ngroups = C(c)->ngroups;
+    return NBX_OK;
+}
+
+int nbx_forces_groups(nbx_ctx *c, const nbx_state *s, int first_group, int ngroups, void *stream) {
+    if (!c || !s || !s->ax || !s->ay || !s->az) return NBX_ERR_ARG;
+    Range r("nbx_forces_groups");
+    return nbx::walk_forces_groups(C(c), s, first_group, ngroups, S(stream));
+}
+
+int nbx_export_group_stats(nbx_ctx *c, int *list_len, int *opened, void *stream) {
+    if (!c) return NBX_ERR_ARG;
+    Ctx *ctx = C(c);
+    if (!ctx->built) return NBX_ERR_STATE;
+    if ((list_len || opened) && ctx->ngroups > 0) {
+        nbx::k_split_gstat<<<nbx::ceil_div(ctx->ngroups, 256), 256, 0, S(stream)>>>(ctx->d_gstat, ctx->ngroups, list_len,
+                                                                                  opened);
+        ++ctx->launches;
+        NBX_CUDA(cudaGetLastError());
+    }
+    NBX_CUDA(cudaStreamSynchronize(S(stream)));
+    return NBX_OK;
 }
 
 int nbx_integrate(nbx_ctx *c, const nbx_state *s, void *stream) {

@@ -204,6 +204,7 @@ int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox
 // walk.cu
 int walk_init(Ctx *ctx);
 int walk_forces(Ctx *ctx, const nbx_state *s, cudaStream_t st);
+int walk_forces_groups(Ctx *ctx, const nbx_state *s, int first, int count, cudaStream_t st);
 int walk_potential(Ctx *ctx, const nbx_state *s, float *pot, cudaStream_t st);
 int walk_fp64_lists(Ctx *ctx, const int *group_starts, int ngroups, double *a64, cudaStream_t st);
 // integrate.cu

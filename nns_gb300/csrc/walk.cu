@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32)
 }  // namespace
 
 int walk2_init(Ctx *ctx);
-int walk2_forces(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st);
+int walk2_forces(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st, int g0 = 0, int gn = -1);
 
 int walk_init(Ctx *ctx) {
     // the attribute is per kernel, not per context: allow the device maximum
@@ -227,6 +227,19 @@ int walk_init(Ctx *ctx) {
 int walk_potential(Ctx *ctx, const nbx_state *s, float *pot, cudaStream_t st) {
     if (!ctx->built) return NBX_ERR_STATE;
     return walk2_forces(ctx, s, pot, ctx->walk_warps, st);
+}
+
+// A rank's share of a system split over several GPUs: the walk of groups
+// [first, first + count) only (production walk variants).
+int walk_forces_groups(Ctx *ctx, const nbx_state *s, int first, int count, cudaStream_t st) {
+    if (!ctx->built) return NBX_ERR_STATE;
+    if (first < 0 || count < 0 || first > ctx->ngroups || count > ctx->ngroups - first) return NBX_ERR_ARG;
+    if (ctx->walk_variant == 2) {
+        ctx->last_error = "walk of a group range: the one-cell walk (variant 2) walks all groups";
+        return NBX_ERR_ARG;
+    }
+    if (count == 0) return NBX_OK;
+    return walk2_forces(ctx, s, nullptr, ctx->walk_warps, st, first, count);
 }
 
 int walk_forces(Ctx *ctx, const nbx_state *s, cudaStream_t st) {

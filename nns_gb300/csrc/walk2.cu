@@ -588,7 +588,8 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
 
 template <int CB, int Mode, bool Pot, bool Rec = false, bool Quad = false>
 int launch(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st, int *rec_list = nullptr,
-           int *rec_len = nullptr, int rec_cap = 0) {
+           int *rec_len = nullptr, int rec_cap = 0, int g_first = 0, int g_count = -1) {
+    if (g_count < 0) g_count = ctx->ngroups - g_first;
     const int cap = ctx->p.stack_depth;
     const size_t smem = (size_t)warps * (sizeof(WarpBuf<CB>) + (Quad ? sizeof(QuadBuf<CB>) : 0) +
                                          (size_t)cap * sizeof(int));
@@ -596,7 +597,7 @@ int launch(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st,
         ctx->last_error = "walk: stack_depth too large for the launch shape's shared memory";
         return NBX_ERR_ARG;
     }
-    const int blocks_needed = ceil_div(ctx->ngroups, warps);
+    const int blocks_needed = ceil_div(g_count, warps);
     int per_sm = 1;
     NBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk2<CB, Mode, Pot, Rec, Quad>, warps * 32,
                                                            smem));
@@ -605,9 +606,10 @@ int launch(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st,
     if (grid <= 0) return NBX_OK;
     NBX_CUDA(cudaMemsetAsync(&ctx->d_status->walk_next, 0, sizeof(unsigned), st));
     k_walk2<CB, Mode, Pot, Rec, Quad><<<grid, warps * 32, smem, st>>>(
-        ctx->d_node4, ctx->d_meta, ctx->d_lvl8, ctx->d_quad4, ctx->d_quad2, ctx->d_body4, ctx->d_val, ctx->d_groups, ctx->ngroups, ctx->d_body_sys,
-        ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first, ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay, s->az,
-        pot, ctx->d_gstat, ctx->d_status, rec_list, rec_len, rec_cap);
+        ctx->d_node4, ctx->d_meta, ctx->d_lvl8, ctx->d_quad4, ctx->d_quad2, ctx->d_body4, ctx->d_val,
+        ctx->d_groups + g_first, g_count, ctx->d_body_sys, ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first,
+        ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay, s->az, pot, ctx->d_gstat + g_first, ctx->d_status, rec_list,
+        rec_len, rec_cap);
     ++ctx->launches;
     NBX_CUDA(cudaGetLastError());
     return NBX_OK;
@@ -621,20 +623,20 @@ int set_attr(Ctx *ctx, int smem_max) {
 }
 
 template <int CB>
-int forces_cb(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st) {
-    if (pot) return launch<CB, 0, true>(ctx, s, pot, warps, st);
+int forces_cb(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st, int g0, int gn) {
+    if (pot) return launch<CB, 0, true>(ctx, s, pot, warps, st, nullptr, nullptr, 0, g0, gn);
     if (ctx->multipole) {
         if (!ctx->d_quad4) return NBX_ERR_STATE;
         switch (ctx->compensated) {
-            case 1: return launch<CB, 1, false, false, true>(ctx, s, nullptr, warps, st);
-            case 2: return launch<CB, 2, false, false, true>(ctx, s, nullptr, warps, st);
-            default: return launch<CB, 0, false, false, true>(ctx, s, nullptr, warps, st);
+            case 1: return launch<CB, 1, false, false, true>(ctx, s, nullptr, warps, st, nullptr, nullptr, 0, g0, gn);
+            case 2: return launch<CB, 2, false, false, true>(ctx, s, nullptr, warps, st, nullptr, nullptr, 0, g0, gn);
+            default: return launch<CB, 0, false, false, true>(ctx, s, nullptr, warps, st, nullptr, nullptr, 0, g0, gn);
         }
     }
     switch (ctx->compensated) {
-        case 1: return launch<CB, 1, false>(ctx, s, nullptr, warps, st);
-        case 2: return launch<CB, 2, false>(ctx, s, nullptr, warps, st);
-        default: return launch<CB, 0, false>(ctx, s, nullptr, warps, st);
+        case 1: return launch<CB, 1, false>(ctx, s, nullptr, warps, st, nullptr, nullptr, 0, g0, gn);
+        case 2: return launch<CB, 2, false>(ctx, s, nullptr, warps, st, nullptr, nullptr, 0, g0, gn);
+        default: return launch<CB, 0, false>(ctx, s, nullptr, warps, st, nullptr, nullptr, 0, g0, gn);
     }
 }
 
@@ -680,11 +682,12 @@ int walk2_unrecorded(Ctx *ctx, const nbx_state *s, cudaStream_t st) {
     return launch<96, 0, false, false>(ctx, s, nullptr, ctx->walk_warps, st, nullptr, nullptr, 0);
 }
 
-// variant 0: 64-slot candidate buffers; 1: 128-slot buffers (<= 8 warps); 3: 96-slot buffers
-int walk2_forces(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st) {
-    if (ctx->walk_variant == 1) return forces_cb<128>(ctx, s, pot, warps > 8 ? 8 : warps, st);
-    if (ctx->walk_variant == 3) return forces_cb<96>(ctx, s, pot, warps, st);
-    return forces_cb<64>(ctx, s, pot, warps, st);
+// variant 0: 64-slot candidate buffers; 1: 128-slot buffers (<= 8 warps); 3: 96-slot buffers.
+// Walk groups [g0, g0 + gn) of the last build (gn < 0: all groups from g0).
+int walk2_forces(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st, int g0, int gn) {
+    if (ctx->walk_variant == 1) return forces_cb<128>(ctx, s, pot, warps > 8 ? 8 : warps, st, g0, gn);
+    if (ctx->walk_variant == 3) return forces_cb<96>(ctx, s, pot, warps, st, g0, gn);
+    return forces_cb<64>(ctx, s, pot, warps, st, g0, gn);
 }
 
 }  // namespace nbx
