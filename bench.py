@@ -378,22 +378,24 @@ def bench_hilbert(args, local, b, targets, acc64, tune) -> dict:
 
 
 ACCURACY_TARGET = 1e-4
-ACCURACY_THETAS = {0: (0.4, 0.3, 0.25, 0.2, 0.15, 0.125, 0.1),
-                   1: (0.7, 0.65, 0.6, 0.55, 0.5, 0.45, 0.4, 0.35, 0.3)}
+ACCURACY_THETAS = {(0, 0): (0.4, 0.3, 0.25, 0.2, 0.15, 0.125, 0.1),
+                   (1, 0): (0.7, 0.65, 0.6, 0.55, 0.5, 0.45, 0.4, 0.35, 0.3),
+                   (1, 1): (0.55, 0.5, 0.45, 0.4, 0.35, 0.3)}
 
 
-def bench_accuracy(args, local, b, targets, acc64, tune, multipole=0) -> dict:
+def bench_accuracy(args, local, b, targets, acc64, tune, multipole=0, key_order=0) -> dict:
     """The same workload at smaller opening angles, until the median force error
     against the FP64 direct sum reaches 1e-4 (the headline's theta 0.5 meets
     1e-4 only as FP32 arithmetic error of its own lists).  multipole 0: the
     parity-mode walk (monopoles, the reference's MAC with theta_ref = theta^2);
-    1: the same lists with cell quadrupoles.  Per theta the error on the same
-    8192 targets, then plain FP32 steps timed with CUDA events after one
-    warm-up step."""
+    1: the same lists with cell quadrupoles; key_order 1: Hilbert order (compact
+    walk groups, other lists).  Per theta the error on the same 8192 targets,
+    then plain FP32 steps timed with CUDA events after one warm-up step."""
     import torch
     from nns_gb300.barnes_hut import Context, State
     n = len(b.x)
-    ctx = Context(max_bodies=n, theta=THETA, eps=EPS, dt=DT, device=local, multipole=multipole)
+    ctx = Context(max_bodies=n, theta=THETA, eps=EPS, dt=DT, device=local, multipole=multipole,
+                  key_order=key_order)
     ctx.set_systems([0, n])
     walk = None
     if multipole:
@@ -406,7 +408,7 @@ def bench_accuracy(args, local, b, targets, acc64, tune, multipole=0) -> dict:
         ctx.set_walk(tune["warps"], tune["variant"])
     _, eps2 = ctx.constants()
     points, at_target = [], None
-    for th in ACCURACY_THETAS[multipole]:
+    for th in ACCURACY_THETAS[(multipole, key_order)]:
         ctx.set_constants(float(np.float32(th) * np.float32(th)), eps2, 0)
         s = State.from_bodies(b, device="cuda:%d" % local)
         ctx.build(s)
@@ -440,10 +442,13 @@ def bench_accuracy(args, local, b, targets, acc64, tune, multipole=0) -> dict:
             break
     kind = ("parity-mode walk (monopoles, the reference MAC)" if multipole == 0 else
             "quadrupole mode (the reference MAC and lists, plus cell quadrupoles; not the parity mode)")
-    return {"multipole": multipole, "target_median": ACCURACY_TARGET, "points": points, "at_target": at_target,
+    if key_order:
+        kind += ", Hilbert key order (other walk groups and lists)"
+    return {"multipole": multipole, "key_order": key_order, "target_median": ACCURACY_TARGET, "points": points,
+            "at_target": at_target,
             "walk_config": walk,
             "note": "%s; the first theta in %s whose median error meets the target"
-                    % (kind, list(ACCURACY_THETAS[multipole]))}
+                    % (kind, list(ACCURACY_THETAS[(multipole, key_order)]))}
 
 
 LEAF_SIZES = (1, 2, 4, 8)
@@ -508,12 +513,12 @@ def ctx_variant(tune):
     return tune["variant"] if tune and "variant" in tune else 3
 
 
-def error_target(errs, errs32, accuracy, accuracy_quad) -> dict:
+def error_target(errs, errs32, accuracy, accuracy_quad, accuracy_quad_h=None) -> dict:
     """Which reading of the metric's 1e-4 force error the headline meets: the FP32
     arithmetic error against an FP64 evaluation of the same interaction lists
     (met), and the total error against the FP64 direct sum (not at theta 0.5;
     the accuracy sections give the steps/s at the theta that meets it, with
-    monopoles and with quadrupoles)."""
+    monopoles, with quadrupoles, and with quadrupoles in Hilbert order)."""
     def at_target(acc):
         at = acc.get("at_target") if isinstance(acc, dict) else None
         return None if at is None else {"theta": at["theta"], "median": at["force_error_vs_fp64_direct"]["median"],
@@ -529,7 +534,8 @@ def error_target(errs, errs32, accuracy, accuracy_quad) -> dict:
                                "compensated": errs["compensated"]["median"],
                                "met": bool(errs["plain"]["median"] <= ACCURACY_TARGET)},
             "vs_fp64_direct_at_target": at_target(accuracy),
-            "vs_fp64_direct_at_target_quadrupole": at_target(accuracy_quad)}
+            "vs_fp64_direct_at_target_quadrupole": at_target(accuracy_quad),
+            "vs_fp64_direct_at_target_quadrupole_hilbert": at_target(accuracy_quad_h)}
 
 
 def _section(fn, *a):
@@ -838,13 +844,16 @@ def main():
     batched = None
     del ctx, s
     torch.cuda.empty_cache()
-    accuracy = accuracy_quad = None
+    accuracy = accuracy_quad = accuracy_quad_h = None
     if not args.no_accuracy:
         accuracy = _section(bench_accuracy, args, local, b, targets, acc64,
                             tune if tune and "warps" in tune else None, 0)
         torch.cuda.empty_cache()
         accuracy_quad = _section(bench_accuracy, args, local, b, targets, acc64,
                                  tune if tune and "warps" in tune else None, 1)
+        torch.cuda.empty_cache()
+        accuracy_quad_h = _section(bench_accuracy, args, local, b, targets, acc64,
+                                   tune if tune and "warps" in tune else None, 1, 1)
         torch.cuda.empty_cache()
     buckets = None
     if not args.no_buckets:
@@ -887,9 +896,10 @@ def main():
                         "ratio_to_plain_time": round(ms_comp / ms_plain, 4)},
         "force_error_vs_fp64_direct": errs,
         "fp32_error_vs_fp64_same_lists": errs32,
-        "error_target": error_target(errs, errs32, accuracy, accuracy_quad),
+        "error_target": error_target(errs, errs32, accuracy, accuracy_quad, accuracy_quad_h),
         "accuracy": accuracy,
         "accuracy_quadrupole": accuracy_quad,
+        "accuracy_quadrupole_hilbert": accuracy_quad_h,
         "frame": frame,
         "energy_drift": energy,
         "interactions_per_step": inter_per_step,

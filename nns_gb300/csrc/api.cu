@@ -101,7 +101,7 @@ int dmalloc(Ctx *ctx, T **p, size_t count) {
 
 void free_all(Ctx *ctx) {
     void *ptrs[] = {ctx->d_sys_off, ctx->d_body_sys, ctx->d_tiles, ctx->d_sys_tiles, ctx->d_groups,
-                    ctx->d_bbox_u, ctx->d_bbox, ctx->d_bbox64, ctx->d_depth0, ctx->d_root_first,
+                    ctx->d_bbox_u, ctx->d_bbox, ctx->d_bbox64, ctx->d_depth0, ctx->d_root_first, ctx->d_sys_lvl,
                     ctx->d_root_nch, ctx->d_key, ctx->d_key_alt, ctx->d_key_lo, ctx->d_val, ctx->d_val_alt,
                     ctx->d_body4, ctx->d_delta, ctx->d_bucket, ctx->d_ecount, ctx->d_body_node, ctx->d_gstat,
                     ctx->d_ent, ctx->d_ent_alt, ctx->d_flags, ctx->d_node4, ctx->d_meta, ctx->d_parent,
@@ -288,6 +288,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     rc |= nbx::dmalloc(ctx, &ctx->d_depth0, Ss);
     rc |= nbx::dmalloc(ctx, &ctx->d_root_first, Ss);
     rc |= nbx::dmalloc(ctx, &ctx->d_root_nch, Ss);
+    rc |= nbx::dmalloc(ctx, &ctx->d_sys_lvl, Ss);
     rc |= nbx::dmalloc(ctx, &ctx->d_key, B);
     rc |= nbx::dmalloc(ctx, &ctx->d_key_alt, B);
     rc |= nbx::dmalloc(ctx, &ctx->d_key_lo, B);

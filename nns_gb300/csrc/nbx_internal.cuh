@@ -88,6 +88,7 @@ struct Ctx {
     float *d_depth0 = nullptr;      // [S]
     int *d_root_first = nullptr;    // [S]
     int *d_root_nch = nullptr;      // [S]
+    int *d_sys_lvl = nullptr;       // [S] deepest node level of each system's tree (last build)
 
     // per body
     unsigned long long *d_key = nullptr, *d_key_alt = nullptr;  // [B]

@@ -39,9 +39,10 @@ constexpr int kMomentsUpMaxBodies = NBX_MOMENTS_UP_MAX;  // one-launch moments u
 __device__ __forceinline__ int grid_stride_start() { return blockIdx.x * blockDim.x + threadIdx.x; }
 __device__ __forceinline__ int grid_stride() { return gridDim.x * blockDim.x; }
 
-__global__ void k_step_reset(unsigned *bbox_u, int nsys, DevStatus *st) {
+__global__ void k_step_reset(unsigned *bbox_u, int nsys, DevStatus *st, int *sys_lvl) {
     int i = grid_stride_start();
     if (i < 6 * nsys) bbox_u[i] = f2ord(0.0f);  // Kernels.cu:56-62: the box contains the origin
+    if (i < nsys) sys_lvl[i] = 0;
     if (i == 0) {
         st->refined_runs = 0;
         st->max_level = 0;
@@ -260,7 +261,8 @@ __global__ void __launch_bounds__(kBlock) k_delta(const float4 *__restrict__ pos
                                                    const unsigned long long *__restrict__ key_lo,
                                                    const int *__restrict__ val, float4 *__restrict__ body4,
                                                    unsigned char *__restrict__ delta,
-                                                   unsigned *__restrict__ ecount, DevStatus *st) {
+                                                   unsigned *__restrict__ ecount, DevStatus *st,
+                                                   int *__restrict__ sys_lvl) {
     int lvl_max = 0;
     for (int p = grid_stride_start(); p < n; p += grid_stride()) {
         const int s = body_sys[p];
@@ -270,7 +272,11 @@ __global__ void __launch_bounds__(kBlock) k_delta(const float4 *__restrict__ pos
         delta[p] = (unsigned char)di;
         ecount[p] = (unsigned)((di > dp ? di - dp : 0) + 1);
         body4[p] = pos4[val[p]];
-        lvl_max = max(lvl_max, max(di, dp) + 1);
+        const int lv = max(di, dp) + 1;
+        lvl_max = max(lvl_max, lv);
+        // each system's deepest level (the walk's depth-first reserve of its
+        // groups); the L2 read skips the atomic for all but the few new maxima
+        if (lv > __ldcg(&sys_lvl[s])) atomicMax(&sys_lvl[s], lv);
     }
     lvl_max = __reduce_max_sync(0xffffffffu, lvl_max);
     if ((threadIdx.x & 31) == 0 && lvl_max > 0) atomicMax(&st->max_level, lvl_max);
@@ -670,7 +676,7 @@ int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox
     const int S = ctx->nsys;
     if (n <= 0 || S <= 0) return NBX_ERR_STATE;
     const int gb = ceil_div(n, kBlock) < ctx->nsm * 8 ? ceil_div(n, kBlock) : ctx->nsm * 8;
-    k_step_reset<<<ceil_div(6 * S + 1, kBlock), kBlock, 0, st>>>(ctx->d_bbox_u, S, ctx->d_status);
+    k_step_reset<<<ceil_div(6 * S + 1, kBlock), kBlock, 0, st>>>(ctx->d_bbox_u, S, ctx->d_status, ctx->d_sys_lvl);
     ++ctx->launches;
     if (!external_bbox) {
         k_bbox<<<ctx->ntiles_body, kBlock, 0, st>>>(s->x, s->y, s->z, ctx->d_tiles, ctx->ntiles_body,
@@ -700,7 +706,7 @@ int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox
     ++ctx->launches;
     k_delta<<<gb, kBlock, 0, st>>>(pos4, ctx->d_body_sys, ctx->d_sys_off, n, ctx->d_key,
                                    ctx->d_key_lo, ctx->d_val, ctx->d_body4, ctx->d_delta, ctx->d_ecount,
-                                   ctx->d_status);
+                                   ctx->d_status, ctx->d_sys_lvl);
     ++ctx->launches;
     const unsigned char *bucket = ctx->leaf_size > 1 ? ctx->d_bucket : nullptr;
     if (bucket) {

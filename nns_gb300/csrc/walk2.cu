@@ -19,9 +19,9 @@
 //            buffer takes one warp vote (dp <= r on every lane) and is
 //            accumulated or pushed.
 // Wide rounds run while the stack keeps a depth-first reserve free (7 entries
-// per level); beyond that the walk pops one cell per round, which can never
-// outgrow the reserve, so a stack of at least kDfsReserve + 7*8 entries cannot
-// overflow (NBX_ERR_STACK otherwise).
+// per level of the group's system's deepest level); beyond that the walk pops
+// one cell per round, which can never outgrow the reserve, so a stack of at
+// least kDfsReserve + 7*8 entries cannot overflow (NBX_ERR_STACK otherwise).
 //
 // Accumulation modes: 0 plain FP32 (two packed partial sums), 1 split
 // compensation (plain FP32 within a round, Kahan across rounds), 2 Kahan on
@@ -189,7 +189,8 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             const float4 *__restrict__ quad4, const float2 *__restrict__ quad2, const float4 *__restrict__ body4,
             const int *__restrict__ val, const int *__restrict__ groups, int ngroups,
             const int *__restrict__ body_sys, const int *__restrict__ sys_off, const float *__restrict__ depth0,
-            const int *__restrict__ root_first, const int *__restrict__ root_nch, float eps2, int stack_cap,
+            const int *__restrict__ root_first, const int *__restrict__ root_nch, const int *__restrict__ sys_lvl,
+            float eps2, int stack_cap,
             float *__restrict__ ax, float *__restrict__ ay, float *__restrict__ az, float *__restrict__ pot,
             int2 *__restrict__ gstat, DevStatus *st, int *__restrict__ rec_list,
             int *__restrict__ rec_len, int rec_cap) {
@@ -205,7 +206,6 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
     const unsigned lt = (1u << lane) - 1u;
     const u64 eps2x2 = pk(eps2, eps2);
     unsigned long long tot_len = 0ull, tot_open = 0ull, tot_rounds = 0ull, tot_cand = 0ull;
-    const int reserve = 7 * min(max(st->max_level, 1), 42) + 8;
 
     // groups are handed out dynamically (costs vary widely between groups)
     for (;;) {
@@ -216,6 +216,9 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
         const int p0 = groups[g];
         const int s = body_sys[p0];
         const int end = min(sys_off[s + 1], p0 + 32);
+        // the depth-first reserve from this system's own tree, so that a system's
+        // rounds (and force sums) do not depend on the other systems of a batch
+        const int reserve = 7 * min(max(sys_lvl[s], 1), 42) + 8;
         const int p = p0 + lane;
         const bool valid = p < end;
         // lanes past the end of the system take lane 0's body: their MAC votes
@@ -608,7 +611,7 @@ int launch(Ctx *ctx, const nbx_state *s, float *pot, int warps, cudaStream_t st,
     k_walk2<CB, Mode, Pot, Rec, Quad><<<grid, warps * 32, smem, st>>>(
         ctx->d_node4, ctx->d_meta, ctx->d_lvl8, ctx->d_quad4, ctx->d_quad2, ctx->d_body4, ctx->d_val,
         ctx->d_groups + g_first, g_count, ctx->d_body_sys, ctx->d_sys_off, ctx->d_depth0, ctx->d_root_first,
-        ctx->d_root_nch, ctx->eps2, cap, s->ax, s->ay, s->az, pot, ctx->d_gstat + g_first, ctx->d_status, rec_list,
+        ctx->d_root_nch, ctx->d_sys_lvl, ctx->eps2, cap, s->ax, s->ay, s->az, pot, ctx->d_gstat + g_first, ctx->d_status, rec_list,
         rec_len, rec_cap);
     ++ctx->launches;
     NBX_CUDA(cudaGetLastError());

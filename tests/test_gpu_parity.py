@@ -213,6 +213,39 @@ def test_batched_equals_unbatched(cuda):
             assert np.array_equal(t1[k], tb[k]), (i, k)
 
 
+@pytest.mark.parametrize("stack_depth", [384, 512])
+def test_batched_equals_unbatched_with_a_deep_system(cuda, stack_depth):
+    """A system whose tree reaches level 39 batched with shallow ones: every
+    system's walk keeps the depth-first reserve of its own tree, so each system's
+    forces equal its single-system run bit for bit (with the reserve of the
+    deepest system of the batch, the shallow systems' rounds and hence their
+    force sums would depend on their neighbours in the batch)."""
+    from adversarial import CASES
+    parts = [ic.star_disk(30000, seed=ic.SEED0 + 90), CASES["deep"](), ic.plummer(40000, seed=ic.SEED0 + 91),
+             ic.binary_disk(20000, seed=ic.SEED0 + 92)]
+    sizes = [len(p.x) for p in parts]
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    cat = lambda k: np.concatenate([getattr(p, k) for p in parts])  # noqa: E731
+    B = ic.Bodies(cat("x"), cat("y"), cat("z"), cat("vx"), cat("vy"), cat("vz"), cat("m"))
+    ctx = _ctx(int(off[-1]), nsys=len(sizes), theta=0.5, eps=0.001, stack_depth=stack_depth)
+    ctx.set_systems(off)
+    s = _state(B)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    accb = s.acc()
+    assert ctx.tree_info()["max_level"] > 30
+    for i, p in enumerate(parts):
+        n = len(p.x)
+        c1 = _ctx(n, theta=0.5, eps=0.001, stack_depth=stack_depth)
+        c1.set_systems([0, n])
+        s1 = _state(p)
+        c1.build(s1)
+        c1.forces(s1)
+        c1.sync()
+        assert np.array_equal(accb[off[i]:off[i + 1]], s1.acc()), i
+
+
 def test_radix_width_gives_the_same_trees(cuda):
     """9-bit digits (7 passes, the keys generated into the alternate buffers)
     against 8-bit digits (8 passes): single systems of odd and ragged sizes and a
