@@ -10,9 +10,11 @@
 //   scan            one exclusive scan over the whole count array: because the
 //                   layout is segment-major, digit-major, tile-minor, the scan
 //                   value IS the absolute output offset of (segment, digit, tile)
-//   k_radix_scatter per-tile stable ranks (warp match + per-warp running
-//                   counters) into a shared-memory copy of the tile in output
-//                   order, then coalesced runs per digit.
+//   k_radix_scatter per-tile stable ranks (the lanes sharing a digit from bit
+//                   ballots, plus per-warp running counters) into a
+//                   shared-memory copy of the tile in output order, then
+//                   coalesced runs per digit; the next keys' loads are in
+//                   flight while the current ones are ranked.
 // Segments are the independent systems of a batch, so one launch sorts every
 // system's keys inside its own range; a single system is one segment.
 #include "nbx_internal.cuh"
@@ -22,6 +24,9 @@ namespace nbx {
 namespace {
 
 constexpr int kWarpsPerBlock = 8;
+#ifndef NBX_RADIX_MATCH
+#define NBX_RADIX_MATCH 0  // 1: rank digits with match.any instead of bit ballots
+#endif
 
 struct TileMap {
     // segmented mode
@@ -84,7 +89,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 }
 
 // Scatter with the tile staged in shared memory in output order: every lane
-// ranks its key stably (warp match + running per-digit counters), writes it to
+// ranks its key stably (digit peers + running per-digit counters), writes it to
 // its tile-local sorted position, and the warp then streams the staged tile
 // out so that each digit's run is written by consecutive lanes to consecutive
 // addresses (coalesced, instead of one sector per key).  The tile's count of a
@@ -155,16 +160,23 @@ __global__ void __launch_bounds__(kScatterWarps * 32)
     }
     __syncwarp();
     const unsigned lt = (1u << lane) - 1u;
-    constexpr int kBatch = 8;  // rounds whose loads are in flight together
-    for (int j0 = 0; j0 < len; j0 += 32 * kBatch) {
-        K kk[kBatch];
-        V vv[kBatch];
+    // Two groups of kBatch rounds of 32 keys: the loads of the next group are in
+    // flight while the current group is ranked, so a warp keeps 2 x 8 x 32 keys
+    // and values moving (the ranking is a chain of shared-memory round trips and
+    // would otherwise leave the loads idle).
+    constexpr int kBatch = 8;
+    constexpr int kGroup = 32 * kBatch;
+    K ka[kBatch], kb[kBatch];
+    V va[kBatch], vb[kBatch];
+    auto load = [&](K *kk, V *vv, int j0) {
 #pragma unroll
         for (int u = 0; u < kBatch; u++) {
             const int i = j0 + u * 32 + lane;
             kk[u] = i < len ? key_in[start + i] : K(0);
             if (val_in) vv[u] = i < len ? val_in[start + i] : V(0);
         }
+    };
+    auto rank = [&](const K *kk, const V *vv, int j0) {
 #pragma unroll
         for (int u = 0; u < kBatch; u++) {
             const int j = j0 + u * 32;
@@ -172,17 +184,38 @@ __global__ void __launch_bounds__(kScatterWarps * 32)
             const bool valid = j + lane < len;
             const K k = kk[u];
             const unsigned d = valid ? ((unsigned)(k >> shift) & kMask) : ((unsigned)kBins + lane);
+#if NBX_RADIX_MATCH
             const unsigned peers = __match_any_sync(0xffffffffu, d);
-            const unsigned rank = __popc(peers & lt);
+#else
+            // the lanes with this lane's digit: the AND over the digit's bits of
+            // the ballot of lanes agreeing on that bit (invalid lanes carry
+            // digits >= kBins, which no valid digit matches)
+            unsigned peers = 0xffffffffu;
+#pragma unroll
+            for (int b = 0; b <= Bits; b++) {
+                const unsigned on = __ballot_sync(0xffffffffu, (d >> b) & 1u);
+                peers &= ((d >> b) & 1u) ? on : ~on;
+            }
+            if (!valid) peers = 1u << lane;  // an invalid lane's digit is unique to it
+#endif
+            const unsigned rnk = __popc(peers & lt);
             const unsigned base = valid ? sg.cnt[d] : 0u;
             __syncwarp();
-            if (valid && rank == 0) sg.cnt[d] = base + __popc(peers);
+            if (valid && rnk == 0) sg.cnt[d] = base + __popc(peers);
             __syncwarp();
             if (valid) {
-                sg.key[base + rank] = k;
-                if (val_in) sg.val[base + rank] = vv[u];
+                sg.key[base + rnk] = k;
+                if (val_in) sg.val[base + rnk] = vv[u];
             }
         }
+    };
+    load(ka, va, 0);
+    for (int j0 = 0; j0 < len; j0 += 2 * kGroup) {
+        if (j0 + kGroup < len) load(kb, vb, j0 + kGroup);
+        rank(ka, va, j0);
+        if (j0 + kGroup >= len) break;
+        if (j0 + 2 * kGroup < len) load(ka, va, j0 + 2 * kGroup);
+        rank(kb, vb, j0 + kGroup);
     }
     __syncwarp();
     for (int j = lane; j < len; j += 32) {
