@@ -175,6 +175,26 @@ __device__ __forceinline__ void accumulate_quad(Sums &a, u64 F, u64 n5, u64 dx, 
     }
 }
 
+// One pair of cells of the quadrupole mode:
+//   a += m d r^-3 - Q d r^-5 + 5/2 (d.Q.d) d r^-7   (d = cell - body),
+// with the cells' quadrupoles from slot pair q of the buffer; `neg` is (-1, -1)
+// for two accepted cells, 0 in a half whose cell is rejected (with its mass
+// zero in mm, the half adds nothing).
+template <int Mode, int CB>
+__device__ __forceinline__ void quad_term(Sums &acc, const QuadBuf<CB> &qbuf, int q, u64 mm, u64 ri, u64 neg, u64 dx,
+                                          u64 dy, u64 dz) {
+    const ulonglong2 QA = qbuf.qa[q], QB = qbuf.qb[q], QC = qbuf.qc[q];
+    const u64 ri2 = mul2(ri, ri);
+    const u64 ri3 = mul2(ri2, ri);
+    const u64 n5 = mul2(mul2(ri3, ri2), neg);
+    const u64 qx = fma2(QC.x, dz, fma2(QB.y, dy, mul2(QA.x, dx)));
+    const u64 qy = fma2(QC.y, dz, fma2(QA.y, dy, mul2(QB.y, dx)));
+    const u64 qz = fma2(QB.x, dz, fma2(QC.y, dy, mul2(QC.x, dx)));
+    const u64 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));
+    const u64 F = fma2(mul2(dqd, mul2(n5, ri2)), pk(-2.5f, -2.5f), mul2(mm, ri3));
+    accumulate_quad<Mode>(acc, F, n5, dx, dy, dz, qx, qy, qz);
+}
+
 // CB = 64 and 96: 64-register budget (two 16-warp or four 8-warp blocks per SM);
 // CB = 128: up to 85 registers for more loads in flight (three 8-warp blocks).
 template <int CB>
@@ -323,7 +343,9 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             }
             const int excl = incl - nch;
             const int cbase = first - excl;  // child t of this lane's cell is node cbase + t
-            int P = __popc(__ballot_sync(0xffffffffu, lane < avail && incl <= kCB - nb));
+            // (the quadrupole mode keeps one slot free: its two cell regions are
+            // padded to whole pairs independently)
+            int P = __popc(__ballot_sync(0xffffffffu, lane < avail && incl <= kCB - nb - (Quad ? 1 : 0)));
             int T = __shfl_sync(0xffffffffu, incl, (P + 31) & 31);
             // the stack grows by at most T - P: wide rounds only while that keeps
             // the depth-first reserve free, else one cell
@@ -355,7 +377,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             //     lane does) is < dp, so the vote would fail: pushed at once;
             //   otherwise it is voted on in the cell buffer.
             // The interaction lists are unchanged; only their order differs.
-            int nbody = nb, ncell = 0, nsrej = 0;
+            int nbody = nb, ncell = 0, nsrej = 0, nacc = 0;
             int jbase = -1;
 #pragma unroll
             for (int k = 0; k < kCB / 32; k++) {
@@ -400,13 +422,24 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                     }
                 }
                 // quadrupole mode: accepted cells need their quadrupoles, so a surely
-                // accepted cell goes to the cell buffer with a threshold that always passes
+                // accepted cell goes to the top of the cell buffer (filled downwards),
+                // evaluated without a vote; the cells to vote on fill it upwards
                 const bool tob = ok && (cm < 0 || (!Quad && isc && sacc));
-                const bool toc = isc && (Quad ? (sacc || !srej) : (!sacc && !srej));
+                const bool toc = isc && !sacc && !srej;
                 const bool tos = isc && !sacc && srej;
+                const bool toa = Quad && isc && sacc;
                 const unsigned bm = __ballot_sync(0xffffffffu, tob);
                 const unsigned cmk = __ballot_sync(0xffffffffu, toc);
                 const unsigned smk = __ballot_sync(0xffffffffu, tos);
+                if (Quad) {
+                    const unsigned amk = __ballot_sync(0xffffffffu, toa);
+                    if (toa) {
+                        const int slot = kCB - 1 - (nacc + __popc(amk & lt));
+                        put4(buf.ca, buf.cb, slot, q);
+                        putq(qbuf.qa, qbuf.qb, qbuf.qc, slot, qq4, qq2);
+                    }
+                    nacc += __popc(amk);
+                }
                 if (tob) {
                     put4(buf.ba, buf.bb, nbody + __popc(bm & lt), q);
                     if (Rec) buf.bid[nbody + __popc(bm & lt)] = c;
@@ -414,7 +447,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 if (toc) {
                     const int slot = ncell + __popc(cmk & lt);
                     put4(buf.ca, buf.cb, slot, q);
-                    reinterpret_cast<float *>(&buf.cd[slot >> 1])[slot & 1] = (Quad && sacc) ? -INFINITY : dpc;
+                    reinterpret_cast<float *>(&buf.cd[slot >> 1])[slot & 1] = dpc;
                     buf.cid[slot] = c;
                     if (Quad) putq(qbuf.qa, qbuf.qb, qbuf.qc, slot, qq4, qq2);
                 }
@@ -431,6 +464,14 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 reinterpret_cast<float *>(&buf.cd[ncell >> 1])[1] = -INFINITY;
                 if (Quad)
                     putq(qbuf.qa, qbuf.qb, qbuf.qc, ncell, make_float4(0.f, 0.f, 0.f, 0.f), make_float2(0.f, 0.f));
+            }
+            // the accepted region [kCB - nacc, kCB) starts on a whole pair: a
+            // massless, quadrupole-free far candidate fills its odd first slot
+            // (ncell + nacc < kCB keeps it clear of the voted region's pad)
+            const int abeg = (kCB - nacc) & ~1;
+            if (Quad && lane == 2 && ((kCB - nacc) & 1)) {
+                put4(buf.ca, buf.cb, abeg, make_float4(1e18f, 1e18f, 1e18f, 0.f));
+                putq(qbuf.qa, qbuf.qb, qbuf.qc, abeg, make_float4(0.f, 0.f, 0.f, 0.f), make_float2(0.f, 0.f));
             }
             __syncwarp();
 
@@ -457,6 +498,24 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 for (int t = lane; t < nbody; t += 32)
                     if (nrec + t < rec_cap) rec[nrec + t] = buf.bid[t];
                 nrec += nbody;
+            }
+            // ---- quadrupole mode: surely accepted cells, no vote
+            if (Quad) {
+#pragma unroll (kCellUnroll)
+                for (int q = abeg >> 1; q < kCB / 2; q++) {
+                    const ulonglong2 A = buf.ca[q];
+                    const ulonglong2 B = buf.cb[q];
+                    const u64 dx = sub2(A.x, px);
+                    const u64 dy = sub2(A.y, py);
+                    const u64 dz = sub2(B.x, pz);
+                    u64 r = fma2(dx, dx, eps2x2);
+                    r = fma2(dy, dy, r);
+                    r = fma2(dz, dz, r);
+                    float ra, rb;
+                    upk(r, ra, rb);
+                    const u64 ri = pk(rsq(ra), rsq(rb));
+                    quad_term<Mode>(acc, qbuf, q, B.y, ri, pk(-1.f, -1.f), dx, dy, dz);
+                }
             }
             // ---- evaluate cells: one vote per cell, accept or push
             const int ncp = (ncell + 1) >> 1;
@@ -491,20 +550,8 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                         const u64 f = mul2(mul2(mul2(mm, ri), ri), ri);
                         accumulate<Mode, Pot>(acc, f, mm, ri, dx, dy, dz);
                     } else {
-                        // a += m d r^-3 - Q d r^-5 + 5/2 (d.Q.d) d r^-7, the rejected
-                        // half of the pair masked through m and r^-5
-                        const ulonglong2 QA = qbuf.qa[q], QB = qbuf.qb[q], QC = qbuf.qc[q];
-                        const u64 ri2 = mul2(ri, ri);
-                        const u64 ri3 = mul2(ri2, ri);
-                        float r5a, r5b;
-                        upk(mul2(ri3, ri2), r5a, r5b);
-                        const u64 n5 = pk(oka ? -r5a : 0.f, okb ? -r5b : 0.f);
-                        const u64 qx = fma2(QC.x, dz, fma2(QB.y, dy, mul2(QA.x, dx)));
-                        const u64 qy = fma2(QC.y, dz, fma2(QA.y, dy, mul2(QB.y, dx)));
-                        const u64 qz = fma2(QB.x, dz, fma2(QC.y, dy, mul2(QC.x, dx)));
-                        const u64 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));
-                        const u64 F = fma2(mul2(dqd, mul2(n5, ri2)), pk(-2.5f, -2.5f), mul2(mm, ri3));
-                        accumulate_quad<Mode>(acc, F, n5, dx, dy, dz, qx, qy, qz);
+                        // the rejected half of the pair masked through m and r^-5
+                        quad_term<Mode>(acc, qbuf, q, mm, ri, pk(oka ? -1.f : 0.f, okb ? -1.f : 0.f), dx, dy, dz);
                     }
                 }
                 if (!oka) {
@@ -524,8 +571,8 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
             }
             top += nrej;
             tot_rounds += 1ull;
-            tot_cand += (unsigned long long)(nbody + ncell + nsrej);
-            len += nbody + ncell - nrej;
+            tot_cand += (unsigned long long)(nbody + ncell + nsrej + nacc);
+            len += nbody + ncell - nrej + nacc;
             opened += nrej + nsrej;
             nb = 0;
             if (Mode == 1) {  // fold this round's partial sums into the compensated totals
