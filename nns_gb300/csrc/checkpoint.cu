@@ -150,15 +150,28 @@ extern "C" int nbx_checkpoint_restore(nbx_ctx *c, nbx_state *s, const void *host
     uint64_t sum;
     std::memcpy(&sum, in + need - sizeof(uint64_t), sizeof(sum));
     if (nbx::payload_sum(payload, (size_t)nbx::kArrays * n) != sum) return NBX_ERR_FORMAT;
+    // settings outside their ranges are a malformed checkpoint: refused before anything changes
+    if (h.multipole < 0 || h.multipole > 1 || h.leaf_size < 1 || h.leaf_size > 8 || h.walk_variant < 0 ||
+        h.walk_variant > 3 || !(h.walk_warps == 4 || h.walk_warps == 8 || h.walk_warps == 16) || h.stack_depth < 360 ||
+        h.stack_depth > 4096 || (h.multipole == 1 && h.walk_variant == 2) || h.compensated < 0 || h.compensated > 2)
+        return NBX_ERR_FORMAT;
     if (n > ctx->cap_bodies || nsys > ctx->cap_sys || h.key_order != ctx->key_order) return NBX_ERR_ARG;
     int rc = nbx_set_systems(c, nsys, off.data());
     if (rc) return rc;
     rc = nbx_set_constants(c, h.theta_ref, h.eps2, h.compensated);
     if (rc) return rc;
-    rc = nbx_set_multipole(c, h.multipole);
-    if (rc) return rc;
+    // the one-cell walk (variant 2) has no quadrupole form: leave quadrupoles
+    // before choosing it, choose the walk before entering them
+    if (h.multipole == 0) {
+        rc = nbx_set_multipole(c, 0);
+        if (rc) return rc;
+    }
     rc = nbx_set_walk_config(c, h.walk_warps, h.walk_variant);
     if (rc) return rc;
+    if (h.multipole != 0) {
+        rc = nbx_set_multipole(c, h.multipole);
+        if (rc) return rc;
+    }
     rc = nbx_set_leaf_size(c, h.leaf_size);
     if (rc) return rc;
     rc = nbx_set_tuning(c, ctx->radix_bits, h.stack_depth);
