@@ -98,6 +98,39 @@ def test_bad_checkpoints_are_refused(cuda):
     assert np.array_equal(s.x.cpu().numpy(), x0)
 
 
+def _fnv1a(data: bytes, h: int = 1469598103934665603) -> int:
+    for b in data:
+        h = ((h ^ b) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+    return h
+
+
+def test_out_of_range_settings_are_refused(cuda):
+    """A checkpoint whose header hash is valid but whose settings are outside
+    their ranges (multipole order 7, here) is malformed: NBX_ERR_FORMAT, and
+    neither the context nor the state changes."""
+    from nns_gb300._lib import NbxError
+    from nns_gb300.barnes_hut import Context, State
+    b = ic.star_disk(2000)
+    ctx = Context(max_bodies=2000, theta=0.5, eps=0.01)
+    ctx.set_systems([0, 2000])
+    s = State.from_bodies(b)
+    buf = ctx.checkpoint(s).copy()
+    # header: magic 8, version 4, nsys 4, nbodies 8, 4 floats, 8 int32 (compensated,
+    # key order, warps, variant, multipole, leaf size, stack depth, reserved), hash 8
+    multipole_at = 8 + 4 + 4 + 8 + 16 + 4 * 4
+    buf[multipole_at:multipole_at + 4] = np.frombuffer(np.int32(7).tobytes(), np.uint8)
+    nsys = int(np.frombuffer(buf[12:16].tobytes(), np.int32)[0])
+    hash_at = 72
+    h = _fnv1a(bytes(buf[80:80 + 8 * (nsys + 1)]), _fnv1a(bytes(buf[:hash_at])))
+    buf[hash_at:hash_at + 8] = np.frombuffer(np.uint64(h).tobytes(), np.uint8)
+    t0 = ctx.constants()
+    s.x.fill_(7.0)
+    with pytest.raises(NbxError) as e:
+        ctx.restore(s, buf)
+    assert e.value.code == 12  # NBX_ERR_FORMAT
+    assert float(s.x[0].item()) == 7.0 and ctx.constants() == t0
+
+
 def test_node_pool_overflow_is_reported(cuda):
     from nns_gb300._lib import NbxError
     from nns_gb300.barnes_hut import Context, State
