@@ -18,10 +18,10 @@ constexpr int kTileMin = 256;     // smallest radix tile (small systems)
 #ifndef NBX_SCATTER_WARPS
 #define NBX_SCATTER_WARPS 4
 #endif
-constexpr int kScatterWarps = NBX_SCATTER_WARPS;  // tiles (warps) per scatter block
+constexpr int kScatterWarps = NBX_SCATTER_WARPS;  // warps of a scatter block (one block per tile)
 
 // Radix tile for n keys: the largest power of two <= kTile that still gives
-// about two scatter blocks per SM, but not below kTileMin.
+// about 2 x kScatterWarps tiles (scatter blocks) per SM, but not below kTileMin.
 inline int tile_for(long long n, int nsm) {
     const long long want = 2ll * nsm * kScatterWarps;
     int t = kTile;

@@ -4,17 +4,17 @@
 // 9-bit digits (nbx_params.radix_bits).  Any digit width gives the same stable
 // order, so the width only trades passes against histogram size.
 //
-// A tile is up to 2048 consecutive keys owned by one warp (smaller for small
-// systems, so that the tiles still fill the GPU).  Per pass:
+// A tile is up to 2048 consecutive keys (smaller for small systems, so that the
+// tiles still fill the GPU).  Per pass:
 //   k_radix_hist    per-tile digit counts, stored [segment][digit][tile]
 //   scan            one exclusive scan over the whole count array: because the
 //                   layout is segment-major, digit-major, tile-minor, the scan
 //                   value IS the absolute output offset of (segment, digit, tile)
-//   k_radix_scatter per-tile stable ranks (the lanes sharing a digit from bit
-//                   ballots, plus per-warp running counters) into a
+//   k_radix_scatter one block per tile: its warps rank quarters of the tile
+//                   stably (digit peers from bit ballots, per-warp running
+//                   counters started from the warps' digit counts) into a
 //                   shared-memory copy of the tile in output order, then
-//                   coalesced runs per digit; the next keys' loads are in
-//                   flight while the current ones are ranked.
+//                   coalesced runs per digit.
 // Segments are the independent systems of a batch, so one launch sorts every
 // system's keys inside its own range; a single system is one segment.
 #include "nbx_internal.cuh"
@@ -88,34 +88,28 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     for (int d = lane; d < kBins; d += 32) hist[hbase + (int64_t)d * hstride] = cnt[w][d];
 }
 
-// Scatter with the tile staged in shared memory in output order: every lane
-// ranks its key stably (digit peers + running per-digit counters), writes it to
-// its tile-local sorted position, and the warp then streams the staged tile
-// out so that each digit's run is written by consecutive lanes to consecutive
-// addresses (coalesced, instead of one sector per key).  The tile's count of a
-// digit is the difference of adjacent entries of the scanned histogram (the
-// layout is tile-minor and the scan is continuous; offs[nh] holds the total).
-// A warp's stage: gbase (output offset of (digit, tile)), lstart (tile-local
-// start of the digit), cnt (running tile-local position), then the tile's keys
-// and values; sized for the launch's tile.
+// Scatter with the tile staged in shared memory in output order.  One block of
+// kScatterWarps warps per tile; warp w takes the w-th quarter (for 4 warps) of
+// the tile's keys, in tile order, into registers:
+//   1. each warp counts its quarter's digits (shared-memory atomics);
+//   2. per digit, the warps' counts become running positions: the digit's
+//      tile-local start plus the counts of the warps before (so the order stays
+//      that of the tile: the sort is stable);
+//   3. each warp ranks its keys batch by batch (the lanes sharing a digit from
+//      bit ballots, rank among them by lane, the leader advances the warp's
+//      counter) and writes them to their tile-local sorted positions;
+//   4. the block streams the staged tile out so that each digit's run is written
+//      by consecutive threads to consecutive addresses (coalesced).
+// The tile's count of a digit is the difference of adjacent entries of the
+// scanned histogram (the layout is tile-minor and the scan is continuous;
+// offs[nh] holds the total).  Shared memory per block: gbase (output offset of
+// (digit, tile)), lstart (tile-local start of the digit), the warps' counters,
+// then the tile's keys and values.
 template <typename K, typename V, int Bits>
 __host__ __device__ constexpr size_t stage_bytes(int tile) {
-    return (3 * (size_t(1) << Bits) * sizeof(unsigned) + (size_t)tile * (sizeof(K) + sizeof(V)) + 15) & ~(size_t)15;
+    return ((2 + kScatterWarps) * (size_t(1) << Bits) * sizeof(unsigned) + (size_t)tile * (sizeof(K) + sizeof(V)) +
+            15) & ~(size_t)15;
 }
-
-template <typename K, typename V, int Bits>
-struct Stage {
-    unsigned *gbase, *lstart, *cnt;
-    K *key;
-    V *val;
-    __device__ Stage(unsigned char *base, int tile) {
-        gbase = reinterpret_cast<unsigned *>(base);
-        lstart = gbase + (1 << Bits);
-        cnt = lstart + (1 << Bits);
-        key = reinterpret_cast<K *>(cnt + (1 << Bits));
-        val = reinterpret_cast<V *>(key + tile);
-    }
-};
 
 template <typename K, typename V, bool Seg, int Bits>
 __global__ void __launch_bounds__(kScatterWarps * 32)
@@ -124,115 +118,127 @@ __global__ void __launch_bounds__(kScatterWarps * 32)
                     const unsigned *__restrict__ offs) {
     constexpr int kBins = 1 << Bits;
     constexpr unsigned kMask = kBins - 1;
-    constexpr int kPer = kBins / 32;  // digits owned by one lane
+    constexpr int kW = kScatterWarps;
+    constexpr int kPer = kBins / 32;                   // digits owned by one lane of warp 0
+    constexpr int kKeys = (kTile + kW * 32 - 1) / (kW * 32);  // keys per lane at the largest tile
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int t = blockIdx.x * kScatterWarps + w;
-    if (t >= tm.ntiles) return;
+    const int t = blockIdx.x;
+    if (t >= tm.ntiles) return;  // uniform over the block
     int start, len, hstride;
     int64_t hbase;
     tile_info<Seg, kBins>(tm, t, start, len, hbase, hstride);
     if (len <= 0) return;
-    Stage<K, V, Bits> sg(smem_raw + (size_t)w * stage_bytes<K, V, Bits>(tm.tile), tm.tile);
-    // lane owns digits kPer*lane .. kPer*lane+kPer-1: counts, then the tile-local starts
-    unsigned c[kPer], sum = 0;
-#pragma unroll
-    for (int k = 0; k < kPer; k++) {
-        const int d = kPer * lane + k;
-        const int64_t idx = hbase + (int64_t)d * hstride;
-        const unsigned g = offs[idx];
-        c[k] = offs[idx + 1] - g;
-        sg.gbase[d] = g;
-        sum += c[k];
-    }
-    unsigned incl = sum;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned u = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += u;
-    }
-    unsigned run = incl - sum;
-#pragma unroll
-    for (int k = 0; k < kPer; k++) {
-        sg.lstart[kPer * lane + k] = run;
-        sg.cnt[kPer * lane + k] = run;
-        run += c[k];
-    }
-    __syncwarp();
+    unsigned *gbase = reinterpret_cast<unsigned *>(smem_raw);
+    unsigned *lstart = gbase + kBins;
+    unsigned *wcnt = lstart + kBins;  // [kW][kBins]
+    K *skey = reinterpret_cast<K *>(wcnt + kW * kBins);
+    V *sval = reinterpret_cast<V *>(skey + tm.tile);
     const unsigned lt = (1u << lane) - 1u;
-    // Two groups of kBatch rounds of 32 keys: the loads of the next group are in
-    // flight while the current group is ranked, so a warp keeps 2 x 8 x 32 keys
-    // and values moving (the ranking is a chain of shared-memory round trips and
-    // would otherwise leave the loads idle).
-    constexpr int kBatch = 8;
-    constexpr int kGroup = 32 * kBatch;
-    K ka[kBatch], kb[kBatch];
-    V va[kBatch], vb[kBatch];
-    auto load = [&](K *kk, V *vv, int j0) {
+
+    // this warp's quarter [q0, q1) of the tile, whole rounds of 32 keys
+    const int quarter = (((len + kW - 1) / kW) + 31) & ~31;
+    const int q0 = min(len, w * quarter), q1 = min(len, q0 + quarter);
+    K kk[kKeys];
+    V vv[kKeys];
 #pragma unroll
-        for (int u = 0; u < kBatch; u++) {
-            const int i = j0 + u * 32 + lane;
-            kk[u] = i < len ? key_in[start + i] : K(0);
-            if (val_in) vv[u] = i < len ? val_in[start + i] : V(0);
-        }
-    };
-    auto rank = [&](const K *kk, const V *vv, int j0) {
-#pragma unroll
-        for (int u = 0; u < kBatch; u++) {
-            const int j = j0 + u * 32;
-            if (j >= len) break;
-            const bool valid = j + lane < len;
-            const K k = kk[u];
-            const unsigned d = valid ? ((unsigned)(k >> shift) & kMask) : ((unsigned)kBins + lane);
-#if NBX_RADIX_MATCH
-            const unsigned peers = __match_any_sync(0xffffffffu, d);
-#else
-            // the lanes with this lane's digit: the AND over the digit's bits of
-            // the ballot of lanes agreeing on that bit (invalid lanes carry
-            // digits >= kBins, which no valid digit matches)
-            unsigned peers = 0xffffffffu;
-#pragma unroll
-            for (int b = 0; b <= Bits; b++) {
-                const unsigned on = __ballot_sync(0xffffffffu, (d >> b) & 1u);
-                peers &= ((d >> b) & 1u) ? on : ~on;
-            }
-            if (!valid) peers = 1u << lane;  // an invalid lane's digit is unique to it
-#endif
-            const unsigned rnk = __popc(peers & lt);
-            const unsigned base = valid ? sg.cnt[d] : 0u;
-            __syncwarp();
-            if (valid && rnk == 0) sg.cnt[d] = base + __popc(peers);
-            __syncwarp();
-            if (valid) {
-                sg.key[base + rnk] = k;
-                if (val_in) sg.val[base + rnk] = vv[u];
-            }
-        }
-    };
-    load(ka, va, 0);
-    for (int j0 = 0; j0 < len; j0 += 2 * kGroup) {
-        if (j0 + kGroup < len) load(kb, vb, j0 + kGroup);
-        rank(ka, va, j0);
-        if (j0 + kGroup >= len) break;
-        if (j0 + 2 * kGroup < len) load(ka, va, j0 + 2 * kGroup);
-        rank(kb, vb, j0 + kGroup);
+    for (int u = 0; u < kKeys; u++) {
+        const int i = q0 + u * 32 + lane;
+        kk[u] = i < q1 ? key_in[start + i] : K(0);
+        if (val_in) vv[u] = i < q1 ? val_in[start + i] : V(0);
     }
-    __syncwarp();
-    for (int j = lane; j < len; j += 32) {
-        const K k = sg.key[j];
+    // the tile's digit counts and starts (warp 0), the warps' counters zeroed
+    if (w == 0) {
+        unsigned c[kPer], sum = 0;
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            const int d = kPer * lane + k;
+            const int64_t idx = hbase + (int64_t)d * hstride;
+            const unsigned g = offs[idx];
+            c[k] = offs[idx + 1] - g;
+            gbase[d] = g;
+            sum += c[k];
+        }
+        unsigned incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
+        }
+        unsigned run = incl - sum;
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            lstart[kPer * lane + k] = run;
+            run += c[k];
+        }
+    }
+    for (int i = threadIdx.x; i < kW * kBins; i += blockDim.x) wcnt[i] = 0u;
+    __syncthreads();
+    // 1. this warp's digit counts
+#pragma unroll
+    for (int u = 0; u < kKeys; u++)
+        if (q0 + u * 32 + lane < q1) atomicAdd(&wcnt[w * kBins + ((unsigned)(kk[u] >> shift) & kMask)], 1u);
+    __syncthreads();
+    // 2. per digit: the warps' starting positions, in tile order
+    for (int d = threadIdx.x; d < kBins; d += blockDim.x) {
+        unsigned run = lstart[d];
+#pragma unroll
+        for (int v = 0; v < kW; v++) {
+            const unsigned c = wcnt[v * kBins + d];
+            wcnt[v * kBins + d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    // 3. stable ranks within the warp, batch by batch
+    unsigned *cnt = wcnt + w * kBins;
+#pragma unroll
+    for (int u = 0; u < kKeys; u++) {
+        if (q0 + u * 32 >= q1) break;  // uniform over the warp
+        const bool valid = q0 + u * 32 + lane < q1;
+        const K k = kk[u];
+        const unsigned d = valid ? ((unsigned)(k >> shift) & kMask) : ((unsigned)kBins + lane);
+#if NBX_RADIX_MATCH
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+#else
+        // the lanes with this lane's digit: the AND over the digit's bits of the
+        // ballot of lanes agreeing on that bit (invalid lanes carry digits >= kBins,
+        // which no valid digit matches)
+        unsigned peers = 0xffffffffu;
+#pragma unroll
+        for (int b = 0; b <= Bits; b++) {
+            const unsigned on = __ballot_sync(0xffffffffu, (d >> b) & 1u);
+            peers &= ((d >> b) & 1u) ? on : ~on;
+        }
+        if (!valid) peers = 1u << lane;
+#endif
+        const unsigned rnk = __popc(peers & lt);
+        const unsigned base = valid ? cnt[d] : 0u;
+        __syncwarp();
+        if (valid && rnk == 0) cnt[d] = base + __popc(peers);
+        __syncwarp();
+        if (valid) {
+            skey[base + rnk] = k;
+            if (val_in) sval[base + rnk] = vv[u];
+        }
+    }
+    __syncthreads();
+    // 4. coalesced runs per digit
+    for (int j = threadIdx.x; j < len; j += blockDim.x) {
+        const K k = skey[j];
         const unsigned d = (unsigned)(k >> shift) & kMask;
-        const unsigned dst = sg.gbase[d] + ((unsigned)j - sg.lstart[d]);
+        const unsigned dst = gbase[d] + ((unsigned)j - lstart[d]);
         key_out[dst] = k;
-        if (val_in) val_out[dst] = sg.val[j];
+        if (val_in) val_out[dst] = sval[j];
     }
 }
 
 template <typename K, typename V, bool Seg, int Bits>
 int launch_scatter(Ctx *ctx, int nt, const K *kin, K *kout, const V *vin, V *vout, const TileMap &tm, int shift,
                    cudaStream_t st) {
-    const size_t smem = stage_bytes<K, V, Bits>(tm.tile) * kScatterWarps;
-    k_radix_scatter<K, V, Seg, Bits><<<ceil_div(nt, kScatterWarps), kScatterWarps * 32, smem, st>>>(
-        kin, kout, vin, vout, tm, shift, ctx->d_hist);
+    const size_t smem = stage_bytes<K, V, Bits>(tm.tile);
+    k_radix_scatter<K, V, Seg, Bits><<<nt, kScatterWarps * 32, smem, st>>>(kin, kout, vin, vout, tm, shift,
+                                                                           ctx->d_hist);
     ++ctx->launches;
     return NBX_OK;
 }
@@ -298,12 +304,12 @@ int radix_sort_entries(Ctx *ctx, cudaStream_t st) {
 int radix_init(Ctx *ctx) {
     NBX_CUDA(cudaFuncSetAttribute(k_radix_scatter<unsigned long long, int, true, 8>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(stage_bytes<unsigned long long, int, 8>(kTile) * kScatterWarps)));
+                                  (int)stage_bytes<unsigned long long, int, 8>(kTile)));
     NBX_CUDA(cudaFuncSetAttribute(k_radix_scatter<unsigned long long, int, true, 9>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(stage_bytes<unsigned long long, int, 9>(kTile) * kScatterWarps)));
+                                  (int)stage_bytes<unsigned long long, int, 9>(kTile)));
     NBX_CUDA(cudaFuncSetAttribute(k_radix_scatter<unsigned, int, false, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(stage_bytes<unsigned, int, 8>(kTile) * kScatterWarps)));
+                                  (int)stage_bytes<unsigned, int, 8>(kTile)));
     return NBX_OK;
 }
 
