@@ -378,9 +378,37 @@ def bench_hilbert(args, local, b, targets, acc64, tune) -> dict:
 
 
 ACCURACY_TARGET = 1e-4
+ACCURACY_REFINE = 2
 ACCURACY_THETAS = {(0, 0): (0.4, 0.3, 0.25, 0.2, 0.15, 0.125, 0.1),
                    (1, 0): (0.7, 0.65, 0.6, 0.55, 0.5, 0.45, 0.4, 0.35, 0.3),
                    (1, 1): (0.55, 0.5, 0.45, 0.4, 0.35, 0.3)}
+
+
+def sweep_to_target(measure, thetas, refine: int):
+    """Opening angles from large to small until measure(theta) -> (point, ok)
+    meets the target, then `refine` bisection steps between that theta and the
+    last one that missed (measure(theta, refine=True)).  Returns (points,
+    at_target): every measured point, and the point of the largest theta that
+    met the target (None when none did)."""
+    points, at_target, above = [], None, None
+    for th in thetas:
+        pt, ok = measure(th)
+        points.append(pt)
+        if ok:
+            at_target = pt
+            break
+        above = th
+    if at_target is not None and above is not None:
+        lo, hi = at_target["theta"], above
+        for _ in range(refine):
+            mid = round(0.5 * (lo + hi), 6)
+            pt, ok = measure(mid, refine=True)
+            points.append(pt)
+            if ok:
+                at_target, lo = pt, mid
+            else:
+                hi = mid
+    return points, at_target
 
 
 def bench_accuracy(args, local, b, targets, acc64, tune, multipole=0, key_order=0) -> dict:
@@ -390,7 +418,9 @@ def bench_accuracy(args, local, b, targets, acc64, tune, multipole=0, key_order=
     parity-mode walk (monopoles, the reference's MAC with theta_ref = theta^2);
     1: the same lists with cell quadrupoles; key_order 1: Hilbert order (compact
     walk groups, other lists).  Per theta the error on the same 8192 targets,
-    then plain FP32 steps timed with CUDA events after one warm-up step."""
+    then plain FP32 steps timed with CUDA events after one warm-up step.  Once a
+    theta meets the target, ACCURACY_REFINE bisection steps between it and the
+    last theta that missed find a larger theta that still meets it."""
     import torch
     from nns_gb300.barnes_hut import Context, State
     n = len(b.x)
@@ -407,8 +437,8 @@ def bench_accuracy(args, local, b, targets, acc64, tune, multipole=0, key_order=
     elif tune:
         ctx.set_walk(tune["warps"], tune["variant"])
     _, eps2 = ctx.constants()
-    points, at_target = [], None
-    for th in ACCURACY_THETAS[(multipole, key_order)]:
+
+    def measure(th, refine=False):
         ctx.set_constants(float(np.float32(th) * np.float32(th)), eps2, 0)
         s = State.from_bodies(b, device="cuda:%d" % local)
         ctx.build(s)
@@ -435,11 +465,12 @@ def bench_accuracy(args, local, b, targets, acc64, tune, multipole=0, key_order=
               "interactions_per_step": info["interactions"],
               "force_error_vs_fp64_direct": {"median": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99)),
                                              "max": float(rel.max())}}
-        points.append(pt)
+        if refine:
+            pt["refine"] = True
         del s
-        if np.median(rel) <= ACCURACY_TARGET:
-            at_target = pt
-            break
+        return pt, bool(np.median(rel) <= ACCURACY_TARGET)
+
+    points, at_target = sweep_to_target(measure, ACCURACY_THETAS[(multipole, key_order)], ACCURACY_REFINE)
     kind = ("parity-mode walk (monopoles, the reference MAC)" if multipole == 0 else
             "quadrupole mode (the reference MAC and lists, plus cell quadrupoles; not the parity mode)")
     if key_order:
@@ -447,8 +478,10 @@ def bench_accuracy(args, local, b, targets, acc64, tune, multipole=0, key_order=
     return {"multipole": multipole, "key_order": key_order, "target_median": ACCURACY_TARGET, "points": points,
             "at_target": at_target,
             "walk_config": walk,
-            "note": "%s; the first theta in %s whose median error meets the target"
-                    % (kind, list(ACCURACY_THETAS[(multipole, key_order)]))}
+            "note": "%s; the first theta in %s whose median error meets the target, then %d bisection steps "
+                    "towards the last theta that missed it (points marked refine); at_target is the largest "
+                    "theta measured that meets it" % (kind, list(ACCURACY_THETAS[(multipole, key_order)]),
+                                                       ACCURACY_REFINE)}
 
 
 LEAF_SIZES = (1, 2, 4, 8)

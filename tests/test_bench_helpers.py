@@ -1,6 +1,6 @@
 """Host-side helpers of bench.py (no GPU): the committed walk-traffic figure is
 read from its profile (only while the walk's source has the captured git blob
-hash), the HBM roofline arithmetic, and the guard that keeps a failing
+hash), the HBM roofline arithmetic, the accuracy sweep's bisection, and the guard that keeps a failing
 extension section from losing the JSON line."""
 import os
 import sys
@@ -45,3 +45,33 @@ def test_failing_section_is_reported_not_raised():
     out = bench._section(boom, 1, 2)
     assert out == {"unavailable": "RuntimeError: no such device"}
     assert bench._section(lambda a, b: {"ok": a + b}, 1, 2) == {"ok": 3}
+
+
+def _fake_measure(threshold):
+    """A sweep whose error meets the target at every theta <= threshold."""
+    calls = []
+
+    def measure(th, refine=False):
+        calls.append((th, refine))
+        return {"theta": th, "refine": refine}, th <= threshold
+    return measure, calls
+
+
+def test_accuracy_sweep_bisects_towards_the_last_miss():
+    measure, calls = _fake_measure(0.53)
+    points, at = bench.sweep_to_target(measure, (0.7, 0.6, 0.5, 0.4), 2)
+    # coarse: 0.7, 0.6 miss, 0.5 meets; then 0.55 misses, 0.525 meets
+    assert [c[0] for c in calls] == [0.7, 0.6, 0.5, 0.55, 0.525]
+    assert [c[1] for c in calls] == [False, False, False, True, True]
+    assert at["theta"] == 0.525 and len(points) == 5
+
+
+def test_accuracy_sweep_edges():
+    # the first theta meets the target: nothing to bisect
+    measure, calls = _fake_measure(1.0)
+    points, at = bench.sweep_to_target(measure, (0.7, 0.6), 2)
+    assert at["theta"] == 0.7 and len(calls) == 1
+    # no theta meets it: no refinement, no point at the target
+    measure, calls = _fake_measure(0.1)
+    points, at = bench.sweep_to_target(measure, (0.7, 0.6), 2)
+    assert at is None and len(points) == 2
