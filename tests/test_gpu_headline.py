@@ -10,7 +10,8 @@ light bodies (about 8.1 million cells, 16 levels deep).
 The walk is checked on 128 random walk groups (4096 bodies): per-body
 interaction-list length and opened-cell count bit-exact (identical MAC
 decisions), and forces within 1e-5 median / 1e-4 max relative error, for the
-plain FP32 walk and both compensated forms.  The oracle restates
+plain FP32 walk and both compensated forms, and for the quadrupole mode against
+the oracle's FP64 quadrupole evaluation of the same lists.  The oracle restates
 3D/CUDA/CUDA_NBody/src/Kernels.cu:157-456 (build and sort) and :460-577 (walk).
 """
 import numpy as np
@@ -96,3 +97,31 @@ def test_binary_disk_2p24_tree_and_walk(cuda, workload, oracle_tree):
         rel = _rel(s.acc()[idx], f.a64[idx])
         assert np.median(rel) <= MED_TOL and rel.max() <= MAX_TOL, (mode, np.median(rel), rel.max())
         assert np.median(rel) <= np.median(plain64) * 1.01, (mode, np.median(rel), np.median(plain64))
+
+
+def test_binary_disk_2p24_quadrupole_walk(cuda, workload, oracle_tree):
+    """The quadrupole mode (multipole = 1, outside the parity mode) at the same
+    size: the same lists as the oracle's monopole walk on 128 random groups, and
+    forces within 1e-5 median / 1e-4 max of the oracle's FP64 evaluation of
+    those lists with FP64 quadrupoles (orc_quad) -- the configuration whose
+    error against the FP64 direct sum meets 1e-4 at theta 0.5."""
+    from nns_gb300.barnes_hut import Context, State
+    b, ot = workload, oracle_tree
+    ctx = Context(max_bodies=N, theta=THETA, eps=EPS, dt=5e-4, multipole=1)
+    ctx.set_systems([0, N])
+    s = State.from_bodies(b)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    assert ctx.tree_info()["ncells"] == ot.ncells
+    theta_ref, eps2 = ctx.constants()
+    groups = np.random.default_rng(11).choice(N // 32, 128, replace=False)
+    q = O.quadrupoles(b.x, b.y, b.z, b.m, ot)
+    f = O.forces(b.x, b.y, b.z, b.m, ot, theta_ref, eps2, groups=groups, quad=q)
+    del q
+    idx = np.concatenate([ot.perm[g * 32:(g + 1) * 32] for g in groups])
+    nl, no = ctx.walk_stats()
+    assert np.array_equal(nl[idx], f.nlist[idx])
+    assert np.array_equal(no[idx], f.nopen[idx])
+    rel = _rel(s.acc()[idx], f.a64[idx])
+    assert np.median(rel) <= MED_TOL and rel.max() <= MAX_TOL, (np.median(rel), rel.max())
