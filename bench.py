@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-hilbert", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-buckets", action="store_true")
+    ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--fd-directions", type=int, default=16)
     ap.add_argument("--adjoint-steps", type=int, default=100)
     ap.add_argument("--adjoint-checkpoint", type=int, default=10)
@@ -375,6 +376,81 @@ def bench_hilbert(args, local, b, targets, acc64, tune) -> dict:
                                            "p99": float(np.quantile(rel, 0.99)), "max": float(rel.max())},
             "note": "key_order=1: same cells and MAC, Hilbert sibling order; the walk groups and so the "
                     "interaction lists differ from the reference's (not the parity mode)"}
+
+
+# the other single-system configurations: name, bodies, theta, eps, dt, steps
+OTHER_CONFIGS = (("star_disk_16384", "star_disk", 16384, 0.5, 0.01, 1e-3, 10),
+                 ("plummer_2^20", "plummer", 1 << 20, 0.6, 0.005, 1e-3, 100))
+
+
+def bench_configs(args, local, tune) -> dict:
+    """The other single-system configurations at their own theta, eps, dt and
+    step counts (the reference arm times whole steps of the same two): the
+    16384-body star + disk (10 steps) and the 2^20-body Plummer sphere (100
+    steps).  Per configuration: the force error against the FP64 direct sum on
+    4096 random targets at the initial state; all its steps replayed from one
+    CUDA graph, timed with CUDA events after one warm-up replay (steps/s); and
+    three eager steps with per-phase events for the walk's FP32 fraction."""
+    import torch
+    from nns_gb300 import ic
+    from nns_gb300.barnes_hut import Context, State
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    peaks = measured_peaks()
+    peak = peak_fp32_tflops(nsm, peaks.get("sm_max_mhz") or 2070.0)
+    out = {}
+    for name, kind, n, theta, eps, dt, steps in OTHER_CONFIGS:
+        b = getattr(ic, kind)(n)
+        ctx = Context(max_bodies=n, theta=theta, eps=eps, dt=dt, device=local)
+        if tune:
+            ctx.set_walk(tune["warps"], tune["variant"])
+        ctx.set_systems([0, n])
+        s = State.from_bodies(b, device="cuda:%d" % local)
+        eps2 = float(np.float32(eps) * np.float32(eps))
+        targets = np.sort(np.random.default_rng(12345).choice(n, size=min(4096, n), replace=False))
+        acc64 = ctx.direct_fp64(s, targets, eps2).cpu().numpy()
+        ctx.build(s)
+        ctx.forces(s)
+        ctx.sync()
+        a = s.acc()[targets].astype(np.float64)
+        rel = np.linalg.norm(a - acc64, axis=1) / np.linalg.norm(acc64, axis=1)
+        ctx.graph_step(s, steps)  # warm-up replay (captures the graph)
+        ctx.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        ctx.graph_step(s, steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ctx.sync()
+        ms = e0.elapsed_time(e1) / steps
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(3)]
+        torch.cuda.synchronize()
+        for e in ev:
+            e[0].record()
+            ctx.build(s)
+            e[1].record()
+            ctx.forces(s)
+            e[2].record()
+            ctx.integrate(s)
+        torch.cuda.synchronize()
+        info = ctx.tree_info()
+        ctx.sync()
+        walk_ms = sum(e[1].elapsed_time(e[2]) for e in ev) / len(ev)
+        tflops = info["interactions"] * FLOP_PER_INTERACTION / (walk_ms * 1e-3) / 1e12
+        out[name] = {"n": n, "theta": theta, "eps": eps, "dt": dt, "steps": steps,
+                     "steps_per_s": round(1000.0 / ms, 2), "ms_per_step": round(ms, 4),
+                     "build_ms": round(sum(e[0].elapsed_time(e[1]) for e in ev) / len(ev), 4),
+                     "walk_ms": round(walk_ms, 4), "interactions_per_step": info["interactions"],
+                     "interactions_per_s": round(info["interactions"] * 1000.0 / ms, 1),
+                     "walk_fp32_frac": round(tflops / peak, 4),
+                     "force_error_vs_fp64_direct": {"median": float(np.median(rel)),
+                                                    "p99": float(np.quantile(rel, 0.99)), "max": float(rel.max())}}
+        del ctx, s
+        torch.cuda.empty_cache()
+    out["note"] = ("each configuration's steps replayed from one CUDA graph (steps_per_s); walk_fp32_frac from "
+                   "three eager steps against the nominal FP32 peak; the reference arm's line times whole "
+                   "steps of the same configurations")
+    return out
 
 
 ACCURACY_TARGET = 1e-4
@@ -896,6 +972,10 @@ def main():
     if not args.no_hilbert:
         hilbert = _section(bench_hilbert, args, local, b, targets, acc64, tune if tune and "warps" in tune else None)
         torch.cuda.empty_cache()
+    configs = None
+    if not args.no_configs:
+        configs = _section(bench_configs, args, local, tune if tune and "warps" in tune else None)
+        torch.cuda.empty_cache()
     if not args.no_batched:
         batched = _section(bench_batched, args, local)
         torch.cuda.empty_cache()
@@ -954,6 +1034,7 @@ def main():
                 "pipeline": "two device states: the copies of one step overlap the compute of the other",
                 "d2h_bytes_per_step": d2h},
         "hilbert": hilbert,
+        "configs": configs,
         "buckets": buckets,
         "batched": batched,
         "adjoint": adjoint,
