@@ -54,7 +54,8 @@ typedef struct nbx_params {
                           (softened) is accepted when s^2 / theta^2 <= r, i.e. the
                           reference's raw constant is theta^2 */
     float theta_ref;   /* > 0: use this raw MAC constant (Kernels.cu:18 `theta`) */
-    float eps;         /* Plummer softening length */
+    float eps;         /* Plummer softening length (the squared softening in use
+                          must be > 0: a body's own term, d = 0, is 0 * inf otherwise) */
     float eps2;        /* > 0: use this squared softening (Kernels.cu:17) */
     float dt;          /* time step (main.cu:52) */
     float dampening;   /* velocity factor of the drift (main.cu:54) */
@@ -122,7 +123,9 @@ int nbx_create(const nbx_params *p, nbx_ctx **out);
 int nbx_destroy(nbx_ctx *ctx);
 const char *nbx_status_string(int status);
 const char *nbx_last_error(nbx_ctx *ctx);
-/* Current effective MAC constant and softening of the context. */
+/* Current effective MAC constant and softening of the context.  nbx_create
+ * and nbx_set_constants take a finite theta_ref > 0 and a finite, normal
+ * eps2 >= FLT_MIN (NBX_ERR_ARG otherwise). */
 int nbx_get_constants(nbx_ctx *ctx, float *theta_ref, float *eps2);
 int nbx_set_constants(nbx_ctx *ctx, float theta_ref, float eps2, int compensated);
 /* Launch shape of the walk: warps per block (4, 8 or 16) and variant; used by

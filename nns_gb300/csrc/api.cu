@@ -1,5 +1,7 @@
 // api.cu -- the C ABI of libnbx: context, reference-compatible phase entry
 // points (3D/CUDA/CUDA_NBody/src/KernelsWrapper.cu) and the native pipeline.
+#include <cfloat>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -239,6 +241,12 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     ctx->p = *p;
     ctx->theta_ref = p->theta_ref > 0.f ? p->theta_ref : p->theta * p->theta;
     ctx->eps2 = p->eps2 > 0.f ? p->eps2 : p->eps * p->eps;
+    // a body's own term (d = 0) is 0 * inf without softening; a normal eps2 keeps
+    // every softened r^2 >= eps2 out of the subnormal range
+    if (!(ctx->theta_ref > 0.f) || !(ctx->eps2 >= FLT_MIN) || !std::isfinite(ctx->theta_ref) || !std::isfinite(ctx->eps2)) {
+        delete ctx;
+        return NBX_ERR_ARG;
+    }
     ctx->compensated = p->compensated;
     ctx->walk_variant = p->walk_variant;
     ctx->key_order = p->key_order;
@@ -349,7 +357,8 @@ int nbx_get_constants(nbx_ctx *c, float *theta_ref, float *eps2) {
 }
 
 int nbx_set_constants(nbx_ctx *c, float theta_ref, float eps2, int compensated) {
-    if (!c || !(theta_ref > 0.f) || !(eps2 >= 0.f)) return NBX_ERR_ARG;
+    if (!c || !(theta_ref > 0.f) || !(eps2 >= FLT_MIN) || !std::isfinite(theta_ref) || !std::isfinite(eps2))
+        return NBX_ERR_ARG;
     if (compensated < 0 || compensated > 2) return NBX_ERR_ARG;
     Ctx *ctx = C(c);
     ctx->theta_ref = theta_ref;

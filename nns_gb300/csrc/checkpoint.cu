@@ -13,6 +13,8 @@
 //   uint64   weighted checksum of the float payload (as 32-bit words)
 // A restore checks the magic, version, sizes and both checksums before it
 // changes anything, then sets the systems and constants and copies the bodies.
+#include <cfloat>
+#include <cmath>
 #include <cstddef>
 #include <cstring>
 #include <vector>
@@ -153,7 +155,8 @@ extern "C" int nbx_checkpoint_restore(nbx_ctx *c, nbx_state *s, const void *host
     // settings outside their ranges are a malformed checkpoint: refused before anything changes
     if (h.multipole < 0 || h.multipole > 1 || h.leaf_size < 1 || h.leaf_size > 8 || h.walk_variant < 0 ||
         h.walk_variant > 3 || !(h.walk_warps == 4 || h.walk_warps == 8 || h.walk_warps == 16) || h.stack_depth < 360 ||
-        h.stack_depth > 4096 || (h.multipole == 1 && h.walk_variant == 2) || h.compensated < 0 || h.compensated > 2)
+        h.stack_depth > 4096 || (h.multipole == 1 && h.walk_variant == 2) || h.compensated < 0 || h.compensated > 2 ||
+        !(h.theta_ref > 0.f) || !(h.eps2 >= FLT_MIN) || !std::isfinite(h.theta_ref) || !std::isfinite(h.eps2))
         return NBX_ERR_FORMAT;
     if (n > ctx->cap_bodies || nsys > ctx->cap_sys || h.key_order != ctx->key_order) return NBX_ERR_ARG;
     int rc = nbx_set_systems(c, nsys, off.data());

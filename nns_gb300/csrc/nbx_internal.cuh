@@ -113,7 +113,7 @@ struct Ctx {
     unsigned char *d_lvl8 = nullptr;                  // [NC] tree level of each node (root children: 1)
     double2 *d_m2 = nullptr;       // [3 NC] quadrupole mode: FP64 second moments about the cell's centre of
                                    // mass, (xx, yy) (zz, xy) (xz, yz)
-    float4 *d_quad4 = nullptr;     // [NC] quadrupole mode: traceless Q of cells in FP32, (xx, yy, zz, xy)
+    float4 *d_quad4 = nullptr;     // [NC] quadrupole mode: P = -Q (Q traceless) of cells in FP32, (xx, yy, zz, xy)
     float2 *d_quad2 = nullptr;     // [NC]                                              (xz, yz)
     int *d_fcl = nullptr;                             // [NC+S+1] first-child list
     int *d_cl = nullptr;                              // [NC+S] cell list (BFS index)

@@ -460,7 +460,9 @@ __global__ void __launch_bounds__(kBlock) k_nodes_b(const unsigned *__restrict__
 // Quadrupole mode: the FP64 second moments of a cell about its centre of mass c,
 // composed from its children in child order -- M2 = sum over children of
 // [M2_child + m_child d d^T], d = c_child - c (a body child: M2 = 0, c_child =
-// its position) -- and the cell's traceless FP32 quadrupole Q = 3 M2 - tr(M2) I.
+// its position) -- and the cell's traceless quadrupole Q = 3 M2 - tr(M2) I,
+// stored negated in FP32 as P = -Q = tr(M2) I - 3 M2 (the walk's form of the
+// term; the FP64 differences are negated before rounding, so P is exactly -Q).
 // Every FP64 operation is rounded explicitly (no contraction), in the order of
 // the oracle's restatement, so both give the same bits.
 __device__ __forceinline__ void m2_add_point(double *a, double mc, double dx, double dy, double dz) {
@@ -507,9 +509,9 @@ __device__ __forceinline__ void quad_cell(int b, int first, int nch, double cx, 
     m2[3 * (size_t)b + 1] = make_double2(a[2], a[3]);
     m2[3 * (size_t)b + 2] = make_double2(a[4], a[5]);
     const double tr = __dadd_rn(__dadd_rn(a[0], a[1]), a[2]);
-    quad4[b] = make_float4((float)__dsub_rn(__dmul_rn(3.0, a[0]), tr), (float)__dsub_rn(__dmul_rn(3.0, a[1]), tr),
-                           (float)__dsub_rn(__dmul_rn(3.0, a[2]), tr), (float)__dmul_rn(3.0, a[3]));
-    quad2[b] = make_float2((float)__dmul_rn(3.0, a[4]), (float)__dmul_rn(3.0, a[5]));
+    quad4[b] = make_float4((float)__dsub_rn(tr, __dmul_rn(3.0, a[0])), (float)__dsub_rn(tr, __dmul_rn(3.0, a[1])),
+                           (float)__dsub_rn(tr, __dmul_rn(3.0, a[2])), (float)__dmul_rn(-3.0, a[3]));
+    quad2[b] = make_float2((float)__dmul_rn(-3.0, a[4]), (float)__dmul_rn(-3.0, a[5]));
 }
 
 // Bottom-up FP64 moments, one BFS level per launch (deepest first): a cell sums

@@ -152,16 +152,14 @@ __device__ __forceinline__ void accumulate(Sums &a, u64 f, u64 mm, u64 ri, u64 d
     if (Pot) a.p = fma2(mm, ri, a.p);
 }
 
-// Accumulate F d + n q for two candidates: the quadrupole mode's contribution,
-// with F = m r^-3 + 5/2 (d.Q.d) r^-7 and n = -r^-5 (d = cell - body, q = Q d).
+// Accumulate r^-2 v for two candidates: the quadrupole mode's contribution.
 template <int Mode>
-__device__ __forceinline__ void accumulate_quad(Sums &a, u64 F, u64 n5, u64 dx, u64 dy, u64 dz, u64 qx, u64 qy,
-                                                u64 qz) {
+__device__ __forceinline__ void accumulate_quad(Sums &a, u64 ri2, u64 vx, u64 vy, u64 vz) {
     if (Mode == 2) {
         float xa, xb, ya, yb, za, zb;
-        upk(fma2(F, dx, mul2(n5, qx)), xa, xb);
-        upk(fma2(F, dy, mul2(n5, qy)), ya, yb);
-        upk(fma2(F, dz, mul2(n5, qz)), za, zb);
+        upk(mul2(ri2, vx), xa, xb);
+        upk(mul2(ri2, vy), ya, yb);
+        upk(mul2(ri2, vz), za, zb);
         kahan(a.kx, a.cx, xa);
         kahan(a.kx, a.cx, xb);
         kahan(a.ky, a.cy, ya);
@@ -169,30 +167,37 @@ __device__ __forceinline__ void accumulate_quad(Sums &a, u64 F, u64 n5, u64 dx, 
         kahan(a.kz, a.cz, za);
         kahan(a.kz, a.cz, zb);
     } else {
-        a.x = fma2(n5, qx, fma2(F, dx, a.x));
-        a.y = fma2(n5, qy, fma2(F, dy, a.y));
-        a.z = fma2(n5, qz, fma2(F, dz, a.z));
+        a.x = fma2(ri2, vx, a.x);
+        a.y = fma2(ri2, vy, a.y);
+        a.z = fma2(ri2, vz, a.z);
     }
 }
 
-// One pair of cells of the quadrupole mode:
-//   a += m d r^-3 - Q d r^-5 + 5/2 (d.Q.d) d r^-7   (d = cell - body),
-// with the cells' quadrupoles from slot pair q of the buffer; `neg` is (-1, -1)
-// for two accepted cells, 0 in a half whose cell is rejected (with its mass
-// zero in mm, the half adds nothing).
+// One pair of cells of the quadrupole mode, with the cells' negated traceless
+// quadrupoles P = -Q from slot pair q of the buffer (d = cell - body,
+// r^2 = |d|^2 + eps^2, e = d / r):
+//   a += m d r^-3 - Q d r^-5 + 5/2 (d.Q.d) d r^-7
+//      = r^-2 [ (m - 5/2 (e.P.e) r^-2) e + (P e) r^-2 ].
+// In the unit-vector form every intermediate is bounded by |Q| or by the
+// mass and force scales, and the only power of r^-1 is r^-2 <= 1 / eps^2.
+// With d itself, r^-5 and r^-7 overflow FP32 once r is below about 1e-8, and
+// d.Q.d (~ |Q| d^2) underflows for cells of about 1e-12 and less, dropping a
+// term that is 1e-2 of such a pair's force.  A rejected half of a voted pair
+// comes with ri = 0, so its e and r^-2, and its whole term, are 0.
 template <int Mode, int CB>
-__device__ __forceinline__ void quad_term(Sums &acc, const QuadBuf<CB> &qbuf, int q, u64 mm, u64 ri, u64 neg, u64 dx,
-                                          u64 dy, u64 dz) {
+__device__ __forceinline__ void quad_term(Sums &acc, const QuadBuf<CB> &qbuf, int q, u64 mm, u64 ri, u64 dx, u64 dy,
+                                          u64 dz) {
     const ulonglong2 QA = qbuf.qa[q], QB = qbuf.qb[q], QC = qbuf.qc[q];
     const u64 ri2 = mul2(ri, ri);
-    const u64 ri3 = mul2(ri2, ri);
-    const u64 n5 = mul2(mul2(ri3, ri2), neg);
-    const u64 qx = fma2(QC.x, dz, fma2(QB.y, dy, mul2(QA.x, dx)));
-    const u64 qy = fma2(QC.y, dz, fma2(QA.y, dy, mul2(QB.y, dx)));
-    const u64 qz = fma2(QB.x, dz, fma2(QC.y, dy, mul2(QC.x, dx)));
-    const u64 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));
-    const u64 F = fma2(mul2(dqd, mul2(n5, ri2)), pk(-2.5f, -2.5f), mul2(mm, ri3));
-    accumulate_quad<Mode>(acc, F, n5, dx, dy, dz, qx, qy, qz);
+    const u64 ex = mul2(dx, ri), ey = mul2(dy, ri), ez = mul2(dz, ri);
+    // P e: P = (xx, yy, zz, xy | xz, yz) in QA = (xx, yy), QB = (zz, xy), QC = (xz, yz)
+    const u64 px = fma2(QC.x, ez, fma2(QB.y, ey, mul2(QA.x, ex)));
+    const u64 py = fma2(QC.y, ez, fma2(QA.y, ey, mul2(QB.y, ex)));
+    const u64 pz = fma2(QB.x, ez, fma2(QC.y, ey, mul2(QC.x, ex)));
+    const u64 epe = fma2(ez, pz, fma2(ey, py, mul2(ex, px)));
+    const u64 mq = fma2(mul2(epe, ri2), pk(-2.5f, -2.5f), mm);
+    accumulate_quad<Mode>(acc, ri2, fma2(mq, ex, mul2(px, ri2)), fma2(mq, ey, mul2(py, ri2)),
+                          fma2(mq, ez, mul2(pz, ri2)));
 }
 
 // CB = 64 and 96: 64-register budget (two 16-warp or four 8-warp blocks per SM);
@@ -514,7 +519,7 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                     float ra, rb;
                     upk(r, ra, rb);
                     const u64 ri = pk(rsq(ra), rsq(rb));
-                    quad_term<Mode>(acc, qbuf, q, B.y, ri, pk(-1.f, -1.f), dx, dy, dz);
+                    quad_term<Mode>(acc, qbuf, q, B.y, ri, dx, dy, dz);
                 }
             }
             // ---- evaluate cells: one vote per cell, accept or push
@@ -542,16 +547,17 @@ __global__ void __launch_bounds__(WalkBounds<CB>::kThreads, WalkBounds<CB>::kMin
                 const bool okb = __all_sync(0xffffffffu, dpb <= rb);
 #endif
                 if (oka || okb) {  // warp-uniform: a pair of rejected cells adds nothing
-                    float ma, mb;
-                    upk(B.y, ma, mb);
-                    const u64 ri = pk(rsq(ra), rsq(rb));
-                    const u64 mm = pk(oka ? ma : 0.f, okb ? mb : 0.f);
                     if (!Quad) {
+                        float ma, mb;
+                        upk(B.y, ma, mb);
+                        const u64 ri = pk(rsq(ra), rsq(rb));
+                        const u64 mm = pk(oka ? ma : 0.f, okb ? mb : 0.f);
                         const u64 f = mul2(mul2(mul2(mm, ri), ri), ri);
                         accumulate<Mode, Pot>(acc, f, mm, ri, dx, dy, dz);
                     } else {
-                        // the rejected half of the pair masked through m and r^-5
-                        quad_term<Mode>(acc, qbuf, q, mm, ri, pk(oka ? -1.f : 0.f, okb ? -1.f : 0.f), dx, dy, dz);
+                        // the rejected half of the pair masked through r^-1 (its term is 0)
+                        const u64 ri = pk(oka ? rsq(ra) : 0.f, okb ? rsq(rb) : 0.f);
+                        quad_term<Mode>(acc, qbuf, q, B.y, ri, dx, dy, dz);
                     }
                 }
                 if (!oka) {

@@ -65,6 +65,26 @@ def test_params_layout_and_option_ranges_without_gpu():
         assert L.nbx_create(ctypes.byref(q), ctypes.byref(h)) == 1, field
 
 
+def test_constants_validated_without_gpu():
+    """The softening and MAC constant in use must be finite and positive, the
+    squared softening a normal float (a body's own term is 0 * inf without it):
+    rejected before any CUDA call, in either multipole order."""
+    from nns_gb300 import _lib
+    L = _lib.lib()
+    cases = ((dict(eps=0.0, eps2=0.0), 1), (dict(eps=-0.0, eps2=0.0), 1), (dict(eps=1e-20, eps2=0.0), 1),
+             (dict(eps2=float("inf")), 1), (dict(eps=float("nan"), eps2=0.0), 1),
+             (dict(theta=0.0, theta_ref=0.0), 1), (dict(theta_ref=float("inf")), 1),
+             (dict(eps=0.0, eps2=0.0, multipole=1), 1), (dict(eps=1e-20, eps2=0.0, multipole=1), 1))
+    for kw, rc in cases:
+        q = _lib.nbx_params()
+        L.nbx_params_default(ctypes.byref(q))
+        for k, v in kw.items():
+            setattr(q, k, v)
+        h = ctypes.c_void_p()
+        assert L.nbx_create(ctypes.byref(q), ctypes.byref(h)) == rc, kw
+    assert L.nbx_set_constants(None, 0.25, 1e-4, 0) == 1
+
+
 def test_capacity_bounds_without_gpu():
     """max_bodies above 2^26 and node pools above 2^28 are rejected before any CUDA call."""
     from nns_gb300 import _lib

@@ -144,3 +144,63 @@ def test_quadrupole_graph_and_switching(cuda):
     with pytest.raises(NbxError) as e:
         Adjoint(graph, 4, 2, 4096, 2)
     assert e.value.code == 1  # NBX_ERR_ARG
+
+
+def _quad_vs_oracle(b, eps=0.01, variant=3):
+    ctx, s = _run(b, variant=variant, eps=eps)
+    t, e2 = ctx.constants()
+    ot = O.build(b.x, b.y, b.z, b.m)
+    q = O.quadrupoles(b.x, b.y, b.z, b.m, ot)
+    f = O.forces(b.x, b.y, b.z, b.m, ot, t, e2, quad=q)
+    nl, no = ctx.walk_stats()
+    assert ctx.tree_info()["status"] == 0
+    assert np.array_equal(nl, f.nlist) and np.array_equal(no, f.nopen)
+    return s.acc().astype(np.float64), f.a64
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 33, 100])
+def test_quadrupole_small_and_ragged(cuda, n):
+    """Tiny and ragged systems (root children only, a partial walk group, one
+    body past a whole group): the same lists as the oracle, forces within
+    1e-4 of its FP64 quadrupole evaluation (a single body feels nothing)."""
+    a, a64 = _quad_vs_oracle(ic.plummer(n, seed=ic.SEED0 + n))
+    if n > 1:
+        assert _rel(a, a64).max() <= MAX_TOL
+    else:
+        assert not a.any()
+
+
+@pytest.mark.parametrize("variant", [3, 1], ids=["walk96", "walk128"])
+@pytest.mark.parametrize("name", ["collinear", "coplanar", "signed_zeros", "cluster", "deep"])
+def test_quadrupole_adversarial_geometry(cuda, name, variant):
+    """The adversarial sets of the parity tests in quadrupole mode: degenerate
+    boxes (cells whose second moments vanish along an axis), signed zeros, split
+    planes, a tight cluster and cells past level 32 (second moments of nearly
+    coincident bodies).  Lists bit-exact; each body's error bounded relative to
+    its own force plus the set's median force (pulls that nearly cancel on a
+    line or in a plane leave only the summation-order error)."""
+    from adversarial import CASES, EPS
+    a, a64 = _quad_vs_oracle(CASES[name](), eps=EPS.get(name, 0.01), variant=variant)
+    rel = _rel(a, a64)
+    assert np.median(rel) <= MED_TOL, np.median(rel)
+    err = np.linalg.norm(a - a64, axis=1)
+    mag = np.linalg.norm(a64, axis=1)
+    assert (err <= MAX_TOL * (mag + np.median(mag))).all(), (err / (mag + np.median(mag))).max()
+
+
+def test_quadrupole_softening_range(cuda):
+    """The quadrupole terms are evaluated in the unit vector d / r, so any normal
+    softening works in the mode (the deep adversarial set above uses 1e-12); a
+    zero or subnormal softening is refused in either mode, leaving the context
+    unchanged."""
+    from nns_gb300._lib import NbxError
+    from nns_gb300.barnes_hut import Context
+    ctx = Context(max_bodies=64, theta=0.5, eps=1e-15, multipole=1)
+    t, e2 = ctx.constants()
+    assert e2 == np.float32(1e-15) * np.float32(1e-15)
+    for mp in (1, 0):
+        ctx.set_multipole(mp)
+        for bad in (0.0, 1e-40, float("inf")):
+            with pytest.raises(NbxError):
+                ctx.set_constants(t, bad)
+            assert ctx.constants()[1] == e2
