@@ -767,3 +767,39 @@ def test_hilbert_walk_lists_match_oracle(cuda, name, multipole):
     assert np.array_equal(nl, f.nlist) and np.array_equal(no, f.nopen)
     rel = _rel(s.acc(), f.a64 if multipole else f.a)
     assert np.median(rel) <= 1e-5 and rel.max() <= 1e-4, (np.median(rel), rel.max())
+
+
+@pytest.mark.parametrize("name", ["collinear", "coplanar", "signed_zeros", "cluster", "deep"])
+def test_hilbert_adversarial_geometry(cuda, name):
+    """Hilbert order on the adversarial sets (degenerate boxes, signed zeros,
+    split planes, a tight cluster, keys refined past level 21): the same cells as
+    the Morton tree, bodies in non-decreasing 21-level Hilbert key order (the
+    reference's Lebesgue2Hilbert), and lists bit-exact against the oracle's walk
+    with the Hilbert groups."""
+    import dataclasses
+    from adversarial import CASES, EPS
+    from nns_gb300.barnes_hut import Context
+    b = CASES[name]()
+    n = len(b.x)
+    ctx = Context(max_bodies=n, theta=0.5, eps=EPS.get(name, 0.01), key_order=1)
+    ctx.set_systems([0, n])
+    s = _state(b)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    assert ctx.tree_info()["status"] == 0
+    _, perm_h = ctx.export_keys()
+    assert np.array_equal(np.sort(perm_h), np.arange(n))
+    ot = O.build(b.x, b.y, b.z, b.m)
+    assert ctx.tree_info()["ncells"] == ot.ncells
+    hi, _ = O.keys(b.x, b.y, b.z, ot.bbox, 21)
+    hk = O.hilbert(O.md_key(hi))
+    assert np.all(np.diff(hk[perm_h].astype(np.float64)) >= 0)
+    t, e2 = ctx.constants()
+    f = O.forces(b.x, b.y, b.z, b.m, dataclasses.replace(ot, perm=np.ascontiguousarray(perm_h, np.int32)), t, e2)
+    nl, no = ctx.walk_stats()
+    assert np.array_equal(nl, f.nlist) and np.array_equal(no, f.nopen)
+    a = s.acc().astype(np.float64)
+    err = np.linalg.norm(a - f.a, axis=1)
+    mag = np.linalg.norm(f.a.astype(np.float64), axis=1)
+    assert (err <= MAX_TOL * (mag + np.median(mag))).all(), (err / (mag + np.median(mag))).max()
