@@ -115,3 +115,36 @@ def test_bucket_batched_and_switching(cuda):
     ctx.sync()
     ot = O.build(parts[0].x, parts[0].y, parts[0].z, parts[0].m)
     assert np.array_equal(ctx.export_tree(0)["cell_child"], ot.cell_child)
+
+
+@pytest.mark.parametrize("name", ["collinear", "coplanar", "signed_zeros", "cluster", "deep"])
+@pytest.mark.parametrize("k", [2, 8])
+def test_bucket_adversarial_geometry(cuda, name, k):
+    """Leaf buckets on the adversarial sets (degenerate boxes, signed zeros,
+    split planes, a tight cluster, runs of keys refined past level 21, where the
+    window test reads deltas up to 41): lists bit-exact against the oracle's
+    pruned tree; each body's error bounded relative to its own force plus the
+    set's median force (pulls that nearly cancel on a line or in a plane)."""
+    from adversarial import CASES as ADV, EPS
+    from nns_gb300.barnes_hut import Context, State
+    b = ADV[name]()
+    n = len(b.x)
+    ctx = Context(max_bodies=n, theta=0.5, eps=EPS.get(name, 0.01), leaf_size=k)
+    ctx.set_systems([0, n])
+    s = State.from_bodies(b)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    assert ctx.tree_info()["status"] == 0
+    t, e2 = ctx.constants()
+    ot = O.build(b.x, b.y, b.z, b.m)
+    bt = O.bucket_tree(ot, k)
+    f = O.forces(b.x, b.y, b.z, b.m, bt, t, e2)
+    nl, no = ctx.walk_stats()
+    assert np.array_equal(nl, f.nlist) and np.array_equal(no, f.nopen)
+    assert ctx.tree_info()["ncells"] == O.reachable_cells(bt)
+    a = s.acc().astype(np.float64)
+    err = np.linalg.norm(a - f.a, axis=1)
+    mag = np.linalg.norm(f.a.astype(np.float64), axis=1)
+    assert np.median(_rel(a, f.a)) <= MED_TOL
+    assert (err <= MAX_TOL * (mag + np.median(mag))).all(), (err / (mag + np.median(mag))).max()
