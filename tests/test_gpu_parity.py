@@ -803,3 +803,32 @@ def test_hilbert_adversarial_geometry(cuda, name):
     err = np.linalg.norm(a - f.a, axis=1)
     mag = np.linalg.norm(f.a.astype(np.float64), axis=1)
     assert (err <= MAX_TOL * (mag + np.median(mag))).all(), (err / (mag + np.median(mag))).max()
+
+
+@pytest.mark.parametrize("mode", [1, 2], ids=["split", "kahan"])
+@pytest.mark.parametrize("name", ["collinear", "coplanar", "signed_zeros", "cluster", "deep"])
+def test_compensated_adversarial_geometry(cuda, name, mode):
+    """The compensated forms on the adversarial sets: the same lists as the
+    plain walk and the oracle, and each body's error against the oracle's FP64
+    evaluation of those lists bounded relative to its own force plus the set's
+    median force, no looser than the plain walk's bound."""
+    from adversarial import CASES, EPS
+    b = CASES[name]()
+    n = len(b.x)
+    ctx = _ctx(n, theta=0.5, eps=EPS.get(name, 0.01))
+    t, e2 = ctx.constants()
+    ctx.set_constants(t, e2, mode)
+    ctx.set_systems([0, n])
+    s = _state(b)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    ot = O.build(b.x, b.y, b.z, b.m)
+    f = O.forces(b.x, b.y, b.z, b.m, ot, t, e2)
+    nl, no = ctx.walk_stats()
+    assert np.array_equal(nl, f.nlist) and np.array_equal(no, f.nopen)
+    a = s.acc().astype(np.float64)
+    err = np.linalg.norm(a - f.a64, axis=1)
+    mag = np.linalg.norm(f.a64, axis=1)
+    assert np.median(_rel(a, f.a64)) <= MED_TOL
+    assert (err <= MAX_TOL * (mag + np.median(mag))).all(), (err / (mag + np.median(mag))).max()
