@@ -172,8 +172,7 @@ __global__ void __launch_bounds__(kAdjWarps * 32)
     __shared__ __align__(16) float4 stage[kAdjWarps][2][kChunk];  // node records of two chunks
     __shared__ float part[kAdjWarps][3][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const u64 eps2x2 = pk(eps2, eps2), three2 = pk(3.f, 3.f);
-    constexpr u64 kSign2 = 0x8000000080000000ull;  // flips the sign of both halves
+    const u64 eps2x2 = pk(eps2, eps2), mthree2 = pk(-3.f, -3.f);
     for (int g = blockIdx.x; g < ngroups; g += gridDim.x) {
         const int p0 = groups[g];
         const int s = body_sys[p0];
@@ -227,21 +226,25 @@ __global__ void __launch_bounds__(kAdjWarps * 32)
                 s2 = fma2(dz, dz, s2);
                 float sa, sb;
                 upk(s2, sa, sb);
+                // m (g s^-3/2 - 3 (d.g) d s^-5/2) = (m r^-3) (g - 3 (e.g) e), e = d / r:
+                // in the unit vector e no intermediate leaves the FP32 range (s^-5/2
+                // alone overflows once r is below about 2e-8, and a body's own entry,
+                // d = 0, then gave 0 * inf)
                 const u64 inv = pk(rsq(sa), rsq(sb));
                 const u64 inv2 = mul2(inv, inv);
-                const u64 inv3 = mul2(inv2, inv);
-                const u64 inv5 = mul2(inv3, inv2);
-                u64 dg = mul2(dx, gx2);
-                dg = fma2(dy, gy2, dg);
-                dg = fma2(dz, gz2, dg);
-                const u64 mt = mul2(mul2(three2, dg), inv5) ^ kSign2;  // -3 (d.g) s^-5
+                const u64 ex = mul2(dx, inv), ey = mul2(dy, inv), ez = mul2(dz, inv);
+                u64 eg = mul2(ex, gx2);
+                eg = fma2(ey, gy2, eg);
+                eg = fma2(ez, gz2, eg);
+                const u64 m3eg = mul2(eg, mthree2);  // -3 (e.g)
                 // a body's own entry has d = 0 and contributes nothing net; entries
                 // past the chunk's end contribute nothing
                 const bool la = e < cnt, lb = e + 1 < cnt;
                 const u64 mm = pk(la && ca != mynode ? qa.w : 0.f, lb && cb != mynode ? qb.w : 0.f);
-                const u64 vx = mul2(mm, fma2(dx, mt, mul2(gx2, inv3)));
-                const u64 vy = mul2(mm, fma2(dy, mt, mul2(gy2, inv3)));
-                const u64 vz = mul2(mm, fma2(dz, mt, mul2(gz2, inv3)));
+                const u64 mi3 = mul2(mul2(mm, inv), inv2);  // m r^-3, grouped as in the forward walk
+                const u64 vx = mul2(mi3, fma2(ex, m3eg, gx2));
+                const u64 vy = mul2(mi3, fma2(ey, m3eg, gy2));
+                const u64 vz = mul2(mi3, fma2(ez, m3eg, gz2));
                 ox = add2(ox, vx);
                 oy = add2(oy, vy);
                 oz = add2(oz, vz);
@@ -249,7 +252,7 @@ __global__ void __launch_bounds__(kAdjWarps * 32)
                 upk(vx, xa, xb);
                 upk(vy, ya, yb);
                 upk(vz, za, zb);
-                upk(mul2(dg, inv3), ma, mb);
+                upk(mul2(eg, inv2), ma, mb);  // (d.g) r^-3
                 red[w][4 * e + 0][lane] = xa;
                 red[w][4 * e + 1][lane] = ya;
                 red[w][4 * e + 2][lane] = za;
