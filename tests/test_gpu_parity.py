@@ -186,7 +186,7 @@ def test_update_bit_exact(cuda):
 
 
 def test_batched_equals_unbatched(cuda):
-    sizes = [1024, 37, 3000, 5, 2048, 777]
+    sizes = [1024, 37, 1, 3000, 5, 2, 2048, 777]
     parts = [ic.star_disk(k, seed=ic.SEED0 + 1 + i) for i, k in enumerate(sizes)]
     off = np.concatenate([[0], np.cumsum(sizes)])
     cat = lambda k: np.concatenate([getattr(p, k) for p in parts])  # noqa: E731
@@ -309,7 +309,7 @@ def test_batched_equals_unbatched_hilbert(cuda):
     """Hilbert keys (key_order 1): each system of a batch equals its own
     single-system run bit for bit (keys, tree and forces)."""
     from nns_gb300.barnes_hut import Context
-    sizes = [3000, 41, 5000, 700]
+    sizes = [3000, 41, 1, 5000, 2, 700]
     parts = [ic.plummer(k, seed=ic.SEED0 + 60 + i) for i, k in enumerate(sizes)]
     off = np.concatenate([[0], np.cumsum(sizes)])
     cat = lambda k: np.concatenate([getattr(p, k) for p in parts])  # noqa: E731
