@@ -673,6 +673,9 @@ def hbm_roofline(n: int, integ_ms: float, peaks: dict) -> dict:
     for a multiple of 4 bodies, bracketed alone by the integrate phase events):
     36 B read + 24 B written per body against the measured copy bandwidth."""
     peak = peaks.get("hbm_gbs")
+    if not integ_ms > 0:
+        return {"bound": "hbm", "kernel": "k_update4", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None,
+                "bytes_per_body": 60, "note": "the integrate phase was not timed"}
     achieved = 60.0 * n / (integ_ms * 1e-3) / 1e9
     return {"bound": "hbm", "kernel": "k_update4", "achieved": round(achieved, 1),
             "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if peak else None,
@@ -810,6 +813,10 @@ def main():
                     ncells=info["ncells"], max_level=info["max_level"])
 
     def timed_split(nsteps):
+        """Steps of the key-range split, phases timed with CUDA events on this
+        rank: build, this rank's walk plus the acceleration all-reduce (and the
+        group-cost all-reduce that rebalances the ranges), integrate."""
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(nsteps)]
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
         launches0 = ctx.tree_info()["launches"]
@@ -817,10 +824,15 @@ def main():
         torch.cuda.synchronize()
         t0.record()
         inter = 0
-        for _ in range(nsteps):
-            split.forces()
+        for k in range(nsteps):
+            ev[k][0].record()
+            ctx.build(s)
+            ev[k][1].record()
+            split.forces(build=False)
+            ev[k][2].record()
             inter += ctx.tree_info()["interactions"]  # this rank's groups
             ctx.integrate(s)
+            ev[k][3].record()
         t1.record()
         torch.cuda.synchronize()
         torch.distributed.barrier()
@@ -828,7 +840,9 @@ def main():
         info = ctx.tree_info()
         from nns_gb300.dist import sum_over_ranks
         inter = int(sum_over_ranks(float(inter), device="cuda")) // max(nsteps, 1)
-        return dict(ms=total, build_ms=0.0, walk_ms=total, integ_ms=0.0, interactions=inter, opened=0,
+        return dict(ms=total, build_ms=sum(e[0].elapsed_time(e[1]) for e in ev),
+                    walk_ms=sum(e[1].elapsed_time(e[2]) for e in ev),
+                    integ_ms=sum(e[2].elapsed_time(e[3]) for e in ev), interactions=inter, opened=0,
                     rounds=0, candidates=0, launches=info["launches"] - launches0, ncells=info["ncells"],
                     max_level=info["max_level"])
 
@@ -942,6 +956,10 @@ def main():
     max_mhz = peaks.get("sm_max_mhz") or clocks.get("sm_max_mhz") or 2070.0
     peak = peak_fp32_tflops(nsm, max_mhz)
     achieved = flops / (walk_ms * 1e-3) / 1e12
+    if world > 1:
+        # the interactions are summed over the ranks, each walking its share on its own GPU: per GPU
+        from nns_gb300.dist import max_over_ranks
+        achieved = flops / (max_over_ranks(walk_ms, device="cuda") * 1e-3) / 1e12 / world
     steps_per_s = 1000.0 / ms_plain
 
     if world > 1:
@@ -1025,8 +1043,10 @@ def main():
         "tree": {"cells": plain["ncells"], "max_level": plain["max_level"]},
         "roofline": {"bound": "fp32", "kernel": "k_walk2", "achieved": round(achieved, 3),
                      "peak": round(peak, 2), "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
-                     "traffic": walk_traffic(n),
-                     "peak_kind": "nominal FP32 FMA peak (SMs x 128 x 2 x max SM clock %g MHz)" % max_mhz},
+                     "traffic": walk_traffic(n) if world == 1 else None,
+                     "peak_kind": "nominal FP32 FMA peak (SMs x 128 x 2 x max SM clock %g MHz)" % max_mhz,
+                     **({"note": "per GPU: each rank walks its key range; the walk phase includes the "
+                                 "acceleration and group-cost all-reduces"} if world > 1 else {})},
         "roofline_hbm": hbm_roofline(n, plain["integ_ms"] / args.steps, peaks),
         "diagnostics_fp64": {"momentum_drift": float(np.abs(diag1["momentum"] - diag0["momentum"]).max()),
                              "kinetic_rel_change": float((diag1["kinetic"] - diag0["kinetic"]) / diag0["kinetic"])},

@@ -119,10 +119,13 @@ class SplitSystem:
         b = self.bounds
         return int(b[self.rank]), int(b[self.rank + 1] - b[self.rank])
 
-    def forces(self):
+    def forces(self, build: bool = True):
+        """One force evaluation; build=False when the caller has just built the
+        tree of the current positions itself (to time the phases apart)."""
         import torch
         ctx, s = self.ctx, self.s
-        ctx.build(s)
+        if build:
+            ctx.build(s)
         if self.bounds is None:
             self.bounds = split_groups(np.ones(ctx.group_count()), self.world)
         for t in (s.ax, s.ay, s.az):

@@ -36,6 +36,9 @@ def test_hbm_roofline_arithmetic():
     assert abs(r["achieved"] - 60.0 * (1 << 24) / 0.2e-3 / 1e9) < 0.1
     assert abs(r["frac"] - r["achieved"] / 6000.0) < 1e-3
     assert bench.hbm_roofline(1 << 20, 0.1, {})["frac"] is None
+    # an untimed integrate phase gives no figure instead of a division by zero
+    r0 = bench.hbm_roofline(1 << 20, 0.0, {"hbm_gbs": 6000.0})
+    assert r0["achieved"] is None and r0["frac"] is None
 
 
 def test_failing_section_is_reported_not_raised():
