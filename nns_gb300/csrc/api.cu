@@ -109,7 +109,7 @@ void free_all(Ctx *ctx) {
                     ctx->d_ent, ctx->d_ent_alt, ctx->d_flags, ctx->d_node4, ctx->d_meta, ctx->d_parent,
                     ctx->d_sums, ctx->d_count, ctx->d_arrive, ctx->d_lvl8, ctx->d_fcl, ctx->d_cl, ctx->d_hist,
                     ctx->d_scan_blk, ctx->d_totals, ctx->d_totals64, ctx->d_status, ctx->d_m2, ctx->d_quad4,
-                    ctx->d_quad2};
+                    ctx->d_quad2, ctx->d_seg_slot, ctx->d_lb_counts, ctx->d_lb_status, ctx->d_lb};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
@@ -289,6 +289,7 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     rc |= nbx::dmalloc(ctx, &ctx->d_body_sys, B);
     rc |= nbx::dmalloc(ctx, &ctx->d_tiles, ctx->cap_tiles_body);
     rc |= nbx::dmalloc(ctx, &ctx->d_sys_tiles, Ss);
+    rc |= nbx::dmalloc(ctx, &ctx->d_seg_slot, Ss);
     rc |= nbx::dmalloc(ctx, &ctx->d_groups, G);
     rc |= nbx::dmalloc(ctx, &ctx->d_bbox_u, 6 * Ss + 6);
     rc |= nbx::dmalloc(ctx, &ctx->d_bbox, 6 * Ss);
@@ -321,6 +322,11 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     rc |= nbx::dmalloc(ctx, &ctx->d_fcl, (size_t)NC + Ss + 2);
     rc |= nbx::dmalloc(ctx, &ctx->d_cl, (size_t)NC + Ss + 2);
     rc |= nbx::dmalloc(ctx, &ctx->d_hist, hist + 1);  // + the scanned total
+    // one-sweep body sort: a system of several tiles takes at least two, so at most
+    // half the tiles (plus one) hold count slots; status words per tile and digit
+    rc |= nbx::dmalloc(ctx, &ctx->d_lb_counts, (size_t)(ctx->cap_tiles_body / 2 + 1) * nbx::kLbMaxCounts);
+    rc |= nbx::dmalloc(ctx, &ctx->d_lb_status, (size_t)ctx->cap_tiles_body << nbx::kMaxRadixBits);
+    rc |= nbx::dmalloc(ctx, &ctx->d_lb, 16);
     rc |= nbx::dmalloc(ctx, &ctx->d_scan_blk, ctx->cap_scan_blk);
     rc |= nbx::dmalloc(ctx, &ctx->d_totals, 8);
     rc |= nbx::dmalloc(ctx, &ctx->d_totals64, 4);
@@ -328,6 +334,10 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     if (rc == 0 && cudaMallocHost((void **)&ctx->h_status, sizeof(nbx::DevStatus)) != cudaSuccess) rc = NBX_ERR_NOMEM;
     if (rc == 0 && cudaMemset(ctx->d_status, 0, sizeof(nbx::DevStatus)) != cudaSuccess) rc = NBX_ERR_CUDA;
     if (rc == 0 && cudaMemset(ctx->d_totals, 0, 8 * sizeof(unsigned)) != cudaSuccess) rc = NBX_ERR_CUDA;
+    // status words start at build 0, which no pass ever uses (its tags are >= 1)
+    if (rc == 0 && cudaMemset(ctx->d_lb_status, 0, sizeof(unsigned long long) * ((size_t)ctx->cap_tiles_body << nbx::kMaxRadixBits)) != cudaSuccess)
+        rc = NBX_ERR_CUDA;
+    if (rc == 0 && cudaMemset(ctx->d_lb, 0, 16 * sizeof(unsigned)) != cudaSuccess) rc = NBX_ERR_CUDA;
     if (rc == 0 && ctx->multipole) rc = nbx::alloc_quadrupoles(ctx);
     if (rc == 0) rc = nbx::walk_init(ctx);
     if (rc == 0) rc = nbx::radix_init(ctx);
@@ -454,12 +464,15 @@ int nbx_set_systems(nbx_ctx *c, int nsys, const int64_t *offsets) {
     std::vector<int> off(nsys + 1);
     std::vector<int4> tiles;
     std::vector<int2> st(nsys);
+    std::vector<int> slot(nsys);
     std::vector<int> groups;
+    int nslots = 0;
     for (int s = 0; s <= nsys; s++) off[s] = (int)offsets[s];
     for (int s = 0; s < nsys; s++) {
         const int beg = off[s], end = off[s + 1];
         const int nt = nbx::ceil_div(end - beg, tile);
         st[s] = make_int2((int)tiles.size(), nt);
+        slot[s] = nt > 1 ? nslots++ : -1;
         for (int t = 0; t < nt; t++) {
             const int a = beg + t * tile;
             const int len = (end - a) < tile ? (end - a) : tile;
@@ -471,6 +484,7 @@ int nbx_set_systems(nbx_ctx *c, int nsys, const int64_t *offsets) {
     NBX_CUDA(cudaMemcpy(ctx->d_sys_off, off.data(), sizeof(int) * (nsys + 1), cudaMemcpyHostToDevice));
     NBX_CUDA(cudaMemcpy(ctx->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice));
     NBX_CUDA(cudaMemcpy(ctx->d_sys_tiles, st.data(), sizeof(int2) * nsys, cudaMemcpyHostToDevice));
+    NBX_CUDA(cudaMemcpy(ctx->d_seg_slot, slot.data(), sizeof(int) * nsys, cudaMemcpyHostToDevice));
     NBX_CUDA(cudaMemcpy(ctx->d_groups, groups.data(), sizeof(int) * groups.size(), cudaMemcpyHostToDevice));
     nbx::k_body_sys<<<nbx::ceil_div(n, 256) < 4096 ? nbx::ceil_div(n, 256) : 4096, 256>>>(ctx->d_sys_off, nsys, n,
                                                                                           ctx->d_body_sys);
@@ -480,6 +494,7 @@ int nbx_set_systems(nbx_ctx *c, int nsys, const int64_t *offsets) {
     ctx->nsys = nsys;
     ctx->nbodies = n;
     ctx->ntiles_body = (int)tiles.size();
+    ctx->nslots = nslots;
     ctx->tile_body = tile;
     ctx->ngroups = (int)groups.size();
     ctx->built = false;

@@ -31,6 +31,9 @@ inline int tile_for(long long n, int nsm) {
 constexpr int kMaxRadixBits = 9;  // body-key digits: 8 or 9 bits (histograms sized for 9)
 // LSD passes over the 63-bit body keys for a digit width
 constexpr int radix_passes(int bits) { return (63 + bits - 1) / bits; }
+// one-sweep body sort: digit counts per system and build, the larger of
+// 8 passes x 256 digits and 7 passes x 512
+constexpr int kLbMaxCounts = 3584;
 constexpr int kMaxLevel = 43;     // 42 key levels + the body level
 constexpr int kBodyFlag = int(0x80000000u);
 constexpr int kLevelShift = 26;   // build node entry = level << 26 | sorted position
@@ -79,6 +82,8 @@ struct Ctx {
     int *d_body_sys = nullptr;      // [B] system of original index
     int4 *d_tiles = nullptr;        // [tiles] start, len, sys, local tile index
     int2 *d_sys_tiles = nullptr;    // [S] tile base, ntiles
+    int *d_seg_slot = nullptr;      // [S] one-sweep sort: count slot of a system of several tiles, else -1
+    int nslots = 0;                 // systems of several tiles (count slots in use)
     int *d_groups = nullptr;        // [G] first sorted position of each walk group
 
     // per-system tree parameters
@@ -120,6 +125,9 @@ struct Ctx {
 
     // radix + scan scratch
     unsigned *d_hist = nullptr;        // [2^kMaxRadixBits * max(tiles)]
+    unsigned *d_lb_counts = nullptr;   // [slots][passes][digits] one-sweep sort: digit counts of each system
+    unsigned long long *d_lb_status = nullptr;  // [tiles][2^kMaxRadixBits] look-back status words
+    unsigned *d_lb = nullptr;          // [16] build counter, next tile of each pass
     unsigned long long *d_scan_blk = nullptr;  // block sums
     unsigned *d_totals = nullptr;      // [8] device-side totals: 0 entries, 1 cells+first..., etc
     unsigned long long *d_totals64 = nullptr;
