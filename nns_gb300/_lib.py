@@ -84,6 +84,7 @@ SIGNATURES = {
     "nbx_step": (_I, [_P, C.POINTER(nbx_state), _I, _P]),
     "nbx_graph_step": (_I, [_P, C.POINTER(nbx_state), _I, _P]),
     "nbx_sync_status": (_I, [_P, _P]),
+    "nbx_selftest_sort_wait": (_I, [_P, _P]),
     "nbx_get_tree_info": (_I, [_P, _P, C.POINTER(nbx_tree_info)]),
     "nbx_export_tree": (_I, [_P, _I] + [_P] * 10 + [_I, C.POINTER(C.c_int64), _P]),
     "nbx_export_keys": (_I, [_P, _P, _P, _P]),

@@ -275,6 +275,9 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     // a tile below kTile is only chosen while there are fewer than 2 * want tiles
     const int want_tiles = 2 * ctx->nsm * nbx::kScatterWarps;
     ctx->cap_tiles_body = (B / nbx::kTile > 2 * want_tiles ? B / nbx::kTile : 2 * want_tiles) + Ss + 1;
+    // no tile is smaller than kTileMin: a small context never needs more tiles than this
+    const int64_t most_tiles = (int64_t)B / nbx::kTileMin + Ss + 1;
+    if (most_tiles < ctx->cap_tiles_body) ctx->cap_tiles_body = (int)most_tiles;
     ctx->tile_node = nbx::tile_for(ctx->cap_nodes, ctx->nsm);
     ctx->cap_tiles_node = nbx::ceil_div(ctx->cap_nodes, ctx->tile_node);
     const int64_t hist = (1ll << nbx::kMaxRadixBits) * (ctx->cap_tiles_body > ctx->cap_tiles_node ? ctx->cap_tiles_body : ctx->cap_tiles_node);
@@ -746,6 +749,13 @@ int nbx_graph_step(nbx_ctx *c, const nbx_state *s, int nsteps, void *stream) {
     if (!s->vx || !s->ax) return NBX_ERR_ARG;
     if (capturing(S(stream))) return NBX_ERR_ARG;  // a captured step cannot be nested in a capture
     return replay_steps(ctx, s, nsteps, S(stream));
+}
+
+int nbx_selftest_sort_wait(nbx_ctx *c, void *stream) {
+    if (!c) return NBX_ERR_ARG;
+    cudaStream_t st = S(stream);
+    if (capturing(st)) return NBX_ERR_ARG;
+    return nbx::radix_selftest_wait(C(c), st);
 }
 
 int nbx_sync_status(nbx_ctx *c, void *stream) {

@@ -207,6 +207,7 @@ int scan_exclusive_u64(Ctx *ctx, const unsigned long long *in, unsigned long lon
 int radix_sort_bodies(Ctx *ctx, cudaStream_t st);
 int radix_sort_entries(Ctx *ctx, cudaStream_t st);
 int radix_init(Ctx *ctx);
+int radix_selftest_wait(Ctx *ctx, cudaStream_t st);
 // tree.cu
 int build_tree(Ctx *ctx, const nbx_state *s, cudaStream_t st, bool external_bbox,
                const float *const *bbox_ptrs);

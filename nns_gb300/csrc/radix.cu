@@ -22,6 +22,8 @@
 // body keys in one launch per pass instead (k_radix_counts once, then the same
 // scatter kernel in its one-sweep form, whose tiles find their offsets by
 // decoupled look-back); the permutation is the same.
+#include <cstring>
+
 #include "nbx_internal.cuh"
 
 namespace nbx {
@@ -539,6 +541,50 @@ int radix_sort_entries(Ctx *ctx, cudaStream_t st) {
                                          tm, 24, st);
     NBX_CUDA(cudaGetLastError());
     return NBX_OK;
+}
+
+// Self-test of the one-sweep pass's bounded wait (nbx_selftest_sort_wait): a
+// system of two 256-key tiles on scratch of its own, whose tile counter starts
+// at 1, so the one block takes the second tile, publishes its counts and waits
+// for the first tile's, which nothing writes.
+int radix_selftest_wait(Ctx *ctx, cudaStream_t st) {
+    constexpr int kT = 256, kN = 2 * kT;
+    struct Scratch {
+        int4 tiles[2];
+        int2 seg_tiles[1];
+        int seg_slot[1];
+        unsigned lb[16];
+        unsigned counts[kLbMaxCounts];
+        unsigned long long status[2 << kMaxRadixBits];
+        unsigned long long key_in[kN], key_out[kN];
+        int val_in[kN], val_out[kN];
+    };
+    Scratch *d = nullptr;
+    NBX_CUDA(cudaMalloc(&d, sizeof(Scratch)));
+    Scratch h;
+    std::memset(&h, 0, sizeof(h));
+    h.tiles[0] = make_int4(0, kT, 0, 0);
+    h.tiles[1] = make_int4(kT, kT, 0, 1);
+    h.seg_tiles[0] = make_int2(0, 2);
+    h.seg_slot[0] = 0;
+    h.lb[0] = 1;  // build counter: status tags of 1 * 16 + pass + 1, none of them written
+    h.lb[1] = 1;  // the pass's next tile: the second
+    h.counts[0] = kN;  // every key (0) has digit 0 in every pass
+    int rc = NBX_OK;
+    if (cudaMemcpyAsync(d, &h, sizeof(Scratch), cudaMemcpyHostToDevice, st) != cudaSuccess) rc = NBX_ERR_CUDA;
+    if (rc == NBX_OK) {
+        TileMap tm{d->tiles, d->seg_tiles, nullptr, 2, kT};
+        SweepArgs sw{d->seg_slot, d->counts, d->status, d->lb, d->lb, ctx->d_status, 0, kN};
+        k_radix_scatter<unsigned long long, int, true, 8, true>
+            <<<1, kScatterWarps * 32, stage_bytes<unsigned long long, int, 8, true>(kT), st>>>(
+                d->key_in, d->key_out, d->val_in, d->val_out, tm, 0, nullptr, sw);
+        ++ctx->launches;
+        if (cudaGetLastError() != cudaSuccess) rc = NBX_ERR_CUDA;
+    }
+    // the scratch (and the host copy) outlive the pass
+    if (cudaStreamSynchronize(st) != cudaSuccess) rc = NBX_ERR_CUDA;
+    cudaFree(d);
+    return rc;
 }
 
 int radix_init(Ctx *ctx) {

@@ -835,3 +835,32 @@ def test_compensated_adversarial_geometry(cuda, name, mode):
     mag = np.linalg.norm(f.a64, axis=1)
     assert np.median(_rel(a, f.a64)) <= MED_TOL
     assert (err <= MAX_TOL * (mag + np.median(mag))).all(), (err / (mag + np.median(mag))).max()
+
+
+def test_sort_wait_runs_out_and_reports(cuda):
+    """The bounded wait of the small-context sort (one-sweep passes): the
+    self-test runs one pass whose tile waits for an earlier tile that never
+    runs.  The wait gives up within a few seconds, NBX_ERR_TIMEOUT is reported
+    once and cleared, and the same context then builds and walks a system
+    bit-exactly against the oracle."""
+    import time
+    from nns_gb300._lib import lib
+    b = ic.star_disk(4096)
+    n = len(b.x)
+    ctx = _ctx(n, theta=0.5, eps=0.01)
+    ctx.set_systems([0, n])
+    t0 = time.time()
+    assert lib().nbx_selftest_sort_wait(ctx.h, None) == 0
+    assert time.time() - t0 < 30
+    assert lib().nbx_sync_status(ctx.h, None) == 8  # NBX_ERR_TIMEOUT
+    assert lib().nbx_sync_status(ctx.h, None) == 0
+    s = _state(b)
+    ctx.build(s)
+    ctx.forces(s)
+    ctx.sync()
+    ot = O.build(b.x, b.y, b.z, b.m)
+    _check_tree(ctx.export_tree(0), ot)
+    t, e2 = ctx.constants()
+    f = O.forces(b.x, b.y, b.z, b.m, ot, t, e2)
+    nl, _ = ctx.walk_stats()
+    assert np.array_equal(nl, f.nlist)

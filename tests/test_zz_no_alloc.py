@@ -88,13 +88,17 @@ def test_noalloc_bounding_box_rejects_oversized_grid(cuda):
 
 def test_noalloc_bounding_box_allocates_nothing(cuda):
     """The property the entry point exists for: after a first call (which may load
-    the module), calls of several sizes leave the device's free memory unchanged."""
+    the module), calls of several sizes leave the device's free memory unchanged.
+    Contexts of earlier tests are collected first, so that none is freed while
+    the calls are measured."""
+    import gc
     import torch
     from nns_gb300._lib import lib
     L = lib()
     sets = [_bodies(n, ic.SEED0 + 10 + j, 0.5 * j) for j, n in enumerate((1 << 18, 3000, 1 << 16))]
     out = _box(0.0)
     assert _noalloc_box(L, sets[0], out) == 0  # warm-up
+    gc.collect()
     torch.cuda.synchronize()
     free0 = torch.cuda.mem_get_info()[0]
     for xyz in sets * 3:
