@@ -129,7 +129,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 // scanned histogram (the layout is tile-minor and the scan is continuous;
 // offs[nh] holds the total).  Shared memory per block: gbase (output offset of
 // (digit, tile)), lstart (tile-local start of the digit), the warps' counters,
-// then the tile's keys and values.
+// then (one-sweep form) the system's start of each digit, then the tile's keys
+// and values.
 template <typename K, typename V, int Bits, bool Sweep = false>
 __host__ __device__ constexpr size_t stage_bytes(int tile) {
     return ((2 + kScatterWarps + (Sweep ? 1 : 0)) * (size_t(1) << Bits) * sizeof(unsigned) +
@@ -149,7 +150,7 @@ __host__ __device__ constexpr size_t stage_bytes(int tile) {
 // themselves.  Every wait is bounded (NBX_ERR_TIMEOUT).
 constexpr unsigned long long kLbAgg = 1ull << 30, kLbPrefix = 1ull << 31;
 constexpr unsigned kLbCountMask = (1u << 30) - 1u;
-constexpr int kLbSpins = 1 << 20;  // polls of one status word before giving up (about 30 ms at 32 ns)
+constexpr int kLbSpins = 1 << 20;  // polls of one status word before giving up (an L2 load each: under a second)
 
 struct SweepArgs {
     const int *seg_slot;          // count slot of each system (-1: the system is one tile)
