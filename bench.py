@@ -710,6 +710,26 @@ def walk_traffic(n: int):
     return traffic
 
 
+def bench_graph_steps(ctx, s, steps: int) -> dict:
+    """The same plain steps replayed from a CUDA graph captured once
+    (nbx_graph_step), timed with CUDA events after a warm-up replay: graph-
+    launched steps/s beside the eager steps of `value` (at this size the launch
+    overhead the graph removes is a small share of a step)."""
+    import torch
+    ctx.graph_step(s, 2)  # capture and warm up
+    ctx.sync()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    ctx.graph_step(s, steps)
+    e1.record()
+    torch.cuda.synchronize()
+    ctx.sync()
+    ms = e0.elapsed_time(e1) / steps
+    return {"value": round(1000.0 / ms, 4), "unit": "steps/s", "ms_per_step": round(ms, 3), "steps": steps}
+
+
 def bench_frame(ctx, s, b, reps: int = 5) -> dict:
     """One headless frame of the current state with the reference renderer's
     constants (1024 x 1024, dot 8; system size from the initial state, as
@@ -945,6 +965,7 @@ def main():
     e2e_ms = e0.elapsed_time(e1) / args.steps
     ctx.sync()
     frame = bench_frame(ctx, s, b)
+    graph = _section(bench_graph_steps, ctx, s, args.steps) if world == 1 else None
 
     ms_plain = plain["ms"] / args.steps
     ms_comp = comp["ms"] / args.steps
@@ -1053,6 +1074,7 @@ def main():
         "e2e": {"value": round(1000.0 / e2e_ms, 4), "unit": "steps/s", "h2d_bytes_per_step": h2d,
                 "pipeline": "two device states: the copies of one step overlap the compute of the other",
                 "d2h_bytes_per_step": d2h},
+        "graph": graph,
         "hilbert": hilbert,
         "configs": configs,
         "buckets": buckets,
