@@ -14,7 +14,10 @@ namespace nbx {
 #define NBX_TILE 2048
 #endif
 constexpr int kTile = NBX_TILE;   // keys per radix tile (one warp)
-constexpr int kTileMin = 256;     // smallest radix tile (small systems)
+#ifndef NBX_TILE_MIN
+#define NBX_TILE_MIN 256
+#endif
+constexpr int kTileMin = NBX_TILE_MIN;  // smallest radix tile (small systems)
 #ifndef NBX_SCATTER_WARPS
 #define NBX_SCATTER_WARPS 4
 #endif
