@@ -238,10 +238,11 @@ int nbx_sync_status(nbx_ctx *ctx, void *stream);
 /* Self-test of the bounded wait in the small-context sort (one-sweep passes,
  * whose tiles wait for the counts of their system's earlier tiles): one pass
  * over the second tile of a two-tile system whose first tile never runs, on
- * scratch of its own.  Its wait gives up after about a second and records
- * NBX_ERR_TIMEOUT in the context's device status, which the next
- * nbx_sync_status returns and clears; the context stays usable.  Writes
- * nothing outside its scratch. */
+ * scratch of its own.  Its wait gives up within a second and records
+ * NBX_ERR_TIMEOUT in the context's device status (which keeps the first error
+ * recorded: call it with no error pending), which the next nbx_sync_status
+ * returns and clears; the context stays usable.  Writes nothing outside its
+ * scratch. */
 int nbx_selftest_sort_wait(nbx_ctx *ctx, void *stream);
 /* synchronises and reports the last build/walk */
 int nbx_get_tree_info(nbx_ctx *ctx, void *stream, nbx_tree_info *out);
