@@ -109,7 +109,8 @@ void free_all(Ctx *ctx) {
                     ctx->d_ent, ctx->d_ent_alt, ctx->d_flags, ctx->d_node4, ctx->d_meta, ctx->d_parent,
                     ctx->d_sums, ctx->d_count, ctx->d_arrive, ctx->d_lvl8, ctx->d_fcl, ctx->d_cl, ctx->d_hist,
                     ctx->d_scan_blk, ctx->d_totals, ctx->d_totals64, ctx->d_status, ctx->d_m2, ctx->d_quad4,
-                    ctx->d_quad2, ctx->d_seg_slot, ctx->d_lb_counts, ctx->d_lb_status, ctx->d_lb};
+                    ctx->d_quad2, ctx->d_seg_slot, ctx->d_lb_counts, ctx->d_lb_status, ctx->d_lb, ctx->d_tiles_sw,
+                    ctx->d_sys_tiles_sw};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
@@ -293,6 +294,8 @@ int nbx_create(const nbx_params *p, nbx_ctx **out) {
     rc |= nbx::dmalloc(ctx, &ctx->d_tiles, ctx->cap_tiles_body);
     rc |= nbx::dmalloc(ctx, &ctx->d_sys_tiles, Ss);
     rc |= nbx::dmalloc(ctx, &ctx->d_seg_slot, Ss);
+    rc |= nbx::dmalloc(ctx, &ctx->d_tiles_sw, ctx->cap_tiles_body);
+    rc |= nbx::dmalloc(ctx, &ctx->d_sys_tiles_sw, Ss);
     rc |= nbx::dmalloc(ctx, &ctx->d_groups, G);
     rc |= nbx::dmalloc(ctx, &ctx->d_bbox_u, 6 * Ss + 6);
     rc |= nbx::dmalloc(ctx, &ctx->d_bbox, 6 * Ss);
@@ -464,9 +467,12 @@ int nbx_set_systems(nbx_ctx *c, int nsys, const int64_t *offsets) {
     if (offsets[nsys] > ctx->cap_bodies) return NBX_ERR_ARG;
     const int n = (int)offsets[nsys];
     const int tile = nbx::tile_for(n, ctx->nsm);
+    // the one-sweep sort's tiling: its passes are bound by the look-back chains
+    // between a system's tiles, so its tiles are at least kTileSweep keys
+    const int tile_sw = tile > nbx::kTileSweep ? tile : (nbx::kTileSweep < nbx::kTile ? nbx::kTileSweep : nbx::kTile);
     std::vector<int> off(nsys + 1);
-    std::vector<int4> tiles;
-    std::vector<int2> st(nsys);
+    std::vector<int4> tiles, tiles_sw;
+    std::vector<int2> st(nsys), st_sw(nsys);
     std::vector<int> slot(nsys);
     std::vector<int> groups;
     int nslots = 0;
@@ -475,19 +481,28 @@ int nbx_set_systems(nbx_ctx *c, int nsys, const int64_t *offsets) {
         const int beg = off[s], end = off[s + 1];
         const int nt = nbx::ceil_div(end - beg, tile);
         st[s] = make_int2((int)tiles.size(), nt);
-        slot[s] = nt > 1 ? nslots++ : -1;
         for (int t = 0; t < nt; t++) {
             const int a = beg + t * tile;
             const int len = (end - a) < tile ? (end - a) : tile;
             tiles.push_back(make_int4(a, len, s, t));
         }
+        const int nts = nbx::ceil_div(end - beg, tile_sw);
+        st_sw[s] = make_int2((int)tiles_sw.size(), nts);
+        slot[s] = nts > 1 ? nslots++ : -1;
+        for (int t = 0; t < nts; t++) {
+            const int a = beg + t * tile_sw;
+            const int len = (end - a) < tile_sw ? (end - a) : tile_sw;
+            tiles_sw.push_back(make_int4(a, len, s, t));
+        }
         for (int g = beg; g < end; g += 32) groups.push_back(g);
     }
-    if ((int)tiles.size() > ctx->cap_tiles_body) return NBX_ERR_ARG;
+    if ((int)tiles.size() > ctx->cap_tiles_body || (int)tiles_sw.size() > ctx->cap_tiles_body) return NBX_ERR_ARG;
     NBX_CUDA(cudaMemcpy(ctx->d_sys_off, off.data(), sizeof(int) * (nsys + 1), cudaMemcpyHostToDevice));
     NBX_CUDA(cudaMemcpy(ctx->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice));
     NBX_CUDA(cudaMemcpy(ctx->d_sys_tiles, st.data(), sizeof(int2) * nsys, cudaMemcpyHostToDevice));
     NBX_CUDA(cudaMemcpy(ctx->d_seg_slot, slot.data(), sizeof(int) * nsys, cudaMemcpyHostToDevice));
+    NBX_CUDA(cudaMemcpy(ctx->d_tiles_sw, tiles_sw.data(), sizeof(int4) * tiles_sw.size(), cudaMemcpyHostToDevice));
+    NBX_CUDA(cudaMemcpy(ctx->d_sys_tiles_sw, st_sw.data(), sizeof(int2) * nsys, cudaMemcpyHostToDevice));
     NBX_CUDA(cudaMemcpy(ctx->d_groups, groups.data(), sizeof(int) * groups.size(), cudaMemcpyHostToDevice));
     nbx::k_body_sys<<<nbx::ceil_div(n, 256) < 4096 ? nbx::ceil_div(n, 256) : 4096, 256>>>(ctx->d_sys_off, nsys, n,
                                                                                           ctx->d_body_sys);
@@ -498,6 +513,8 @@ int nbx_set_systems(nbx_ctx *c, int nsys, const int64_t *offsets) {
     ctx->nbodies = n;
     ctx->ntiles_body = (int)tiles.size();
     ctx->nslots = nslots;
+    ctx->ntiles_sw = (int)tiles_sw.size();
+    ctx->tile_sw = tile_sw;
     ctx->tile_body = tile;
     ctx->ngroups = (int)groups.size();
     ctx->built = false;

@@ -18,6 +18,10 @@ constexpr int kTile = NBX_TILE;   // keys per radix tile (one warp)
 #define NBX_TILE_MIN 256
 #endif
 constexpr int kTileMin = NBX_TILE_MIN;  // smallest radix tile (small systems)
+#ifndef NBX_TILE_SWEEP
+#define NBX_TILE_SWEEP 1024
+#endif
+constexpr int kTileSweep = NBX_TILE_SWEEP;  // smallest tile of the one-sweep sort (shorter look-back chains)
 #ifndef NBX_SCATTER_WARPS
 #define NBX_SCATTER_WARPS 4
 #endif
@@ -85,7 +89,11 @@ struct Ctx {
     int *d_body_sys = nullptr;      // [B] system of original index
     int4 *d_tiles = nullptr;        // [tiles] start, len, sys, local tile index
     int2 *d_sys_tiles = nullptr;    // [S] tile base, ntiles
-    int *d_seg_slot = nullptr;      // [S] one-sweep sort: count slot of a system of several tiles, else -1
+    // one-sweep sort (small contexts): its own tiling of at least kTileSweep keys
+    int4 *d_tiles_sw = nullptr;     // [tiles] start, len, sys, local tile index
+    int2 *d_sys_tiles_sw = nullptr; // [S] tile base, ntiles
+    int *d_seg_slot = nullptr;      // [S] count slot of a system of several tiles, else -1
+    int ntiles_sw = 0, tile_sw = 0;
     int nslots = 0;                 // systems of several tiles (count slots in use)
     int *d_groups = nullptr;        // [G] first sorted position of each walk group
 

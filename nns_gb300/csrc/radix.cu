@@ -18,10 +18,11 @@
 // Segments are the independent systems of a batch, so one launch sorts every
 // system's keys inside its own range; a single system is one segment.
 //
-// Small contexts (fewer than 2^18 bodies, 2^15 in a captured graph) sort their
-// body keys in one launch per pass instead (k_radix_counts once, then the same
-// scatter kernel in its one-sweep form, whose tiles find their offsets by
-// decoupled look-back); the permutation is the same.
+// Small and mid-size contexts (fewer than 1.5 x 2^20 bodies, 2^17 in a captured
+// graph) sort their body keys in one launch per pass instead (k_radix_counts
+// once, then the same scatter kernel in its one-sweep form on a tiling of its
+// own, whose tiles find their offsets by decoupled look-back); the permutation
+// is the same.
 #include <cstring>
 
 #include "nbx_internal.cuh"
@@ -38,18 +39,19 @@ constexpr int kWarpsPerBlock = 8;
 #define NBX_RADIX_SWEEP 1  // body keys: 1 one-sweep passes below the size switch, 0 always histogram + scan + scatter
 #endif
 #ifndef NBX_RADIX_SWEEP_MAX
-#define NBX_RADIX_SWEEP_MAX (1 << 18)
+#define NBX_RADIX_SWEEP_MAX (3 << 19)
 #endif
 #ifndef NBX_RADIX_SWEEP_MAX_GRAPH
-#define NBX_RADIX_SWEEP_MAX_GRAPH (1 << 15)
+#define NBX_RADIX_SWEEP_MAX_GRAPH (1 << 17)
 #endif
-// One-sweep passes below this many bodies (over all systems): they save four
-// launches per pass, which is what small builds spend their time on.  Eager
-// builds: 4096 bodies 0.20 against 0.24 ms, 65536 0.32 against 0.37; from 2^18
-// on the counts pass and the look-back cost more than the launches (2^19: 0.69
-// against 0.59 ms, 2^24: 5.78 against 5.42 ms).  In a captured graph a launch
-// costs less, and the switch comes earlier: whole graph-replayed steps of 16384
-// bodies 0.325 against 0.361 ms, of 65536 0.453 against 0.438.
+// One-sweep passes below this many bodies (over all systems).  They save four
+// launches per pass, and with their own tiling of at least kTileSweep keys the
+// look-back chains stay short.  Eager builds: 4096 bodies 0.20 against 0.24 ms,
+// 2^17 0.315 against 0.403, 2^20 0.711 against 0.755; from 2^21 the counts pass
+// and the look-back cost more than the launches (1.196 against 1.114 ms, 2^23
+// 3.14 against 2.97).  In a captured graph a launch costs less and the switch
+// comes earlier: whole graph-replayed steps of 65536 bodies 0.421 against 0.442
+// ms, of 2^17 equal.
 constexpr int kSweepMaxBodies = NBX_RADIX_SWEEP_MAX;
 constexpr int kSweepMaxBodiesGraph = NBX_RADIX_SWEEP_MAX_GRAPH;
 
@@ -451,8 +453,8 @@ int launch_scatter(Ctx *ctx, int nt, const K *kin, K *kout, const V *vin, V *vou
 // per pass.
 template <int Bits>
 int sort_bodies_sweep(Ctx *ctx, cudaStream_t st) {
-    TileMap tm{ctx->d_tiles, ctx->d_sys_tiles, nullptr, ctx->ntiles_body, ctx->tile_body};
-    const int nt = ctx->ntiles_body;
+    TileMap tm{ctx->d_tiles_sw, ctx->d_sys_tiles_sw, nullptr, ctx->ntiles_sw, ctx->tile_sw};
+    const int nt = ctx->ntiles_sw;
     if (nt == 0) return NBX_OK;
     constexpr int kBins = 1 << Bits, kPasses = radix_passes(Bits);
     unsigned long long *k0 = ctx->d_key, *k1 = ctx->d_key_alt;
@@ -464,8 +466,9 @@ int sort_bodies_sweep(Ctx *ctx, cudaStream_t st) {
     if (ctx->nslots > 0)
         NBX_CUDA(cudaMemsetAsync(ctx->d_lb_counts, 0, sizeof(unsigned) * (size_t)ctx->nslots * kPasses * kBins, st));
     const int cgrid = ctx->nslots > 0 ? (nt < 2 * ctx->nsm ? nt : 2 * ctx->nsm) : 1;
-    k_radix_counts<Bits><<<cgrid, 256, sizeof(unsigned) * kPasses * kBins, st>>>(k0, ctx->d_tiles, nt, ctx->d_seg_slot,
-                                                                                ctx->d_lb_counts, ctx->d_lb);
+    k_radix_counts<Bits><<<cgrid, 256, sizeof(unsigned) * kPasses * kBins, st>>>(k0, ctx->d_tiles_sw, nt,
+                                                                                ctx->d_seg_slot, ctx->d_lb_counts,
+                                                                                ctx->d_lb);
     ++ctx->launches;
     const size_t smem = stage_bytes<unsigned long long, int, Bits, true>(tm.tile);
     for (int pass = 0; pass < kPasses; pass++) {
