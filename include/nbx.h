@@ -235,8 +235,9 @@ int nbx_step(nbx_ctx *ctx, const nbx_state *s, int nsteps, void *stream);
 int nbx_graph_step(nbx_ctx *ctx, const nbx_state *s, int nsteps, void *stream);
 /* synchronises `stream` and returns (and clears) the sticky device status */
 int nbx_sync_status(nbx_ctx *ctx, void *stream);
-/* Self-test of the bounded wait in the one-sweep sort (one-sweep passes,
- * whose tiles wait for the counts of their system's earlier tiles): one pass
+/* Self-test of the bounded wait in the one-sweep body sort (contexts below
+ * 1.5 x 2^20 bodies; its tiles wait for the counts of their system's earlier
+ * tiles): one pass
  * over the second tile of a two-tile system whose first tile never runs, on
  * scratch of its own.  Its wait gives up within a second and records
  * NBX_ERR_TIMEOUT in the context's device status (which keeps the first error
